@@ -1,0 +1,375 @@
+"""Benchmark: sector solves/s for the flux-scan batch, versus the plain FP64 drop-in.
+
+Workload (default "flux_scan_haldane3x4"): hard-core bosons on a 3x4 Haldane
+honeycomb (24 sites, t=1, t'=0.6 e^{+-i0.4pi}, t''=-0.58), Np=6; every one of
+the 12 momentum sectors at each of an 8x8 grid of flux twists
+(theta/2pi in {0, 1/8, ..., 7/8}^2): 768 sector solves of dimension ~1.1e4,
+lowest 4 eigenvalues each.  One step = the whole 768-solve batch.
+  value : solves/s of the batched mixed-precision path (complex64 matvec, FP64
+          Lanczos + polish) with inputs resident in HBM, CUDA events;
+  e2e   : the same through the C ABI with host buffers (H2D of the request
+          parameters and D2H of the results inside the timed region);
+and beside them the plain FP64 drop-in (sed_solve on one sector at a time, the
+reference's call pattern), the FP64 batched path, |dE|/|E| of the mixed results
+against FP64, p50/p99 request latency, the kernel roofline and clocks.
+
+``--impl reference`` times the CPU restatement of the reference's matrix-free
+path (projection table + threaded _apply_table! + Lanczos, oracle/) on the host
+cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sector solves/s (flux-scan batch), mixed precision at |dE|/|E|<=1e-9"
+UNIT = "solves/s"
+WORKLOAD = "flux_scan_haldane3x4"
+
+
+def workload_requests(grid: int = 8):
+    from realspace_exactdiagonalization_gb300 import lattice as L
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.haldane_honeycomb(3, 4)
+    twists = [(a / grid, b / grid) for a in range(grid) for b in range(grid)]
+    return spec, twists, flux_scan_requests(spec, twists)
+
+
+def config(n_req, extra=None):
+    c = {"workload": WORKLOAD, "model": "haldane_honeycomb_3x4_hardcore_bosons", "n_site": 24, "n_particles": 6,
+         "sectors_per_step": n_req, "momenta": 12, "twist_grid": "8x8", "nev": 4, "tol": 1e-10,
+         "l2": "flushed between timed steps (256 MiB write)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        j = json.load(open(p))
+        return float(j["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args, rank):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    if rank != 0:
+        return
+    O.build()
+    spec, twists, reqs = workload_requests()
+    cores = O.max_threads()
+    from realspace_exactdiagonalization_gb300.groups import statistics_from_name
+
+    st = statistics_from_name(spec.statistics).code
+    G0 = reqs[0].group
+    cat = O.Catalog(G0.perm0(), G0.phases(), 0, st, spec.n_filled)
+    per_step = max(1, args.ref_sample)
+    # each step: a bounded sample of the batch, spread over twists and momenta
+    order = [(i * 97) % len(reqs) for i in range(len(reqs))]
+    pos = 0
+
+    def step():
+        nonlocal pos
+        n = 0
+        for _ in range(per_step):
+            b = order[pos % len(order)]
+            pos += 1
+            r = reqs[b]
+            cat.update_phases(r.group.phases())
+            sec = O.Sector(cat, r.irrep.array())
+            if sec.dim == 0:
+                continue
+            terms = [(i - 1, j - 1, t) for (i, j), t in zip(
+                [(i, j) for (i, j, _) in spec.bilinear_terms()], r.amplitudes)]
+            op = O.Op(sec, terms, [(i - 1, j - 1, v) for (i, j, v) in spec.density_terms])
+            res = op.solve(4, tol=1e-10, maxiter=300, krylovdim=30, seed=r.seed)
+            assert res["status"] == 0
+            n += 1
+        return n
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(args.steps):
+        done += step()
+    dt = time.perf_counter() - t0
+    v = done / dt
+    sample = f"{per_step} of the {len(reqs)} sector solves per step (spread over twists and momenta); " \
+             f"projection-table build + threaded table apply + thick-restart Lanczos, catalog excluded"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (generated lattice model)", "config": config(len(reqs), {"sample": sample}),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(n_solves=4):
+    """CPU restatement of the reference on the host cores, bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    spec, twists, reqs = workload_requests()
+    G0 = reqs[0].group
+    cat = O.Catalog(G0.perm0(), G0.phases(), 0, 0, spec.n_filled)
+    pairs = [(i, j) for (i, j, _) in spec.bilinear_terms()]
+    t0 = time.perf_counter()
+    done = 0
+    evals = {}
+    for b in [(i * 97) % len(reqs) for i in range(n_solves)]:
+        r = reqs[b]
+        cat.update_phases(r.group.phases())
+        sec = O.Sector(cat, r.irrep.array())
+        op = O.Op(sec, [(i - 1, j - 1, t) for (i, j), t in zip(pairs, r.amplitudes)], [])
+        res = op.solve(4, tol=1e-10, maxiter=300, krylovdim=30, seed=r.seed)
+        evals[b] = res["evals"]
+        done += 1
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+            "sample": f"{n_solves} of the {len(reqs)} sector solves (CPU restatement of the reference's matrix-free "
+                      f"path: projection table + threaded table apply + Lanczos)"}, evals
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, rank, world):
+    import torch
+
+    import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300.batched import BatchedSectorSolver
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    spec, twists, reqs = workload_requests()
+    n = len(reqs)
+    G0 = reqs[0].group
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G0,
+                                         particle_statistics=A.Bosonic())
+    pairs = [(i, j) for (i, j, _) in spec.bilinear_terms()]
+    solver = BatchedSectorSolver(cat, pairs, spec.density_terms, precision="mixed", nev=4, max_requests=n)
+    stream = torch.cuda.current_stream()
+    solver.set_stream(stream.cuda_stream)
+    chi, ph, amp, seeds = solver.pack(reqs)
+    # device-resident inputs and outputs
+    d = {k: torch.from_numpy(v.view(np.float64) if v.dtype == np.complex128 else v.view(np.int64)).cuda()
+         for k, v in (("chi", chi), ("ph", ph), ("amp", amp), ("seeds", seeds))}
+    out = {"ev": torch.zeros(n * 4, dtype=torch.float64, device="cuda"),
+           "st": torch.zeros(n, dtype=torch.int32, device="cuda"),
+           "dims": torch.zeros(n, dtype=torch.int64, device="cuda"),
+           "delta": torch.zeros(n, dtype=torch.float64, device="cuda"),
+           "nmv": torch.zeros(n, dtype=torch.int32, device="cuda")}
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        solver.run_device(n, d["chi"].data_ptr(), d["ph"].data_ptr(), d["amp"].data_ptr(), d["seeds"].data_ptr(),
+                          out["ev"].data_ptr(), out["st"].data_ptr(), out["dims"].data_ptr(),
+                          out["delta"].data_ptr(), out["nmv"].data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(dev) as clk:
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            times.append((e0, e1))
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in times]
+    tot_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([tot_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = world * n * args.steps / (tot_ms / 1e3)
+    st = out["st"].cpu().numpy()
+    ev_mixed = out["ev"].cpu().numpy().reshape(n, 4)
+    dims = out["dims"].cpu().numpy()
+    nmv = out["nmv"].cpu().numpy()
+    stats = solver.last_stats()
+    lat_ms = (stats["t_end_ns"] - stats["t_start_ns"].min()) / 1e6
+    if rank != 0:
+        return
+    assert (st == 0).all(), "unconverged requests in the batch"
+
+    # --- roofline of the batch kernel: algorithmic bytes of its matvecs
+    s = 8  # complex64 matvec input
+    b_mv = dims * (8 + 4 + 2 * s) + stats["hops"] * (4 + 1 + 4 + s)
+    bytes_launch = float((nmv * b_mv).sum())
+    achieved = bytes_launch / (tot_ms / args.steps / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+
+    # --- end to end through the C ABI with host buffers
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = solver.run_packed(chi, ph, amp, seeds)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    h2d = chi.nbytes + ph.nbytes + amp.nbytes + seeds.nbytes
+    d2h = n * (4 * 8 + 4 + 8 + 8 + 4)
+
+    # --- FP64 batched path and |dE|/|E| of the mixed results
+    solver64 = BatchedSectorSolver(cat, pairs, spec.density_terms, precision="fp64", nev=4, max_requests=n)
+    t0 = time.perf_counter()
+    r64 = solver64.run_packed(chi, ph, amp, seeds)
+    fp64_batch_s = time.perf_counter() - t0
+    ev64 = r64["evals"]
+    rel = np.abs(ev_mixed - ev64) / np.maximum(np.abs(ev64), 1e-300)
+    max_rel = float(np.nanmax(rel))
+
+    # --- plain FP64 drop-in: one sector at a time through sed_solve (sample)
+    n_plain = args.plain_sample
+    idx = [(i * 97) % n for i in range(n_plain)]
+    t0 = time.perf_counter()
+    plain_ev = {}
+    for b in idx:
+        rq = reqs[b]
+        A.update_orbit_stabilizer_phases_(cat, rq.group, A.Bosonic())
+        basis = A.build_symmetry_sector_basis(cat, rq.irrep)
+        H = A.MatrixFreeHamiltonian(basis, [(i, j, t) for (i, j), t in zip(pairs, rq.amplitudes)],
+                                    spec.density_terms)
+        vals, _, info = H.solve(4, tol=1e-10, seed=rq.seed, want_vectors=False)
+        plain_ev[b] = vals
+    plain_s = (time.perf_counter() - t0) / n_plain
+    plain_rate = 1.0 / plain_s
+    max_rel_plain = max(float(np.max(np.abs(ev_mixed[b] - plain_ev[b]) / np.abs(plain_ev[b]))) for b in idx)
+
+    cpu = None
+    if not args.no_cpu:
+        cpu, cpu_ev = cpu_baseline_sample(args.cpu_sample)
+        cpu["max_rel_dE_vs_gpu_fp64"] = max(float(np.max(np.abs(cpu_ev[b] - ev64[b]) / np.abs(ev64[b])))
+                                           for b in cpu_ev)
+
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 matvec / f64 Lanczos", "data": "synthetic (generated lattice model, seeded start vectors)",
+        "config": config(n, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
+        "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_batch (persistent batched Lanczos)",
+                     "bytes_per_launch": bytes_launch,
+                     "note": "algorithmic matvec bytes (D*(8+4+2s)+hops*(4+1+4+s), s=8) of all matvecs of one launch"},
+        "cpu_baseline": cpu,
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "plain_fp64_dropin": {"solves_per_s": plain_rate, "sample": n_plain,
+                              "p50_ms": 1e3 * plain_s * (n / 2 + 0.5), "p99_ms": 1e3 * plain_s * (0.99 * n + 1),
+                              "max_rel_dE_mixed_vs_plain": max_rel_plain},
+        "fp64_batched": {"solves_per_s": n / fp64_batch_s},
+        "speedup_vs_plain_fp64": value / plain_rate,
+        "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99))},
+        "max_rel_dE_mixed_vs_fp64": max_rel,
+        "dims": {"min": int(dims.min()), "max": int(dims.max())},
+        "matvecs_per_solve": float(nmv.mean()),
+        "wall_s_timed": t_wall,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--plain-sample", type=int, default=24)
+    ap.add_argument("--cpu-sample", type=int, default=6)
+    ap.add_argument("--ref-sample", type=int, default=4)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

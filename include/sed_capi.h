@@ -1,0 +1,194 @@
+/*
+ * sed_capi.h -- C ABI of the GB300 symmetry-sector exact-diagonalization
+ * library (libsed_gb300.so).
+ *
+ * Drop-in for the matrix-free hot path of the Julia package
+ * RealSpace_ExactDiagonalization v0.1.0 (SRE = src/symmetry_resolved_ed.jl).
+ * Each entry point names the reference function it replaces.  Conventions:
+ *   - plain C types only; caller-owned host buffers unless a flag says device;
+ *   - sites, group elements and sector rows are 0-based here (the reference is
+ *     1-based; readback fields it stores 1-based are returned 1-based);
+ *   - complex numbers are interleaved (re, im) doubles;
+ *   - every call returns an int status (0 = SED_OK); sed_last_error() returns
+ *     the message of the last failing call on the calling thread;
+ *   - one CUDA stream per object (sed_*_set_stream overrides it); calls on one
+ *     object are not thread-safe, distinct objects may be used concurrently.
+ * Objects hold shared references to what they were built from (an operator
+ * keeps its sector, catalog and group alive), so destroy order is free.
+ */
+#ifndef SED_CAPI_H
+#define SED_CAPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SED_API_VERSION 1
+
+/* status codes */
+#define SED_OK 0
+#define SED_ERR_ARG 1           /* invalid argument (the reference asserts or errors) */
+#define SED_ERR_CUDA 2          /* CUDA runtime failure */
+#define SED_ERR_NOMEM 3         /* device allocation failed / over budget */
+#define SED_ERR_NOT_CONVERGED 4 /* SRE:1023 "Lanczos did not converge" */
+#define SED_ERR_LIMIT 5         /* size outside what the library supports */
+#define SED_ERR_NOT_HERMITIAN 6 /* term list not Hermitian-closed or not group-symmetric */
+#define SED_ERR_TIMEOUT 7       /* a bounded device wait gave up */
+
+#define SED_BOSONIC 0
+#define SED_FERMIONIC 1
+
+/* operator precision */
+#define SED_PREC_FP64 0  /* complex128 matvec: the plain drop-in */
+#define SED_PREC_MIXED 1 /* complex64 matvec, FP64 Lanczos + FP64 Rayleigh-Ritz polish */
+
+/* catalog readback fields (SRE:305-327 Symmetry_Orbit_Catalog) */
+#define SED_FIELD_REPS 0       /* uint64[n_orbits]   representative_mask_list */
+#define SED_FIELD_STAB_ORDER 1 /* int32[n_orbits]    stabilizer_order_list */
+#define SED_FIELD_STAB_PTR 2   /* int64[n_orbits+1]  CSR offsets of the stabilizer lists */
+#define SED_FIELD_STAB_G 3     /* int32[n_stab]      stabilizer_g_indices_list (1-based) */
+#define SED_FIELD_STAB_PHASE 4 /* f64x2[n_stab]      stabilizer_phases_list */
+#define SED_FIELD_REP_RANK 5   /* int32[n_states]    rep_rank_table (1-based, 0 unset) */
+#define SED_FIELD_REP_SYM 6    /* int32[n_states]    rep_sym_table (1-based) */
+#define SED_FIELD_REP_AMP 7    /* f64x2[n_states]    rep_amp_table */
+
+typedef struct sed_group sed_group;
+typedef struct sed_catalog sed_catalog;
+typedef struct sed_sector sed_sector;
+typedef struct sed_op sed_op;
+
+typedef struct sed_solve_info {
+  int32_t n_restarts;      /* outer (thick-restart) iterations */
+  int32_t n_matvec;        /* sector matvecs in the working precision */
+  int32_t n_matvec_fp64;   /* FP64 matvecs of the polish step (mixed precision) */
+  int32_t converged;       /* number of converged eigenpairs */
+  double max_residual;     /* largest Ritz residual of the returned pairs */
+  double max_delta_polish; /* max |E_polished - E_working| (mixed precision), else 0 */
+  double seconds;          /* wall time of the solve */
+} sed_solve_info;
+
+/* ---------------------------------------------------------------- library */
+const char* sed_last_error(void);
+int sed_api_version(void);
+/* Current device, its SM count and free/total memory (bytes). */
+int sed_device_info(int* device, int* sm_count, int64_t* free_bytes, int64_t* total_bytes);
+
+/* ------------------------------------------------------------------ group */
+/* Finite_Symmetry_Group (SRE:90-104) with _inverse_operation_indices
+ * (SRE:109-117).  perm: n_ops x n_site 0-based targets (perm[g*n_site+i] is
+ * the image of site i); phase_reim: n_ops x n_site complex eta_g(i);
+ * stats: SED_BOSONIC / SED_FERMIONIC.  Limits: n_site <= 63, n_ops <= 64. */
+int sed_group_create(int n_site, int n_ops, const int32_t* perm, const double* phase_reim, int identity_idx,
+                     int stats, sed_group** out);
+/* 0-based inverse element of every operation. */
+int sed_group_inverse(const sed_group* g, int32_t* inv_out);
+void sed_group_destroy(sed_group* g);
+
+/* ---------------------------------------------------------------- catalog */
+/* build_symmetry_orbit_catalog (SRE:371-487), built on the device:
+ * combinadic unranking in place of the serial Gosper loop, canonical test
+ * over |G| permutations held in shared memory, orbit expansion into the
+ * representative tables.  Limit: binomial(n_site, n_filled) < 2^32. */
+int sed_catalog_build(const sed_group* g, int n_filled, sed_catalog** out);
+int sed_catalog_info(const sed_catalog* c, int64_t* n_states, int64_t* n_orbits, int64_t* n_stab_total);
+/* Read one table back to the host in the reference's layout (bit-exact). */
+int sed_catalog_get(const sed_catalog* c, int field, void* out, int64_t out_bytes);
+/* update_orbit_stabilizer_phases! (SRE:338-369): same permutations, new
+ * per-site phases (a flux-twisted group); no re-enumeration. */
+int sed_catalog_update_phases(sed_catalog* c, const sed_group* new_group);
+int sed_catalog_set_stream(sed_catalog* c, void* cuda_stream);
+void sed_catalog_destroy(sed_catalog* c);
+
+/* ----------------------------------------------------------------- sector */
+/* build_symmetry_sector_basis (SRE:534-556): orbits whose stabilizer phases
+ * match chi (|chi(h) - alpha_h(rep)| <= atol), in catalog order. */
+int sed_sector_build(const sed_catalog* c, const double* chi_reim, double atol, sed_sector** out, int64_t* dim);
+/* representative_mask_list, stabilizer_order_list and the catalog orbit index
+ * of every sector row (any pointer may be NULL). */
+int sed_sector_get(const sed_sector* s, uint64_t* reps, int32_t* stab_order, int32_t* orbit_index);
+void sed_sector_destroy(sed_sector* s);
+
+/* --------------------------------------------------------------- operator */
+/* MatrixFreeHamiltonian (SRE:767-791) / hamiltonian_linear_operator
+ * (SRE:891-897).  Bilinear term t moves a particle from site bil_ij[2k] to
+ * site bil_ij[2k+1] (the reference's gate (m & hop) == from, SRE:709-710);
+ * density term v counts n_i n_j.  The term list must be Hermitian-closed and
+ * invariant under the group (SED_ERR_NOT_HERMITIAN otherwise): the device
+ * kernel gathers rows through H_rc = conj(H_cr).  precision: SED_PREC_*. */
+int sed_op_create(const sed_sector* s, int n_bil, const int32_t* bil_ij, const double* bil_t_reim, int n_den,
+                  const int32_t* den_ij, const double* den_v_reim, int precision, sed_op** out);
+/* Host-only validation of a bilinear term list against a group (no device
+ * work): the checks sed_op_create applies before building an operator. */
+int sed_terms_validate(const sed_group* g, int n_bil, const int32_t* bil_ij, const double* bil_t_reim);
+/* apply_hamiltonian! (SRE:804-878) / H(x) (SRE:880-884): y = H x for
+ * sector-ordered complex128 vectors of length n == sector dim.  With
+ * is_device_ptr the pointers are device memory on this op's stream; the call
+ * is then asynchronous. */
+int sed_op_apply(sed_op* op, const double* x_reim, double* y_reim, int64_t n, int is_device_ptr);
+/* dim = sector dimension, n_orbits = length of the orbit-indexed device
+ * vectors, hops = valid hops one matvec evaluates (counted on the device). */
+int sed_op_info(const sed_op* op, int64_t* dim, int64_t* n_orbits, int64_t* hops);
+int sed_op_set_stream(sed_op* op, void* cuda_stream);
+/* Orbit-indexed matvec for benchmarking the kernel alone: xs_dev holds
+ * sqrt(stab)*x in the op's precision (complex64 or complex128, length
+ * n_orbits), y_dev receives complex128 H x (length n_orbits).  Asynchronous. */
+int sed_op_apply_orbit(sed_op* op, const void* xs_dev, double* y_dev);
+void sed_op_destroy(sed_op* op);
+
+/* -------------------------------------------------------------------- solve */
+/* diagonalize_block_matrixfree (SRE:998-1030): lowest nev eigenpairs by
+ * thick-restart Lanczos with full reorthogonalisation on the device.  tol is
+ * the absolute Ritz-residual bound (the reference passes 1e-10), maxiter the
+ * restart budget (300), krylovdim the basis size (0 = 30).  seed selects the
+ * complex Gaussian start vector.  evecs_reim (nullable) receives nev
+ * sector-ordered complex128 vectors, vector-major.  Mixed-precision operators
+ * converge with the complex64 matvec, then run one FP64 Rayleigh-Ritz polish
+ * over span{x, Hx}. */
+int sed_solve(sed_op* op, int nev, double tol, int maxiter, int krylovdim, uint64_t seed, double* evals,
+              double* evecs_reim, sed_solve_info* info);
+
+/* ---------------------------------------------------------- batched solves */
+/* Many small sector solves sharing one catalog (one set of permutations and
+ * one (i, j) term list), run by a persistent kernel: every thread block takes
+ * the next request from a device-side queue and runs a whole thick-restart
+ * Lanczos for it, with the sector vector in shared memory.  This replaces the
+ * reference's sequential per-sector / per-twist loop (SRE:1227-1254,
+ * SRE:1320-1355).  Request b brings its own momentum chi (n_ops complex), its
+ * group phases (n_ops x n_site complex: the flux-twisted group of
+ * build_translation_group, SRE:1374-1405), its bilinear amplitudes (n_bil
+ * complex, same (i, j) list for every request) and its start-vector seed, so
+ * its result does not depend on which other requests share the launch.
+ * precision: SED_PREC_MIXED (complex64 matvec + FP64 Rayleigh-Ritz polish) or
+ * SED_PREC_FP64.  Outputs per request: nev eigenvalues (ascending), status
+ * (0 ok, SED_ERR_NOT_CONVERGED), sector dimension, |E_polished - E_c64| and
+ * the matvec count. */
+typedef struct sed_batch sed_batch;
+int sed_batch_create(const sed_catalog* c, int n_bil, const int32_t* bil_ij, int n_den, const int32_t* den_ij,
+                     const double* den_v_reim, int precision, int nev, int krylovdim, int max_requests,
+                     sed_batch** out);
+int sed_batch_run(sed_batch* b, int n_req, const double* chi_reim, const double* group_phase_reim,
+                  const double* bil_t_reim, const uint64_t* seeds, double tol, int maxiter, double* evals,
+                  int32_t* status, int64_t* dims, double* delta_polish, int32_t* n_matvec);
+/* Per-request diagnostics of the last run (host buffers of n_req entries, any
+ * may be NULL): hops evaluated by one matvec of the request's sector, and the
+ * device clock (ns) when its block picked it up and when it finished. */
+int sed_batch_last_stats(const sed_batch* b, int64_t* hops, int64_t* t_start_ns, int64_t* t_end_ns);
+/* Same solve with every buffer in device memory (inputs resident in HBM);
+ * asynchronous on the batch stream.  Device arrays have the layouts of
+ * sed_batch_run; outputs may not be NULL. */
+int sed_batch_run_device(sed_batch* b, int n_req, const double* d_chi, const double* d_group_phase,
+                         const double* d_bil_t, const uint64_t* d_seeds, double tol, int maxiter, double* d_evals,
+                         int32_t* d_status, int64_t* d_dims, double* d_delta, int32_t* d_n_matvec);
+int sed_batch_set_stream(sed_batch* b, void* cuda_stream);
+/* Dynamic shared memory per block, resident blocks (= concurrent requests)
+ * and device bytes held by the batch object. */
+int sed_batch_info(const sed_batch* b, int64_t* smem_bytes, int64_t* n_blocks, int64_t* footprint_bytes);
+void sed_batch_destroy(sed_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SED_CAPI_H */

@@ -1,0 +1,351 @@
+"""Reference-facing API: the Julia package's hot-path types and functions,
+backed by the GPU library.
+
+Names, argument meaning and error behaviour follow
+src/symmetry_resolved_ed.jl (SRE) of RealSpace_ExactDiagonalization v0.1.0;
+Julia's mutating ``f!`` becomes ``f_``.  Site indices in term lists and
+permutations are 1-based, as in the reference; the C ABI underneath is 0-based.
+Every compute call goes to libsed_gb300.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Any, Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, ptr
+from .groups import (Bosonic, Fermionic, Finite_Symmetry_Group, OneDim_Irrep, Particle_Statistics,
+                     Symmetry_Operation, build_identity_group, build_identity_irrep_list, group_order)
+
+__all__ = [
+    "Bosonic", "Fermionic", "Symmetry_Operation", "Finite_Symmetry_Group", "OneDim_Irrep", "group_order",
+    "build_identity_group", "build_identity_irrep_list", "Real_Space_Second_Quantized_Model",
+    "Symmetry_Orbit_Catalog", "build_symmetry_orbit_catalog", "update_orbit_stabilizer_phases_",
+    "Symmetry_Sector_Basis", "build_symmetry_sector_basis", "CanonicalMap", "populate_canonical_map_",
+    "MatrixFreeHamiltonian", "apply_hamiltonian_", "hamiltonian_linear_operator", "diagonalize_block_matrixfree",
+    "DeviceGroup",
+]
+
+
+@dataclass
+class Real_Space_Second_Quantized_Model:
+    """Mirror of ``Real_Space_Second_Quantized_Model{T}`` (src/second_quantized_model.jl:19-26).
+    ``bilinear_terms`` are ``(i, j, t)``: t moves a particle from site i to site j."""
+
+    params: Dict[str, Any]
+    lattice: Any
+    tb_model: Any
+    particle_statistics: Particle_Statistics
+    bilinear_terms: List[Tuple[int, int, complex]]
+    density_density_terms: List[Tuple[int, int, complex]]
+
+
+def update_second_quantized_model_with_twisted_phases_(model: Real_Space_Second_Quantized_Model,
+                                                       twisted_phases_over_2pi: Sequence[float]):
+    """src/second_quantized_model.jl:39-53: regenerate the bilinear terms with a twist."""
+    from .lattice import generate_bilinear_terms
+
+    if len(twisted_phases_over_2pi) != model.lattice.dim:
+        raise ValueError(f"twisted_phases_over_2π must have length {model.lattice.dim}.")
+    model.bilinear_terms = generate_bilinear_terms(model.tb_model, twisted_phases_over_2pi)
+    model.lattice.twisted_phases_over_2pi = list(twisted_phases_over_2pi)
+    return model
+
+
+# ------------------------------------------------------------------- handles
+class _Handle:
+    _destroy = ""
+
+    def __init__(self, h: C.c_void_p):
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                getattr(_lib.load(), self._destroy)(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+class DeviceGroup(_Handle):
+    """A Finite_Symmetry_Group uploaded to the library (with its statistics)."""
+
+    _destroy = "sed_group_destroy"
+
+    def __init__(self, G: Finite_Symmetry_Group, stats: Particle_Statistics):
+        lib = _lib.load()
+        perm = np.ascontiguousarray(G.perm0(), dtype=np.int32)
+        ph = np.ascontiguousarray(G.phases(), dtype=np.complex128)
+        h = C.c_void_p()
+        check(lib.sed_group_create(G.n_site, len(G), ptr(perm), ptr(ph), G.identity_idx - 1, stats.code,
+                                   C.byref(h)))
+        super().__init__(h)
+        self.group = G
+        self.stats = stats
+
+    def inverse(self) -> np.ndarray:
+        inv = np.zeros(len(self.group), dtype=np.int32)
+        check(_lib.load().sed_group_inverse(self._h, ptr(inv)))
+        return inv
+
+
+class Symmetry_Orbit_Catalog(_Handle):
+    """SRE:305-327.  The tables live on the device; the reference's fields are
+    read back lazily, in the reference's layout (1-based indices)."""
+
+    _destroy = "sed_catalog_destroy"
+
+    def __init__(self, h, dgroup: DeviceGroup, n_filled: int):
+        super().__init__(h)
+        self._dgroup = dgroup
+        self.symmetry_group = dgroup.group
+        self.particle_statistics = dgroup.stats
+        self.n_filled = n_filled
+        ns, no, nst = C.c_int64(), C.c_int64(), C.c_int64()
+        check(_lib.load().sed_catalog_info(h, C.byref(ns), C.byref(no), C.byref(nst)))
+        self.n_states, self.n_orbits, self.n_stab_total = ns.value, no.value, nst.value
+        self._cache: Dict[int, np.ndarray] = {}
+
+    def _get(self, field: int) -> np.ndarray:
+        if field not in self._cache:
+            n, dt = {
+                _lib.FIELD_REPS: (self.n_orbits, np.uint64), _lib.FIELD_STAB_ORDER: (self.n_orbits, np.int32),
+                _lib.FIELD_STAB_PTR: (self.n_orbits + 1, np.int64), _lib.FIELD_STAB_G: (self.n_stab_total, np.int32),
+                _lib.FIELD_STAB_PHASE: (self.n_stab_total, np.complex128),
+                _lib.FIELD_REP_RANK: (self.n_states, np.int32), _lib.FIELD_REP_SYM: (self.n_states, np.int32),
+                _lib.FIELD_REP_AMP: (self.n_states, np.complex128),
+            }[field]
+            out = np.zeros(n, dtype=dt)
+            check(_lib.load().sed_catalog_get(self._h, field, ptr(out), out.nbytes))
+            self._cache[field] = out
+        return self._cache[field]
+
+    @property
+    def representative_mask_list(self) -> np.ndarray:
+        return self._get(_lib.FIELD_REPS)
+
+    @property
+    def stabilizer_order_list(self) -> np.ndarray:
+        return self._get(_lib.FIELD_STAB_ORDER)
+
+    @property
+    def stabilizer_g_indices_list(self) -> List[np.ndarray]:
+        p, g = self._get(_lib.FIELD_STAB_PTR), self._get(_lib.FIELD_STAB_G)
+        return [g[p[i]:p[i + 1]] for i in range(self.n_orbits)]
+
+    @property
+    def stabilizer_phases_list(self) -> List[np.ndarray]:
+        p, v = self._get(_lib.FIELD_STAB_PTR), self._get(_lib.FIELD_STAB_PHASE)
+        return [v[p[i]:p[i + 1]] for i in range(self.n_orbits)]
+
+    @property
+    def rep_rank_table(self) -> np.ndarray:
+        return self._get(_lib.FIELD_REP_RANK)
+
+    @property
+    def rep_sym_table(self) -> np.ndarray:
+        return self._get(_lib.FIELD_REP_SYM)
+
+    @property
+    def rep_amp_table(self) -> np.ndarray:
+        return self._get(_lib.FIELD_REP_AMP)
+
+
+def build_symmetry_orbit_catalog(*, second_quantized_model=None, n_filled: int,
+                                 symmetry_group: Finite_Symmetry_Group,
+                                 particle_statistics: Particle_Statistics) -> Symmetry_Orbit_Catalog:
+    """SRE:371-487, on the device."""
+    if second_quantized_model is not None and second_quantized_model.lattice.n_site != symmetry_group.n_site:
+        raise ValueError("the group and the model act on different numbers of sites")
+    if not 0 <= n_filled <= symmetry_group.n_site:
+        raise ValueError("n_filled must be in [0, n_site]")
+    dg = DeviceGroup(symmetry_group, particle_statistics)
+    h = C.c_void_p()
+    check(_lib.load().sed_catalog_build(dg.handle, n_filled, C.byref(h)))
+    return Symmetry_Orbit_Catalog(h, dg, n_filled)
+
+
+def update_orbit_stabilizer_phases_(catalog: Symmetry_Orbit_Catalog, new_group: Finite_Symmetry_Group,
+                                    particle_statistics: Particle_Statistics) -> Symmetry_Orbit_Catalog:
+    """SRE:338-369: adopt a twisted copy of the group without re-enumeration."""
+    if new_group is catalog.symmetry_group:
+        return catalog
+    dg = DeviceGroup(new_group, particle_statistics)
+    check(_lib.load().sed_catalog_update_phases(catalog.handle, dg.handle))
+    catalog._dgroup = dg
+    catalog.symmetry_group = new_group
+    catalog._cache.clear()
+    return catalog
+
+
+class Symmetry_Sector_Basis(_Handle):
+    """SRE:522-528: orbits compatible with a 1D irrep, in catalog order."""
+
+    _destroy = "sed_sector_destroy"
+
+    def __init__(self, h, catalog: Symmetry_Orbit_Catalog, irrep: OneDim_Irrep, dim: int):
+        super().__init__(h)
+        self.catalog = catalog
+        self.irrep = irrep
+        self.symmetry_group = catalog.symmetry_group
+        self.dim = dim
+        self._arrays = None
+        self._map = None
+
+    def _load(self):
+        if self._arrays is None:
+            reps = np.zeros(self.dim, dtype=np.uint64)
+            stab = np.zeros(self.dim, dtype=np.int32)
+            orb = np.zeros(self.dim, dtype=np.int32)
+            check(_lib.load().sed_sector_get(self._h, ptr(reps), ptr(stab), ptr(orb)))
+            self._arrays = (reps, stab, orb)
+        return self._arrays
+
+    @property
+    def representative_mask_list(self) -> np.ndarray:
+        return self._load()[0]
+
+    @property
+    def stabilizer_order_list(self) -> np.ndarray:
+        return self._load()[1]
+
+    @property
+    def orbit_index_list(self) -> np.ndarray:
+        return self._load()[2]
+
+    @property
+    def representative_mask_to_mask_idx_map(self) -> Dict[int, int]:
+        if self._map is None:
+            self._map = {int(m): i + 1 for i, m in enumerate(self.representative_mask_list)}
+        return self._map
+
+
+def build_symmetry_sector_basis(catalog: Symmetry_Orbit_Catalog, irrep: OneDim_Irrep,
+                                atol: float = 1e-12) -> Symmetry_Sector_Basis:
+    """SRE:544-556."""
+    chi = np.ascontiguousarray(irrep.array(), dtype=np.complex128)
+    if len(chi) != group_order(catalog.symmetry_group):
+        raise ValueError("the irrep needs one value per group element")
+    h, dim = C.c_void_p(), C.c_int64()
+    check(_lib.load().sed_sector_build(catalog.handle, ptr(chi), float(atol), C.byref(h), C.byref(dim)))
+    return Symmetry_Sector_Basis(h, catalog, irrep, dim.value)
+
+
+@dataclass
+class CanonicalMap:
+    """SRE:577-581.  The representative tables are already on the device."""
+
+    symmetry_group: Finite_Symmetry_Group
+    particle_statistics: Particle_Statistics
+    catalog: Symmetry_Orbit_Catalog
+
+
+def populate_canonical_map_(cmap: CanonicalMap, basis, bilinear_terms) -> CanonicalMap:
+    """SRE:605-608: a no-op kept for API compatibility, as in the reference."""
+    return cmap
+
+
+def _terms_arrays(terms, n_site: int, what: str):
+    n = len(terms)
+    ij = np.zeros((n, 2), dtype=np.int32)
+    v = np.zeros(n, dtype=np.complex128)
+    for k, (i, j, t) in enumerate(terms):
+        if not (1 <= int(i) <= n_site and 1 <= int(j) <= n_site):
+            raise ValueError(f"{what} term {k} has a site index outside 1:{n_site}")
+        ij[k] = (int(i) - 1, int(j) - 1)
+        v[k] = complex(t)
+    return ij, v
+
+
+class MatrixFreeHamiltonian(_Handle):
+    """SRE:767-791 / hamiltonian_linear_operator SRE:891-897: ``H(x) -> y``.
+
+    ``precision="fp64"`` is the plain drop-in (complex128 matvec);
+    ``"mixed"`` runs the matvec in complex64 and solves with FP64 Lanczos and
+    an FP64 Rayleigh-Ritz polish."""
+
+    _destroy = "sed_op_destroy"
+
+    def __init__(self, basis: Symmetry_Sector_Basis, bilinear_terms, density_terms, cmap: Optional[CanonicalMap] = None,
+                 precision: str = "fp64"):
+        self.basis = basis
+        n_site = basis.symmetry_group.n_site
+        self.bilinear_terms = [(int(i), int(j), complex(t)) for (i, j, t) in bilinear_terms]
+        self.density_terms = [(int(i), int(j), complex(v)) for (i, j, v) in density_terms]
+        bij, bt = _terms_arrays(self.bilinear_terms, n_site, "bilinear")
+        dij, dv = _terms_arrays(self.density_terms, n_site, "density")
+        prec = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}[precision]
+        h = C.c_void_p()
+        check(_lib.load().sed_op_create(basis.handle, len(bt), ptr(bij), ptr(bt), len(dv), ptr(dij), ptr(dv), prec,
+                                        C.byref(h)))
+        super().__init__(h)
+        self.precision = precision
+        self.n = basis.dim
+
+    def __call__(self, x: np.ndarray) -> np.ndarray:
+        y = np.empty(self.n, dtype=np.complex128)
+        return self.apply(x, y)
+
+    def apply(self, x: np.ndarray, y: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        if x.shape != (self.n,) or y.shape != (self.n,) or y.dtype != np.complex128:
+            raise ValueError(f"x and y must be complex128 vectors of length {self.n}")
+        check(_lib.load().sed_op_apply(self._h, ptr(x), ptr(y), self.n, 0))
+        return y
+
+    def info(self):
+        d, no, hops = C.c_int64(), C.c_int64(), C.c_int64()
+        check(_lib.load().sed_op_info(self._h, C.byref(d), C.byref(no), C.byref(hops)))
+        return {"dim": d.value, "n_orbits": no.value, "hops": hops.value}
+
+    def solve(self, nev: int, tol: float = 1e-10, maxiter: int = 300, krylovdim: int = 30, seed: int = 0x5EED0000,
+              want_vectors: bool = True):
+        ev = np.zeros(max(nev, 1), dtype=np.float64)
+        k = min(nev, self.n)
+        vecs = np.zeros((k, self.n), dtype=np.complex128) if (want_vectors and k > 0) else None
+        info = _lib.sed_solve_info()
+        st = _lib.load().sed_solve(self._h, nev, float(tol), int(maxiter), int(krylovdim), C.c_uint64(seed), ptr(ev),
+                                   ptr(vecs), C.byref(info))
+        check(st)
+        return ev[:k], (vecs.T.copy() if vecs is not None else None), info
+
+
+def apply_hamiltonian_(y: np.ndarray, x: np.ndarray, basis: Symmetry_Sector_Basis, bilinear_terms, density_terms,
+                       cmap: Optional[CanonicalMap] = None) -> np.ndarray:
+    """SRE:804-878: y = H x on the device (builds a transient operator)."""
+    if len(y) != len(x):
+        raise ValueError("length(y) == n")
+    H = MatrixFreeHamiltonian(basis, bilinear_terms, density_terms, cmap)
+    return H.apply(x, y)
+
+
+def hamiltonian_linear_operator(basis: Symmetry_Sector_Basis, bilinear_terms, density_terms,
+                                cmap: Optional[CanonicalMap] = None, precision: str = "fp64"):
+    """SRE:891-897: ``(H_op, n)``."""
+    H = MatrixFreeHamiltonian(basis, bilinear_terms, density_terms, cmap, precision=precision)
+    return H, basis.dim
+
+
+def diagonalize_block_matrixfree(H_op: MatrixFreeHamiltonian, n: int, nev: int = 5, tol: float = 1e-10,
+                                 maxiter: int = 300, krylovdim: int = 30, seed: int = 0x5EED0000):
+    """SRE:998-1030: lowest ``nev`` eigenpairs, ``(vals, vecs)`` with
+    ``vecs[:, i]`` the i-th eigenvector.  Raises SEDError (status
+    SED_ERR_NOT_CONVERGED) where the reference raises "Lanczos did not
+    converge".  Only device operators are accepted: there is no CPU path."""
+    if n == 0:
+        return np.zeros(0), np.zeros((0, 0), dtype=np.complex128)
+    if not isinstance(H_op, MatrixFreeHamiltonian):
+        raise TypeError("diagonalize_block_matrixfree needs a device MatrixFreeHamiltonian")
+    if H_op.n != n:
+        raise ValueError("n must equal the operator dimension")
+    vals, vecs, _ = H_op.solve(nev, tol=tol, maxiter=maxiter, krylovdim=krylovdim, seed=seed)
+    return vals, vecs

@@ -1,0 +1,210 @@
+// sed_capi.cu -- extern "C" entry points of libsed_gb300.so (see include/sed_capi.h).
+// Each entry point converts C++ exceptions into an int status plus a
+// thread-local message, so no exception ever crosses the ABI.
+#include <cstring>
+#include <string>
+
+#include "../../include/sed_capi.h"
+#include "sed_internal.cuh"
+
+struct sed_group {
+  std::shared_ptr<sed::GroupImpl> p;
+};
+struct sed_catalog {
+  std::shared_ptr<sed::CatalogImpl> p;
+};
+struct sed_sector {
+  std::shared_ptr<sed::SectorImpl> p;
+};
+struct sed_op {
+  std::shared_ptr<sed::OpImpl> p;
+};
+
+namespace sed {
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace sed
+
+template <class F>
+static int guarded(F&& f) {
+  try {
+    f();
+    return SED_OK;
+  } catch (const sed::Error& e) {
+    sed::set_error(e.msg);
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    sed::set_error("host allocation failed");
+    return SED_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    sed::set_error(e.what());
+    return SED_ERR_ARG;
+  }
+}
+
+#define REQ(cond, msg) SED_REQUIRE(cond, SED_ERR_ARG, msg)
+
+extern "C" {
+
+const char* sed_last_error(void) { return sed::g_last_error.c_str(); }
+int sed_api_version(void) { return SED_API_VERSION; }
+
+int sed_device_info(int* device, int* sm_count, int64_t* free_bytes, int64_t* total_bytes) {
+  return guarded([&] {
+    int d = 0;
+    SED_CUDA(cudaGetDevice(&d));
+    size_t fr = 0, tot = 0;
+    SED_CUDA(cudaMemGetInfo(&fr, &tot));
+    if (device) *device = d;
+    if (sm_count) *sm_count = sed::device_sm_count();
+    if (free_bytes) *free_bytes = (int64_t)fr;
+    if (total_bytes) *total_bytes = (int64_t)tot;
+  });
+}
+
+int sed_group_create(int n_site, int n_ops, const int32_t* perm, const double* phase_reim, int identity_idx,
+                     int stats, sed_group** out) {
+  return guarded([&] {
+    REQ(out != nullptr, "out must not be NULL");
+    *out = nullptr;
+    auto g = sed::make_group(n_site, n_ops, perm, phase_reim, identity_idx, stats);
+    *out = new sed_group{g};
+  });
+}
+int sed_group_inverse(const sed_group* g, int32_t* inv_out) {
+  return guarded([&] {
+    REQ(g && inv_out, "NULL argument");
+    std::memcpy(inv_out, g->p->inv.data(), g->p->inv.size() * 4);
+  });
+}
+void sed_group_destroy(sed_group* g) { delete g; }
+
+int sed_catalog_build(const sed_group* g, int n_filled, sed_catalog** out) {
+  return guarded([&] {
+    REQ(g && out, "NULL argument");
+    *out = nullptr;
+    auto c = sed::build_catalog(g->p, n_filled);
+    *out = new sed_catalog{c};
+  });
+}
+int sed_catalog_info(const sed_catalog* c, int64_t* n_states, int64_t* n_orbits, int64_t* n_stab_total) {
+  return guarded([&] {
+    REQ(c, "NULL catalog");
+    if (n_states) *n_states = c->p->n_states;
+    if (n_orbits) *n_orbits = c->p->n_orbits;
+    if (n_stab_total) *n_stab_total = c->p->n_stab_total;
+  });
+}
+int sed_catalog_get(const sed_catalog* c, int field, void* out, int64_t out_bytes) {
+  return guarded([&] {
+    REQ(c, "NULL catalog");
+    sed::catalog_readback(*c->p, field, out, out_bytes);
+  });
+}
+int sed_catalog_update_phases(sed_catalog* c, const sed_group* g) {
+  return guarded([&] {
+    REQ(c && g, "NULL argument");
+    sed::catalog_update_phases(*c->p, g->p);
+  });
+}
+int sed_catalog_set_stream(sed_catalog* c, void* stream) {
+  return guarded([&] {
+    REQ(c, "NULL catalog");
+    if (c->p->own_stream && c->p->stream) cudaStreamDestroy(c->p->stream);
+    c->p->own_stream = false;
+    c->p->stream = (cudaStream_t)stream;
+  });
+}
+void sed_catalog_destroy(sed_catalog* c) { delete c; }
+
+int sed_sector_build(const sed_catalog* c, const double* chi_reim, double atol, sed_sector** out, int64_t* dim) {
+  return guarded([&] {
+    REQ(c && out, "NULL argument");
+    REQ(atol >= 0.0, "atol must be non-negative");
+    *out = nullptr;
+    auto s = sed::build_sector(c->p, chi_reim, atol);
+    if (dim) *dim = s->dim;
+    *out = new sed_sector{s};
+  });
+}
+int sed_sector_get(const sed_sector* s, uint64_t* reps, int32_t* stab_order, int32_t* orbit_index) {
+  return guarded([&] {
+    REQ(s, "NULL sector");
+    sed::sector_readback(*s->p, reps, stab_order, orbit_index);
+  });
+}
+void sed_sector_destroy(sed_sector* s) { delete s; }
+
+int sed_op_create(const sed_sector* s, int n_bil, const int32_t* bil_ij, const double* bil_t_reim, int n_den,
+                  const int32_t* den_ij, const double* den_v_reim, int precision, sed_op** out) {
+  return guarded([&] {
+    REQ(s && out, "NULL argument");
+    *out = nullptr;
+    auto op = sed::make_op(s->p, n_bil, bil_ij, bil_t_reim, n_den, den_ij, den_v_reim, precision);
+    *out = new sed_op{op};
+  });
+}
+int sed_terms_validate(const sed_group* g, int n_bil, const int32_t* bil_ij, const double* bil_t_reim) {
+  return guarded([&] {
+    REQ(g, "NULL group");
+    REQ(n_bil == 0 || (bil_ij && bil_t_reim), "bilinear arrays must not be NULL");
+    sed::TermTables tt;
+    sed::build_term_tables(*g->p, n_bil, bil_ij, bil_t_reim, tt);
+    sed::check_hermitian_symmetric(*g->p, n_bil, bil_ij, bil_t_reim);
+  });
+}
+int sed_op_apply(sed_op* op, const double* x_reim, double* y_reim, int64_t n, int is_device_ptr) {
+  return guarded([&] {
+    REQ(op, "NULL operator");
+    sed::op_apply_host(*op->p, x_reim, y_reim, n, is_device_ptr != 0);
+  });
+}
+int sed_op_info(const sed_op* op, int64_t* dim, int64_t* n_orbits, int64_t* hops) {
+  return guarded([&] {
+    REQ(op, "NULL operator");
+    if (dim) *dim = op->p->sec->dim;
+    if (n_orbits) *n_orbits = op->p->sec->cat->n_orbits;
+    if (hops) *hops = sed::op_count_hops(*op->p);
+  });
+}
+int sed_op_set_stream(sed_op* op, void* stream) {
+  return guarded([&] {
+    REQ(op, "NULL operator");
+    if (op->p->own_stream && op->p->stream) cudaStreamDestroy(op->p->stream);
+    op->p->own_stream = false;
+    op->p->stream = (cudaStream_t)stream;
+  });
+}
+int sed_op_apply_orbit(sed_op* op, const void* xs_dev, double* y_dev) {
+  return guarded([&] {
+    REQ(op && xs_dev && y_dev, "NULL argument");
+    sed::op_apply_orbit(*op->p, xs_dev, y_dev, op->p->stream);
+  });
+}
+void sed_op_destroy(sed_op* op) { delete op; }
+
+int sed_solve(sed_op* op, int nev, double tol, int maxiter, int krylovdim, uint64_t seed, double* evals,
+              double* evecs_reim, sed_solve_info* info) {
+  sed::SolveResult r;
+  int st = guarded([&] {
+    REQ(op && evals, "NULL argument");
+    REQ(tol > 0.0, "tol must be positive");
+    r = sed::solve(*op->p, nev, tol, maxiter, krylovdim, seed, evals, evecs_reim);
+  });
+  if (info) {
+    info->n_restarts = r.restarts;
+    info->n_matvec = r.matvecs;
+    info->n_matvec_fp64 = r.matvecs64;
+    info->converged = r.converged;
+    info->max_residual = r.max_residual;
+    info->max_delta_polish = r.max_delta;
+    info->seconds = r.seconds;
+  }
+  if (st == SED_OK && r.status != 0) {
+    sed::set_error("Lanczos did not converge the requested eigenpairs within maxiter restarts.");
+    return SED_ERR_NOT_CONVERGED;
+  }
+  return st;
+}
+
+}  // extern "C"

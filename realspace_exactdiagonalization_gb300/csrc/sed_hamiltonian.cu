@@ -1,0 +1,509 @@
+// sed_hamiltonian.cu -- the matrix-free sector Hamiltonian H|psi> on the GPU.
+//
+// Replaces apply_hamiltonian! (SRE:804-878) and the MatrixFreeHamiltonian
+// functor (SRE:680-765, 880-884) of src/symmetry_resolved_ed.jl.  The
+// reference scatters column by column into per-thread buffers; this kernel
+// gathers row by row through Hermiticity, y_r = sum_c conj(H_cr) x_c, where
+// column r of H is enumerated on the fly from the representative of row r:
+//   for every occupied site i and every hop record i -> j with j empty
+//     new  = m_r ^ (bit i | bit j)                (SRE:709-710, XOR hop)
+//     s_JW = (-1)^popcount(m_r & between(i, j))   (SRE:646-654, fermions)
+//     w    = state[rank(new)]                     (SRE:584-594, one table read)
+//     H_cr = t * s_JW * conj(alpha_g(rep_c)) * conj(chi(h)) * sqrt(stab_c / stab_r)
+// with h = g^-1.  Inputs are pre-scaled, xs_c = sqrt(stab_c) x_c, so a hop costs
+// one table read, one vector read and one complex multiply-add:
+//   y_r = (1/sqrt(stab_r)) * ( diag_r xs_r + sum_hops tchi[u][h] * sign * conj(P_h(new)) * xs_c )
+// where tchi[u][h] = conj(t_u) chi(h) is tabulated per distinct amplitude u and
+// P_h(new) is the per-site phase product of a flux-twisted group (1 otherwise).
+#include <algorithm>
+#include <cmath>
+#include <map>
+
+#include "sed_internal.cuh"
+#include "sed_rowgather.cuh"
+
+namespace sed {
+
+// ---------------------------------------------------------------- host checks
+void build_term_tables(const GroupImpl& G, int n_bil, const int32_t* bil_ij, const double* bil_t, TermTables& tt) {
+  const int N = G.n_site;
+  SED_REQUIRE(n_bil >= 0 && n_bil < 65535, 5, "at most 65534 bilinear terms");
+  std::vector<std::vector<std::pair<int, int>>> by_site(N);  // (to, class)
+  std::map<std::pair<double, double>, int> cls;
+  tt.amp.clear();
+  for (int k = 0; k < n_bil; ++k) {
+    const int i = bil_ij[2 * k], j = bil_ij[2 * k + 1];
+    SED_REQUIRE(i >= 0 && i < N && j >= 0 && j < N, 1, "bilinear term site index out of range");
+    SED_REQUIRE(i != j, 1, "a bilinear term (i, i, t) changes the particle number; write it as a density term");
+    const double re = bil_t[2 * k], im = bil_t[2 * k + 1];
+    if (re == 0.0 && im == 0.0) continue;
+    auto key = std::make_pair(re, im);
+    auto it = cls.find(key);
+    int u;
+    if (it == cls.end()) {
+      u = (int)tt.amp.size() / 2;
+      cls[key] = u;
+      tt.amp.push_back(re);
+      tt.amp.push_back(im);
+    } else {
+      u = it->second;
+    }
+    by_site[i].push_back({j, u});
+  }
+  tt.n_site = N;
+  tt.n_class = (int)tt.amp.size() / 2;
+  SED_REQUIRE(tt.n_class < (1 << 23), 5, "too many distinct hopping amplitudes");
+  tt.site_off.assign(N + 1, 0);
+  tt.rec.clear();
+  for (int i = 0; i < N; ++i) {
+    tt.site_off[i] = (uint16_t)tt.rec.size();
+    for (auto& p : by_site[i]) tt.rec.push_back((uint32_t)p.first | ((uint32_t)p.second << 8));
+  }
+  tt.site_off[N] = (uint16_t)tt.rec.size();
+  tt.n_terms = (int)tt.rec.size();
+}
+
+// The gather needs H = H^dagger and [H, U_g] = 0 for every g: every hop
+// (i -> j, t) needs its partner (j -> i, conj t), and the group must map it to
+// (perm_g(i) -> perm_g(j), t * eta_g(j) * conj(eta_g(i))).
+void check_hermitian_symmetric(const GroupImpl& G, int n_bil, const int32_t* bil_ij, const double* bil_t) {
+  std::map<std::pair<int, int>, std::pair<double, double>> T;
+  double scale = 0.0;
+  for (int k = 0; k < n_bil; ++k) {
+    auto& e = T[{bil_ij[2 * k], bil_ij[2 * k + 1]}];
+    e.first += bil_t[2 * k];
+    e.second += bil_t[2 * k + 1];
+    scale = std::max(scale, std::hypot(bil_t[2 * k], bil_t[2 * k + 1]));
+  }
+  const double tol = 1e-9 * std::max(scale, 1e-300);
+  auto get = [&](int i, int j) {
+    auto it = T.find({i, j});
+    return it == T.end() ? std::make_pair(0.0, 0.0) : it->second;
+  };
+  for (auto& kv : T) {
+    const int i = kv.first.first, j = kv.first.second;
+    const auto t = kv.second;
+    const auto r = get(j, i);
+    SED_REQUIRE(std::hypot(t.first - r.first, t.second + r.second) <= tol, 6,
+                "bilinear terms are not Hermitian-closed: (i, j, t) needs (j, i, conj(t))");
+    const int N = G.n_site;
+    for (int g = 0; g < G.n_ops; ++g) {
+      const int pi = G.perm[(size_t)g * N + i], pj = G.perm[(size_t)g * N + j];
+      const double eir = G.phase[((size_t)g * N + i) * 2], eii = G.phase[((size_t)g * N + i) * 2 + 1];
+      const double ejr = G.phase[((size_t)g * N + j) * 2], eji = G.phase[((size_t)g * N + j) * 2 + 1];
+      // t * eta_j * conj(eta_i)
+      const double ar = ejr * eir + eji * eii, ai = eji * eir - ejr * eii;
+      const double er = t.first * ar - t.second * ai, ei = t.first * ai + t.second * ar;
+      const auto s = get(pi, pj);
+      SED_REQUIRE(std::hypot(er - s.first, ei - s.second) <= tol, 6,
+                  "bilinear terms are not invariant under the symmetry group");
+    }
+  }
+}
+
+struct ApplyArgs {
+  int64_t n_orb;
+  int N, G, n_class, n_terms;
+  const uint64_t* reps;
+  const uint8_t* stab;
+  const uint8_t* rowflag;
+  const double2* diag;
+  const uint64_t* state;
+  const uint32_t* rank_tab;
+  RankParams rp;
+  const uint16_t* site_off;
+  const uint32_t* rec;
+  const void* tchi;  // [n_class][G] V  (table mode)
+  const void* amp;   // [n_class] V     (on-the-fly mode)
+  const void* chi;   // [G] V
+  const uint8_t* inv;
+  const void* eta;   // [G][N] V        (twisted groups)
+};
+
+// Shared-memory image of the tables, 16-byte aligned pieces first.
+template <class V>
+struct SmemLayout {
+  size_t tchi, chi, isr, rank, rec, site_off, inv, total;
+  static SmemLayout make(const ApplyArgs& a, bool table) {
+    SmemLayout L;
+    size_t o = 0;
+    auto al = [&](size_t x) { return (x + 15) & ~(size_t)15; };
+    L.tchi = o;
+    o = al(o + (table ? (size_t)a.n_class * a.G : (size_t)a.n_class) * sizeof(V));
+    L.chi = o;
+    o = al(o + (size_t)a.G * sizeof(V));
+    L.isr = o;
+    o = al(o + 65 * sizeof(double));
+    L.rank = o;
+    o = al(o + (size_t)a.rp.total * 4);
+    L.rec = o;
+    o = al(o + (size_t)a.n_terms * 4);
+    L.site_off = o;
+    o = al(o + (size_t)(a.N + 1) * 2);
+    L.inv = o;
+    o = al(o + 64);
+    L.total = o;
+    return L;
+  }
+};
+
+template <class P, bool FERMI, bool PHASES, bool TABLE>
+__global__ void __launch_bounds__(256) k_apply(ApplyArgs a, SmemLayout<typename P::V> L,
+                                               const typename P::V* __restrict__ xs, double2* __restrict__ y) {
+  using V = typename P::V;
+  using S = typename P::S;
+  extern __shared__ __align__(16) unsigned char smem[];
+  V* s_tchi = reinterpret_cast<V*>(smem + L.tchi);
+  V* s_chi = reinterpret_cast<V*>(smem + L.chi);
+  double* s_isr = reinterpret_cast<double*>(smem + L.isr);
+  uint32_t* s_rank = reinterpret_cast<uint32_t*>(smem + L.rank);
+  uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem + L.rec);
+  uint16_t* s_off = reinterpret_cast<uint16_t*>(smem + L.site_off);
+  uint8_t* s_inv = reinterpret_cast<uint8_t*>(smem + L.inv);
+  {
+    const int nt = TABLE ? a.n_class * a.G : a.n_class;
+    const V* src = reinterpret_cast<const V*>(TABLE ? a.tchi : a.amp);
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) s_tchi[i] = src[i];
+    const V* chi = reinterpret_cast<const V*>(a.chi);
+    for (int i = threadIdx.x; i < a.G; i += blockDim.x) s_chi[i] = chi[i];
+    for (int i = threadIdx.x; i < 65; i += blockDim.x) s_isr[i] = i ? 1.0 / sqrt((double)i) : 0.0;
+    for (int i = threadIdx.x; i < a.rp.total; i += blockDim.x) s_rank[i] = a.rank_tab[i];
+    for (int i = threadIdx.x; i < a.n_terms; i += blockDim.x) s_rec[i] = a.rec[i];
+    for (int i = threadIdx.x; i <= a.N; i += blockDim.x) s_off[i] = a.site_off[i];
+    for (int i = threadIdx.x; i < a.G; i += blockDim.x) s_inv[i] = a.inv[i];
+  }
+  __syncthreads();
+  const V* __restrict__ eta = reinterpret_cast<const V*>(a.eta);
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < a.n_orb; o += (int64_t)gridDim.x * blockDim.x) {
+    if (!a.rowflag[o]) {
+      y[o] = make_double2(0.0, 0.0);
+      continue;
+    }
+    const double2 dg = a.diag[o];
+    const V xo = xs[o];
+    S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
+    S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
+    row_gather<P, FERMI, PHASES, TABLE>(a.reps[o], xs, s_tchi, s_chi, a.G, eta, a.N, s_rank, a.rp, s_rec, s_off,
+                                        s_inv, a.state, ar, ai);
+    const double is = s_isr[a.stab[o]];
+    y[o] = make_double2((double)ar * is, (double)ai * is);
+  }
+}
+
+// ----------------------------------------------------------------- helpers
+__global__ void k_diag(int64_t n_orb, const uint64_t* __restrict__ reps, const uint8_t* __restrict__ rowflag,
+                       int n_den, const int32_t* __restrict__ den_ij, const double2* __restrict__ den_v,
+                       double2* __restrict__ diag) {
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_orb; o += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t m = reps[o];
+    double re = 0.0, im = 0.0;  // SRE:697-703: summed in term order from zero
+    for (int t = 0; t < n_den; ++t)
+      if (((m >> den_ij[2 * t]) & 1ULL) && ((m >> den_ij[2 * t + 1]) & 1ULL)) {
+        re = __dadd_rn(re, den_v[t].x);
+        im = __dadd_rn(im, den_v[t].y);
+      }
+    diag[o] = (!rowflag || rowflag[o]) ? make_double2(re, im) : make_double2(0.0, 0.0);
+  }
+}
+
+__global__ void k_count_hops(int64_t n_orb, const uint64_t* __restrict__ reps, const uint8_t* __restrict__ rowflag,
+                             int N, const uint16_t* __restrict__ site_off, const uint32_t* __restrict__ rec,
+                             unsigned long long* __restrict__ total) {
+  unsigned long long cnt = 0;
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_orb; o += (int64_t)gridDim.x * blockDim.x) {
+    if (!rowflag[o]) continue;
+    const uint64_t m = reps[o];
+    uint64_t occ = m;
+    while (occ) {
+      const int i = __ffsll((long long)occ) - 1;
+      occ &= occ - 1;
+      for (int t = site_off[i]; t < site_off[i + 1]; ++t) cnt += !((m >> (rec[t] & 0xFF)) & 1ULL);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(total, cnt);
+}
+
+template <class V>
+__global__ void k_scale_xs(int64_t n_orb, const double2* __restrict__ v, const uint8_t* __restrict__ stab,
+                           V* __restrict__ xs) {
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_orb; o += (int64_t)gridDim.x * blockDim.x) {
+    const double s = sqrt((double)stab[o]);
+    const double2 x = v[o];
+    xs[o].x = x.x * s;
+    xs[o].y = x.y * s;
+  }
+}
+
+__global__ void k_expand_vec(int64_t dim, const uint32_t* __restrict__ row_orbit, const double2* __restrict__ xsec,
+                             double2* __restrict__ xpad) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x)
+    xpad[row_orbit[r]] = xsec[r];
+}
+
+__global__ void k_compress_vec(int64_t dim, const uint32_t* __restrict__ row_orbit, const double2* __restrict__ ypad,
+                               double2* __restrict__ ysec) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x)
+    ysec[r] = ypad[row_orbit[r]];
+}
+
+int grid1(int64_t work, int block) {
+  const int64_t sms = device_sm_count();
+  const int64_t g = (work + block - 1) / block;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, sms * 32));
+}
+
+void compute_diag(int64_t n_orb, const uint64_t* reps, const uint8_t* rowflag, int n_den, const int32_t* den_ij,
+                  const double2* den_v, double2* diag, cudaStream_t s) {
+  if (!n_orb) return;
+  k_diag<<<grid1(n_orb, 256), 256, 0, s>>>(n_orb, reps, rowflag, n_den, den_ij, den_v, diag);
+  SED_CUDA(cudaGetLastError());
+}
+
+OpImpl::~OpImpl() {
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+// -------------------------------------------------------------- op creation
+std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> sp, int n_bil, const int32_t* bil_ij, const double* bil_t,
+                                int n_den, const int32_t* den_ij, const double* den_v, int precision) {
+  SED_REQUIRE(precision == 0 || precision == 1, 1, "precision must be SED_PREC_FP64 or SED_PREC_MIXED");
+  SED_REQUIRE(n_bil == 0 || (bil_ij && bil_t), 1, "bilinear arrays must not be NULL");
+  SED_REQUIRE(n_den == 0 || (den_ij && den_v), 1, "density arrays must not be NULL");
+  const SectorImpl& S = *sp;
+  const CatalogImpl& C = *S.cat;
+  const GroupImpl& G = *C.group;
+  check_hermitian_symmetric(G, n_bil, bil_ij, bil_t);
+  for (int k = 0; k < n_den; ++k)
+    SED_REQUIRE(den_ij[2 * k] >= 0 && den_ij[2 * k] < G.n_site && den_ij[2 * k + 1] >= 0 &&
+                    den_ij[2 * k + 1] < G.n_site,
+                1, "density term site index out of range");
+  auto op = std::make_shared<OpImpl>();
+  op->sec = sp;
+  op->precision = precision;
+  SED_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  op->own_stream = true;
+  cudaStream_t s = op->stream;
+  build_term_tables(G, n_bil, bil_ij, bil_t, op->terms);
+  const TermTables& tt = op->terms;
+  upload(op->site_off, tt.site_off, s);
+  upload(op->rec, tt.rec, s);
+  // tchi[u][h] = conj(t_u) * chi(h), and the plain amplitude / chi tables
+  const int nG = G.n_ops;
+  std::vector<double> tchi((size_t)tt.n_class * nG * 2);
+  for (int u = 0; u < tt.n_class; ++u)
+    for (int h = 0; h < nG; ++h) {
+      const double tr = tt.amp[2 * u], ti = -tt.amp[2 * u + 1];
+      const double cr = S.chi[2 * h], ci = S.chi[2 * h + 1];
+      tchi[((size_t)u * nG + h) * 2] = tr * cr - ti * ci;
+      tchi[((size_t)u * nG + h) * 2 + 1] = tr * ci + ti * cr;
+    }
+  std::vector<double> ampc(tt.amp);
+  for (size_t u = 1; u < ampc.size(); u += 2) ampc[u] = -ampc[u];  // conj(t)
+  auto to32 = [](const std::vector<double>& v) {
+    std::vector<float> f(v.size());
+    for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
+    return f;
+  };
+  // one buffer per precision holding [tchi | conj(amp) | chi | eta]
+  std::vector<double> eta(G.phase);
+  std::vector<double> pack;
+  pack.insert(pack.end(), tchi.begin(), tchi.end());
+  pack.insert(pack.end(), ampc.begin(), ampc.end());
+  pack.insert(pack.end(), S.chi.begin(), S.chi.end());
+  pack.insert(pack.end(), eta.begin(), eta.end());
+  upload(op->tchi64, pack, s);
+  upload(op->tchi32, to32(pack), s);
+  // density-density diagonal (SRE:697-703)
+  op->den_ij.assign(den_ij, den_ij + 2 * n_den);
+  op->den_v.assign(den_v, den_v + 2 * n_den);
+  DevBuf dij, dv;
+  upload(dij, op->den_ij, s);
+  upload(dv, op->den_v, s);
+  op->diag.alloc((size_t)std::max<int64_t>(C.n_orbits, 1) * 16);
+  if (C.n_orbits) {
+    k_diag<<<grid1(C.n_orbits, 256), 256, 0, s>>>(C.n_orbits, C.reps.as<uint64_t>(), S.rowflag.as<uint8_t>(), n_den,
+                                             dij.as<int32_t>(), dv.as<double2>(), op->diag.as<double2>());
+    SED_CUDA(cudaGetLastError());
+  }
+  SED_CUDA(cudaStreamSynchronize(s));
+  op->tchi_in_smem = (size_t)tt.n_class * nG * 16 <= 48 * 1024;
+  return op;
+}
+
+static ApplyArgs make_args(const OpImpl& op, bool fp32) {
+  const SectorImpl& S = *op.sec;
+  const CatalogImpl& C = *S.cat;
+  const GroupImpl& G = *C.group;
+  const TermTables& tt = op.terms;
+  ApplyArgs a{};
+  a.n_orb = C.n_orbits;
+  a.N = G.n_site;
+  a.G = G.n_ops;
+  a.n_class = tt.n_class;
+  a.n_terms = tt.n_terms;
+  a.reps = C.reps.as<uint64_t>();
+  a.stab = C.stab.as<uint8_t>();
+  a.rowflag = S.rowflag.as<uint8_t>();
+  a.diag = op.diag.as<double2>();
+  a.state = C.state.as<uint64_t>();
+  a.rank_tab = C.rank.dev.as<uint32_t>();
+  a.rp = C.rank.rp;
+  a.site_off = op.site_off.as<uint16_t>();
+  a.rec = op.rec.as<uint32_t>();
+  const size_t el = fp32 ? 8 : 16;
+  const unsigned char* base = (const unsigned char*)(fp32 ? op.tchi32.p : op.tchi64.p);
+  a.tchi = base;
+  a.amp = base + (size_t)tt.n_class * G.n_ops * el;
+  a.chi = base + ((size_t)tt.n_class * G.n_ops + tt.n_class) * el;
+  a.eta = base + ((size_t)tt.n_class * G.n_ops + tt.n_class + G.n_ops) * el;
+  a.inv = C.inv_u8.as<uint8_t>();
+  return a;
+}
+
+template <class P, bool F, bool PH, bool T>
+static void launch_apply(const ApplyArgs& a, const void* xs, double* y, cudaStream_t s) {
+  using V = typename P::V;
+  const SmemLayout<V> L = SmemLayout<V>::make(a, T);
+  auto kern = k_apply<P, F, PH, T>;
+  static size_t configured = 0;
+  if (L.total > 48 * 1024 && L.total > configured) {
+    SED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
+    configured = L.total;
+  }
+  SED_REQUIRE(L.total <= 200 * 1024, 5, "operator tables exceed the shared-memory budget");
+  int blocks_per_sm = 0;
+  SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, 256, L.total));
+  blocks_per_sm = std::max(blocks_per_sm, 1);
+  const int64_t want = (a.n_orb + 255) / 256;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * blocks_per_sm));
+  kern<<<grid, 256, L.total, s>>>(a, L, reinterpret_cast<const V*>(xs), reinterpret_cast<double2*>(y));
+  SED_CUDA(cudaGetLastError());
+}
+
+template <class P>
+static void dispatch_apply(const ApplyArgs& a, bool fermi, bool phases, bool table, const void* xs, double* y,
+                           cudaStream_t s) {
+  if (fermi) {
+    if (phases) {
+      if (table) launch_apply<P, true, true, true>(a, xs, y, s);
+      else launch_apply<P, true, true, false>(a, xs, y, s);
+    } else {
+      if (table) launch_apply<P, true, false, true>(a, xs, y, s);
+      else launch_apply<P, true, false, false>(a, xs, y, s);
+    }
+  } else {
+    if (phases) {
+      if (table) launch_apply<P, false, true, true>(a, xs, y, s);
+      else launch_apply<P, false, true, false>(a, xs, y, s);
+    } else {
+      if (table) launch_apply<P, false, false, true>(a, xs, y, s);
+      else launch_apply<P, false, false, false>(a, xs, y, s);
+    }
+  }
+}
+
+static void apply_impl(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s) {
+  const GroupImpl& G = *op.sec->cat->group;
+  if (op.sec->cat->n_orbits == 0) return;
+  const ApplyArgs a = make_args(op, fp32);
+  if (fp32)
+    dispatch_apply<P32>(a, G.stats == 1, G.has_phases, op.tchi_in_smem, xs, ypad, s);
+  else
+    dispatch_apply<P64>(a, G.stats == 1, G.has_phases, op.tchi_in_smem, xs, ypad, s);
+}
+
+void op_apply_orbit(OpImpl& op, const void* xs, double* ypad, cudaStream_t s) {
+  apply_impl(op, op.precision == 1, xs, ypad, s);
+}
+
+// FP64 matvec regardless of the op precision (the polish step of mixed solves)
+void op_apply_orbit64(OpImpl& op, const void* xs64, double* ypad, cudaStream_t s) {
+  apply_impl(op, false, xs64, ypad, s);
+}
+
+void op_scale_to_xs_prec(OpImpl& op, const double* v, void* xs, bool fp32, cudaStream_t s) {
+  const CatalogImpl& C = *op.sec->cat;
+  if (!C.n_orbits) return;
+  if (fp32)
+    k_scale_xs<float2><<<grid1(C.n_orbits, 256), 256, 0, s>>>(C.n_orbits, (const double2*)v, C.stab.as<uint8_t>(),
+                                                          (float2*)xs);
+  else
+    k_scale_xs<double2><<<grid1(C.n_orbits, 256), 256, 0, s>>>(C.n_orbits, (const double2*)v, C.stab.as<uint8_t>(),
+                                                           (double2*)xs);
+  SED_CUDA(cudaGetLastError());
+}
+
+void op_scale_to_xs(OpImpl& op, const double* v, void* xs, cudaStream_t s) {
+  op_scale_to_xs_prec(op, v, xs, op.precision == 1, s);
+}
+
+void expand_vec(const SectorImpl& S, const double* xsec, double* xpad, cudaStream_t s) {
+  const int64_t n = S.cat->n_orbits;
+  SED_CUDA(cudaMemsetAsync(xpad, 0, (size_t)n * 16, s));
+  if (S.dim) {
+    k_expand_vec<<<grid1(S.dim, 256), 256, 0, s>>>(S.dim, S.row_orbit.as<uint32_t>(), (const double2*)xsec,
+                                              (double2*)xpad);
+    SED_CUDA(cudaGetLastError());
+  }
+}
+
+void compress_vec(const SectorImpl& S, const double* ypad, double* ysec, cudaStream_t s) {
+  if (S.dim) {
+    k_compress_vec<<<grid1(S.dim, 256), 256, 0, s>>>(S.dim, S.row_orbit.as<uint32_t>(), (const double2*)ypad,
+                                                (double2*)ysec);
+    SED_CUDA(cudaGetLastError());
+  }
+}
+
+void op_apply_host(OpImpl& op, const double* x, double* y, int64_t n, bool device_ptrs) {
+  const SectorImpl& S = *op.sec;
+  SED_REQUIRE(n == S.dim, 1, "vector length must equal the sector dimension");
+  SED_REQUIRE(x != nullptr && y != nullptr, 1, "x and y must not be NULL");
+  const int64_t n_orb = S.cat->n_orbits;
+  cudaStream_t s = op.stream;
+  if (!op.xs.p) {
+    op.xs.alloc((size_t)std::max<int64_t>(n_orb, 1) * 16);
+    op.ypad.alloc((size_t)std::max<int64_t>(n_orb, 1) * 16);
+  }
+  const double* xsec = x;
+  double* ysec = y;
+  if (!device_ptrs) {
+    if (!op.xsec.p) {
+      op.xsec.alloc((size_t)std::max<int64_t>(n, 1) * 16);
+      op.ysec.alloc((size_t)std::max<int64_t>(n, 1) * 16);
+    }
+    if (n) SED_CUDA(cudaMemcpyAsync(op.xsec.p, x, (size_t)n * 16, cudaMemcpyHostToDevice, s));
+    xsec = op.xsec.as<double>();
+    ysec = op.ysec.as<double>();
+  }
+  // ypad doubles as the expanded (unscaled) input before the matvec overwrites it
+  expand_vec(S, xsec, op.ypad.as<double>(), s);
+  op_scale_to_xs(op, op.ypad.as<double>(), op.xs.p, s);
+  op_apply_orbit(op, op.xs.p, op.ypad.as<double>(), s);
+  compress_vec(S, op.ypad.as<double>(), ysec, s);
+  if (!device_ptrs) {
+    if (n) SED_CUDA(cudaMemcpyAsync(y, op.ysec.p, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+    SED_CUDA(cudaStreamSynchronize(s));
+  }
+}
+
+int64_t op_count_hops(OpImpl& op) {
+  if (op.hops >= 0) return op.hops;
+  const SectorImpl& S = *op.sec;
+  const CatalogImpl& C = *S.cat;
+  DevBuf tot(8);
+  SED_CUDA(cudaMemsetAsync(tot.p, 0, 8, op.stream));
+  if (C.n_orbits)
+    k_count_hops<<<grid1(C.n_orbits, 256), 256, 0, op.stream>>>(C.n_orbits, C.reps.as<uint64_t>(), S.rowflag.as<uint8_t>(),
+                                                           C.group->n_site, op.site_off.as<uint16_t>(),
+                                                           op.rec.as<uint32_t>(), tot.as<unsigned long long>());
+  SED_CUDA(cudaGetLastError());
+  unsigned long long h = 0;
+  SED_CUDA(cudaMemcpyAsync(&h, tot.p, 8, cudaMemcpyDeviceToHost, op.stream));
+  SED_CUDA(cudaStreamSynchronize(op.stream));
+  op.hops = (int64_t)h;
+  return op.hops;
+}
+
+}  // namespace sed

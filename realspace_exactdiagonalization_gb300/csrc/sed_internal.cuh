@@ -1,0 +1,299 @@
+// sed_internal.cuh -- shared definitions of the GB300 sector library.
+//
+// Device data layout (one catalog serves every momentum and every flux twist
+// that shares the same permutations):
+//   state[rank]   uint64 per fixed-filling basis state, indexed by the colex
+//                 rank of its mask:
+//                   bits  0..31 orbit index (0xFFFFFFFF = unset)
+//                   bits 32..39 g, the last (largest) group element with
+//                               g(rep) = state (SRE:461-466, last write wins)
+//                   bit  40     sign of the fermionic reordering of g on rep
+//                   bits 41..47 stabilizer order of the orbit
+//   reps[orbit]   uint64 representative mask (ascending = catalog order)
+//   stab[orbit]   uint8 stabilizer order
+// Sector vectors on the device are indexed by catalog orbit (length n_orbits);
+// entries of orbits outside the sector are exactly zero.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#define SED_MAX_SITES 63
+#define SED_MAX_OPS 64
+#define SED_UNSET_ORBIT 0xFFFFFFFFu
+
+namespace sed {
+
+// ------------------------------------------------------------------ errors
+void set_error(const std::string& msg);
+struct Error {
+  int code;
+  std::string msg;
+};
+#define SED_CUDA(call)                                                                              \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess)                                                                          \
+      throw ::sed::Error{2, std::string(#call " failed: ") + cudaGetErrorString(e_) + " at " __FILE__}; \
+  } while (0)
+#define SED_REQUIRE(cond, code, msg)      \
+  do {                                    \
+    if (!(cond)) throw ::sed::Error{code, msg}; \
+  } while (0)
+
+// ------------------------------------------------------------ device buffer
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t n) { alloc(n); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { reset(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+    return *this;
+  }
+  ~DevBuf() { reset(); }
+  void alloc(size_t n) {
+    reset();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw Error{3, std::string("cudaMalloc of ") + std::to_string(n) + " bytes failed: " + cudaGetErrorString(e)};
+    }
+    bytes = n;
+  }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+template <class T>
+inline void upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
+  b.alloc(v.size() * sizeof(T));
+  if (!v.empty()) SED_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+// ------------------------------------------------------------ rank tables
+// Colex rank of a k-subset, sum_j binom(b_j, j+1) (SRE:231-243), evaluated
+// one byte of the mask at a time: entry [c][p][v] is the contribution of byte
+// value v in chunk c when p set bits lie below the chunk.  Tables hold
+// uint32 (binomial(n, k) < 2^32 is a library limit) and live in shared memory.
+struct RankParams {
+  int nchunk;
+  int total;  // entries
+  int off[8];
+  int pmin[8];
+};
+
+struct RankTable {
+  RankParams rp{};
+  std::vector<uint32_t> host;
+  DevBuf dev;
+};
+void build_rank_table(int n_site, int k, RankTable& rt, cudaStream_t s);
+
+// host binomial table (exact int64)
+int64_t binom64(int n, int k);
+
+// ------------------------------------------------------------------ objects
+struct GroupImpl {
+  int n_site = 0, n_ops = 0, identity = 0, stats = 0;
+  std::vector<int32_t> perm;  // n_ops * n_site
+  std::vector<double> phase;  // n_ops * n_site * 2
+  std::vector<int32_t> inv;
+  bool has_phases = false;    // some eta differs from exactly 1+0i
+};
+
+struct CatalogImpl {
+  std::shared_ptr<GroupImpl> group;
+  int n_filled = 0;
+  int64_t n_states = 0, n_orbits = 0, n_stab_total = 0;
+  RankTable rank;
+  DevBuf state, reps, stab;            // see layout above
+  DevBuf perm_u8, inv_u8, phase, binom;  // perm_u8: [n_ops][64]
+  std::vector<uint8_t> stab_host;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  ~CatalogImpl();
+  void upload_group_phases();
+};
+
+struct SectorImpl {
+  std::shared_ptr<CatalogImpl> cat;
+  std::vector<double> chi;  // n_ops * 2
+  double atol = 1e-12;
+  int64_t dim = 0;
+  DevBuf rowflag;    // uint8[n_orbits], 1 if the orbit belongs to the sector
+  DevBuf row_orbit;  // uint32[dim]
+  cudaStream_t stream() const { return cat->stream; }
+};
+
+// Hop records in shared memory: for every from-site i, records
+// [site_off[i], site_off[i+1]) hold (to-site | amplitude-class << 8).
+struct TermTables {
+  int n_site = 0, n_terms = 0, n_class = 0;
+  std::vector<uint16_t> site_off;  // n_site + 1
+  std::vector<uint32_t> rec;       // n_terms
+  std::vector<double> amp;         // n_class * 2: distinct amplitudes t
+};
+
+struct ApplyWork;
+
+struct OpImpl {
+  std::shared_ptr<SectorImpl> sec;
+  int precision = 0;
+  TermTables terms;
+  std::vector<double> diag_host;  // density terms stay on the host until upload
+  std::vector<int32_t> den_ij;
+  std::vector<double> den_v;
+  DevBuf site_off, rec;           // term tables
+  DevBuf tchi64, tchi32;          // [n_class][n_ops] conj(t_u) * chi(h)
+  DevBuf eta64, eta32;            // [n_ops][n_site] per-site phases (twisted groups)
+  DevBuf diag;                    // double2[n_orbits] density-density diagonal
+  DevBuf xs, ypad, xsec, ysec;    // work vectors for sed_op_apply
+  int64_t hops = -1;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  size_t smem_bytes = 0;
+  bool tchi_in_smem = true;
+  ~OpImpl();
+};
+
+// ----------------------------------------------------------- entry points
+std::shared_ptr<GroupImpl> make_group(int n_site, int n_ops, const int32_t* perm, const double* phase, int identity,
+                                      int stats);
+std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> g, int n_filled);
+void catalog_readback(const CatalogImpl& c, int field, void* out, int64_t out_bytes);
+void catalog_update_phases(CatalogImpl& c, std::shared_ptr<GroupImpl> g);
+std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> c, const double* chi, double atol);
+void sector_readback(const SectorImpl& s, uint64_t* reps, int32_t* stab, int32_t* orbit);
+std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> s, int n_bil, const int32_t* bil_ij, const double* bil_t,
+                                int n_den, const int32_t* den_ij, const double* den_v, int precision);
+void build_term_tables(const GroupImpl& G, int n_bil, const int32_t* bil_ij, const double* bil_t, TermTables& tt);
+void check_hermitian_symmetric(const GroupImpl& G, int n_bil, const int32_t* bil_ij, const double* bil_t);
+void op_apply_host(OpImpl& op, const double* x, double* y, int64_t n, bool device_ptrs);
+// y_pad (complex128, orbit-indexed) = H x given xs = sqrt(stab) * x in the op precision
+void op_apply_orbit(OpImpl& op, const void* xs, double* ypad, cudaStream_t s);
+// xs = sqrt(stab) * v (cast to the op precision); v orbit-indexed complex128
+void op_scale_to_xs(OpImpl& op, const double* v, void* xs, cudaStream_t s);
+int64_t op_count_hops(OpImpl& op);
+
+struct SolveResult {
+  int status = 0;
+  int restarts = 0, matvecs = 0, matvecs64 = 0, converged = 0;
+  double max_residual = 0, max_delta = 0, seconds = 0;
+};
+SolveResult solve(OpImpl& op, int nev, double tol, int maxiter, int krylovdim, uint64_t seed, double* evals,
+                  double* evecs);
+
+// small dense eigen-solvers (host)
+void eigh_real_sym(int n, std::vector<double>& A, std::vector<double>& w, std::vector<double>& Z);
+void eigh_complex_herm(int n, const std::vector<double>& Hreim, std::vector<double>& w, std::vector<double>& Zreim);
+
+int device_sm_count();
+int grid1(int64_t work, int block);
+void compute_diag(int64_t n_orb, const uint64_t* reps, const uint8_t* rowflag, int n_den, const int32_t* den_ij,
+                  const double2* den_v, double2* diag, cudaStream_t s);
+
+}  // namespace sed
+
+// ============================================================ device helpers
+namespace sed {
+namespace dev {
+
+__device__ __forceinline__ uint64_t gosper_next(uint64_t x) {
+  uint64_t c = x & (0ULL - x);
+  uint64_t r = x + c;
+  return (((r ^ x) >> 2) >> (__ffsll((long long)x) - 1)) | r;
+}
+
+// bits of m strictly above position q (q in [0, 63])
+__device__ __forceinline__ uint64_t bits_above(uint64_t m, int q) { return m & ~((2ULL << q) - 1ULL); }
+
+// bits strictly between positions a and b
+__device__ __forceinline__ uint64_t bits_between(int a, int b) {
+  int lo = min(a, b), hi = max(a, b);
+  return (hi - lo <= 1) ? 0ULL : (((1ULL << (hi - lo - 1)) - 1ULL) << (lo + 1));
+}
+
+__device__ __forceinline__ uint32_t rank_of(uint64_t m, const uint32_t* __restrict__ tab, const RankParams& rp) {
+  uint32_t r = 0;
+  int p = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    if (c < rp.nchunk) {
+      const uint32_t v = (uint32_t)(m >> (8 * c)) & 0xFFu;
+      r += tab[rp.off[c] + ((p - rp.pmin[c]) << 8) + v];
+      p += __popc(v);
+    }
+  }
+  return r;
+}
+
+// Permutation image of m (bit i -> bit perm[i]) and the parity of the
+// fermionic reordering (SRE:146-163 counts set bits above each new position).
+__device__ __forceinline__ uint64_t apply_perm(uint64_t m, const uint8_t* perm) {
+  uint64_t r = 0;
+  while (m) {
+    const int i = __ffsll((long long)m) - 1;
+    m &= m - 1;
+    r |= 1ULL << perm[i];
+  }
+  return r;
+}
+__device__ __forceinline__ uint64_t apply_perm_parity(uint64_t m, const uint8_t* perm, int* parity) {
+  uint64_t r = 0;
+  int s = 0;
+  while (m) {
+    const int i = __ffsll((long long)m) - 1;
+    m &= m - 1;
+    const int q = perm[i];
+    s ^= __popcll(bits_above(r, q));
+    r |= 1ULL << q;
+  }
+  *parity = s & 1;
+  return r;
+}
+
+// Non-fused complex product (each multiply and add separately rounded), the
+// evaluation the reference's tables are reproduced with.
+__device__ __forceinline__ double2 cmul_rn(double2 a, double2 b) {
+  return make_double2(__dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)),
+                      __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
+}
+
+// Full group action with amplitude (SRE:132-163): phase product in lsb-first
+// order, times the reordering sign for fermions.
+__device__ __forceinline__ uint64_t apply_full(uint64_t m, const uint8_t* perm, const double2* __restrict__ phase,
+                                               int fermi, double2* amp) {
+  uint64_t r = 0;
+  double2 ph = make_double2(1.0, 0.0);
+  int s = 0;
+  while (m) {
+    const int i = __ffsll((long long)m) - 1;
+    m &= m - 1;
+    const int q = perm[i];
+    if (fermi) s ^= __popcll(bits_above(r, q));
+    r |= 1ULL << q;
+    ph = cmul_rn(ph, phase[i]);
+  }
+  if (fermi) {
+    const double sg = (s & 1) ? -1.0 : 1.0;
+    ph = make_double2(__dmul_rn(ph.x, sg), __dmul_rn(ph.y, sg));
+  }
+  *amp = ph;
+  return r;
+}
+
+}  // namespace dev
+}  // namespace sed

@@ -1,0 +1,127 @@
+// sed_rowgather.cuh -- one row of the sector Hamiltonian, gathered.
+//
+// Shared by the device-wide matvec (sed_hamiltonian.cu) and the batched
+// per-CTA solver (sed_batched.cu).  For the representative m of row r it walks
+// the hops out of m (occupied site i -> empty site j, hop records grouped by
+// from-site), and accumulates conj(H_cr) xs_c:
+//   coef = tchi[u][h] * sign * conj(P_h(new)),  tchi[u][h] = conj(t_u) chi(h)
+// (reference: apply_hamiltonian!, src/symmetry_resolved_ed.jl:813-878, whose
+// column element is t * s_JW * alpha * conj(chi) * sqrt(stab_row/stab_col)).
+// The hop walk is software-pipelined: the state-table load of the next hop is
+// issued before the current hop is consumed, so every thread keeps two
+// independent random loads in flight.
+#pragma once
+
+#include "sed_internal.cuh"
+
+namespace sed {
+
+struct P64 {
+  using V = double2;
+  using S = double;
+  __device__ static __forceinline__ V make(S a, S b) { return make_double2(a, b); }
+};
+struct P32 {
+  using V = float2;
+  using S = float;
+  __device__ static __forceinline__ V make(S a, S b) { return make_float2(a, b); }
+};
+
+// Iterator over the valid hops of one representative.
+struct HopIter {
+  uint64_t m, occ;
+  int i, t, t1;
+  __device__ __forceinline__ void init(uint64_t m_, const uint16_t* s_off) {
+    m = m_;
+    occ = m_;
+    i = -1;
+    t = t1 = 0;
+  }
+  // advance to the next hop with an empty target; false when exhausted
+  __device__ __forceinline__ bool next(const uint16_t* s_off, const uint32_t* s_rec, uint32_t& rec, int& from) {
+    for (;;) {
+      while (t < t1) {
+        const uint32_t r = s_rec[t++];
+        if (!((m >> (r & 0xFF)) & 1ULL)) {
+          rec = r;
+          from = i;
+          return true;
+        }
+      }
+      if (!occ) return false;
+      i = __ffsll((long long)occ) - 1;
+      occ &= occ - 1;
+      t = s_off[i];
+      t1 = s_off[i + 1];
+    }
+  }
+};
+
+template <class P, bool FERMI, bool PHASES, bool TABLE>
+__device__ __forceinline__ void row_gather(uint64_t m, const typename P::V* __restrict__ xs,
+                                           const typename P::V* tab,  // TABLE ? tchi[u][G] : conj(t_u)
+                                           const typename P::V* chi, int G, const typename P::V* __restrict__ eta,
+                                           int N, const uint32_t* s_rank, const RankParams& rp,
+                                           const uint32_t* s_rec, const uint16_t* s_off, const uint8_t* s_inv,
+                                           const uint64_t* __restrict__ state, typename P::S& ar,
+                                           typename P::S& ai) {
+  using V = typename P::V;
+  using S = typename P::S;
+  HopIter it;
+  it.init(m, s_off);
+  uint32_t rec_n;
+  int from_n;
+  bool have = it.next(s_off, s_rec, rec_n, from_n);
+  uint64_t w_n = 0;
+  uint64_t nw_n = 0;
+  if (have) {
+    nw_n = m ^ ((1ULL << from_n) | (1ULL << (rec_n & 0xFF)));
+    w_n = __ldg(state + dev::rank_of(nw_n, s_rank, rp));
+  }
+  while (have) {
+    const uint32_t rec = rec_n;
+    const int i = from_n;
+    const uint64_t nw = nw_n;
+    const uint64_t w = w_n;
+    // prefetch the next hop's state word
+    have = it.next(s_off, s_rec, rec_n, from_n);
+    if (have) {
+      nw_n = m ^ ((1ULL << from_n) | (1ULL << (rec_n & 0xFF)));
+      w_n = __ldg(state + dev::rank_of(nw_n, s_rank, rp));
+    }
+    const int j = rec & 0xFF;
+    const uint32_t c = (uint32_t)w;
+    const int g = (int)((w >> 32) & 0xFF);
+    int neg = (int)((w >> 40) & 1);
+    const V xc = xs[c];
+    const int h = s_inv[g];
+    const int u = (int)(rec >> 8);
+    V cf;
+    if (TABLE) {
+      cf = tab[u * G + h];
+    } else {
+      const V tt = tab[u], ch = chi[h];  // tt holds conj(t_u)
+      cf = P::make(tt.x * ch.x - tt.y * ch.y, tt.x * ch.y + tt.y * ch.x);
+    }
+    if (FERMI) neg ^= __popcll(m & dev::bits_between(i, j)) & 1;
+    if (PHASES) {
+      S pr = 1, pi = 0;
+      uint64_t b = nw;
+      const V* eh = eta + (size_t)h * N;
+      while (b) {
+        const int q = __ffsll((long long)b) - 1;
+        b &= b - 1;
+        const V e = eh[q];
+        const S nr = pr * e.x - pi * e.y;
+        pi = pr * e.y + pi * e.x;
+        pr = nr;
+      }
+      cf = P::make(cf.x * pr + cf.y * pi, cf.y * pr - cf.x * pi);  // * conj(P)
+    }
+    if (neg) cf = P::make(-cf.x, -cf.y);
+    ar += cf.x * xc.x - cf.y * xc.y;
+    ai += cf.x * xc.y + cf.y * xc.x;
+  }
+}
+
+}  // namespace sed
