@@ -344,6 +344,75 @@ def run_ours(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_large(args):
+    """One large sector: checkerboard 4x6 spinless fermions (48 sites, NN t=1
+    e^{+-i pi/4}, NNN +-0.3, NNNN -0.2, V=1), Np=8, k=(0,0), nev=3.  Reports
+    the device catalog build, the H|psi> kernel in FP64 and complex64 (GB/s of
+    algorithmic bytes against the HBM peak), and the FP64 / mixed solves."""
+    import torch
+
+    import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300 import lattice as L
+
+    torch.cuda.set_device(0)
+    L1, L2, npart = args.large_shape
+    spec = L.checkerboard(L1, L2, n_filled=npart)
+    G = L.build_translation_group(spec.lattice)
+    t0 = time.perf_counter()
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G, particle_statistics=A.Fermionic())
+    t_cat = time.perf_counter() - t0
+    irr = L.build_translation_irrep_list(G, spec.lattice)[0]
+    t0 = time.perf_counter()
+    basis = A.build_symmetry_sector_basis(cat, irr)
+    t_sec = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    res = {}
+    peak, peak_kind = measured_peak()
+    for prec in ("fp64", "mixed"):
+        H = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms(), spec.density_terms, precision=prec)
+        info = H.info()
+        from realspace_exactdiagonalization_gb300 import _lib
+        import ctypes as C
+
+        _lib.check(_lib.load().sed_op_set_stream(H.handle, C.c_void_p(stream.cuda_stream)))
+        n_orb = info["n_orbits"]
+        s = 16 if prec == "fp64" else 8
+        xs = torch.randn(n_orb * 2, dtype=torch.float64 if prec == "fp64" else torch.float32, device="cuda")
+        y = torch.empty(n_orb * 2, dtype=torch.float64, device="cuda")
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        for _ in range(2):
+            _lib.check(_lib.load().sed_op_apply_orbit(H.handle, C.c_void_p(xs.data_ptr()), C.c_void_p(y.data_ptr())))
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(_lib.load().sed_op_apply_orbit(H.handle, C.c_void_p(xs.data_ptr()), C.c_void_p(y.data_ptr())))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        t_mv = statistics.median(ms) / 1e3
+        b_alg = info["dim"] * (8 + 4 + 2 * s) + info["hops"] * (4 + 1 + 4 + s)
+        r = {"matvec_ms": 1e3 * t_mv, "bytes_alg": b_alg, "achieved_gbs": b_alg / t_mv / 1e9,
+             "frac": b_alg / t_mv / 1e9 / peak, "hops": info["hops"]}
+        if not args.no_solve:
+            t0 = time.perf_counter()
+            vals, _, sinfo = H.solve(3, tol=1e-10, want_vectors=False)
+            r.update({"solve_s": time.perf_counter() - t0, "evals": [float(v) for v in vals],
+                      "matvecs": sinfo.n_matvec, "matvecs_fp64": sinfo.n_matvec_fp64,
+                      "max_residual": sinfo.max_residual, "delta_polish": sinfo.max_delta_polish})
+        res[prec] = r
+        del H
+    if "evals" in res.get("fp64", {}) and "evals" in res.get("mixed", {}):
+        e64, em = np.array(res["fp64"]["evals"]), np.array(res["mixed"]["evals"])
+        res["max_rel_dE_mixed_vs_fp64"] = float(np.max(np.abs(em - e64) / np.abs(e64)))
+    line = {"workload": f"checkerboard{L1}x{L2}_np{npart}_k00", "n_states": cat.n_states, "n_orbits": cat.n_orbits,
+            "dim": basis.dim, "catalog_build_s": t_cat, "sector_build_s": t_sec, "peak_gbs": peak,
+            "peak_kind": peak_kind, **res}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -354,7 +423,13 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=6)
     ap.add_argument("--ref-sample", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="flux_scan", choices=["flux_scan", "large"])
+    ap.add_argument("--large-shape", type=int, nargs=3, default=[4, 6, 8], metavar=("L1", "L2", "NP"))
+    ap.add_argument("--no-solve", action="store_true")
     args = ap.parse_args()
+    if args.workload == "large":
+        run_large(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

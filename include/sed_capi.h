@@ -108,6 +108,11 @@ int sed_sector_build(const sed_catalog* c, const double* chi_reim, double atol, 
 /* representative_mask_list, stabilizer_order_list and the catalog orbit index
  * of every sector row (any pointer may be NULL). */
 int sed_sector_get(const sed_sector* s, uint64_t* reps, int32_t* stab_order, int32_t* orbit_index);
+/* project_to_sector (SRE:627-632) for n masks with the catalog's filling:
+ * row_out[i] = 0-based sector row of the orbit of masks[i] (-1 when the
+ * orbit is not in the sector), coeff_out[i] = rep_amp * conj(chi(rep_sym)),
+ * bit-exact with the reference's evaluation order. */
+int sed_sector_project(const sed_sector* s, int64_t n, const uint64_t* masks, int64_t* row_out, double* coeff_reim);
 void sed_sector_destroy(sed_sector* s);
 
 /* --------------------------------------------------------------- operator */

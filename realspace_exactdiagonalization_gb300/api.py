@@ -222,6 +222,15 @@ class Symmetry_Sector_Basis(_Handle):
     def orbit_index_list(self) -> np.ndarray:
         return self._load()[2]
 
+    def project(self, masks) -> Tuple[np.ndarray, np.ndarray]:
+        """project_to_sector (SRE:627-632) for many masks: (1-based rows, 0 when
+        the orbit is outside the sector; coefficients)."""
+        m = np.ascontiguousarray(masks, dtype=np.uint64)
+        rows = np.zeros(len(m), dtype=np.int64)
+        coeff = np.zeros(len(m), dtype=np.complex128)
+        check(_lib.load().sed_sector_project(self._h, len(m), ptr(m), ptr(rows), ptr(coeff)))
+        return rows + 1, coeff
+
     @property
     def representative_mask_to_mask_idx_map(self) -> Dict[int, int]:
         if self._map is None:

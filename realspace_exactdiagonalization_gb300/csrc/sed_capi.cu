@@ -133,6 +133,12 @@ int sed_sector_get(const sed_sector* s, uint64_t* reps, int32_t* stab_order, int
     sed::sector_readback(*s->p, reps, stab_order, orbit_index);
   });
 }
+int sed_sector_project(const sed_sector* s, int64_t n, const uint64_t* masks, int64_t* row_out, double* coeff_reim) {
+  return guarded([&] {
+    REQ(s, "NULL sector");
+    sed::sector_project(*s->p, n, masks, row_out, coeff_reim);
+  });
+}
 void sed_sector_destroy(sed_sector* s) { delete s; }
 
 int sed_op_create(const sed_sector* s, int n_bil, const int32_t* bil_ij, const double* bil_t_reim, int n_den,

@@ -608,6 +608,69 @@ __global__ void k_sector_gather(int64_t dim, const uint32_t* __restrict__ row_or
   }
 }
 
+// project_to_sector (SRE:627-632): rank -> state word -> (orbit, g); the
+// coefficient is rep_amp * conj(chi(rep_sym)) with rep_amp = conj(alpha_g(rep)).
+__global__ void k_sector_project(int64_t n, const uint64_t* __restrict__ masks, const uint64_t* __restrict__ state,
+                                 const uint64_t* __restrict__ reps, const int32_t* __restrict__ orbit_row, int G,
+                                 int N, int fermi, const uint8_t* __restrict__ perm_g, const uint8_t* __restrict__ inv,
+                                 const double2* __restrict__ phase, const double2* __restrict__ chi,
+                                 const uint32_t* __restrict__ rank_tab, RankParams rp, int64_t* row_out,
+                                 double2* coeff_out) {
+  __shared__ uint8_t sperm[SED_MAX_OPS * 64];
+  for (int i = threadIdx.x; i < G * 64; i += blockDim.x) sperm[i] = perm_g[i];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t w = state[dev::rank_of(masks[i], rank_tab, rp)];
+    const uint32_t o = (uint32_t)w;
+    const int32_t r = o == SED_UNSET_ORBIT ? -1 : orbit_row[o];
+    row_out[i] = r;
+    if (r < 0) {
+      coeff_out[i] = make_double2(0.0, 0.0);
+      continue;
+    }
+    const int g = (int)((w >> 32) & 0xFF);
+    double2 a;
+    dev::apply_full(reps[o], sperm + g * 64, phase + (size_t)g * N, fermi, &a);
+    a.y = -a.y;  // rep_amp
+    const double2 c = chi[inv[g]];
+    coeff_out[i] = dev::cmul_rn(a, make_double2(c.x, -c.y));
+  }
+}
+
+__global__ void k_orbit_row(int64_t dim, const uint32_t* __restrict__ row_orbit, int32_t* __restrict__ orbit_row) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x)
+    orbit_row[row_orbit[r]] = (int32_t)r;
+}
+
+void sector_project(const SectorImpl& S, int64_t n, const uint64_t* masks, int64_t* rows, double* coeff) {
+  const CatalogImpl& c = *S.cat;
+  const GroupImpl& G = *c.group;
+  SED_REQUIRE(n >= 0 && (n == 0 || (masks && rows && coeff)), 1, "NULL argument");
+  const uint64_t valid = G.n_site == 64 ? ~0ULL : ((1ULL << G.n_site) - 1ULL);
+  for (int64_t i = 0; i < n; ++i)
+    SED_REQUIRE((masks[i] & ~valid) == 0 && __builtin_popcountll(masks[i]) == c.n_filled, 1,
+                "every mask must hold n_filled particles on the lattice sites");
+  if (n == 0) return;
+  cudaStream_t s = c.stream;
+  DevBuf orow((size_t)std::max<int64_t>(c.n_orbits, 1) * 4), dm((size_t)n * 8), dr((size_t)n * 8),
+      dc((size_t)n * 16), dchi;
+  SED_CUDA(cudaMemsetAsync(orow.p, 0xFF, (size_t)std::max<int64_t>(c.n_orbits, 1) * 4, s));
+  if (S.dim)
+    k_orbit_row<<<grid_for(S.dim, 256), 256, 0, s>>>(S.dim, S.row_orbit.as<uint32_t>(), orow.as<int32_t>());
+  upload(dchi, S.chi, s);
+  SED_CUDA(cudaMemcpyAsync(dm.p, masks, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+  k_sector_project<<<grid_for(n, 256), 256, 0, s>>>(n, dm.as<uint64_t>(), c.state.as<uint64_t>(), c.reps.as<uint64_t>(),
+                                                    orow.as<int32_t>(), G.n_ops, G.n_site, G.stats,
+                                                    c.perm_u8.as<uint8_t>(), c.inv_u8.as<uint8_t>(),
+                                                    c.phase.as<double2>(), dchi.as<double2>(),
+                                                    c.rank.dev.as<uint32_t>(), c.rank.rp, dr.as<int64_t>(),
+                                                    dc.as<double2>());
+  SED_CUDA(cudaGetLastError());
+  SED_CUDA(cudaMemcpyAsync(rows, dr.p, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+  SED_CUDA(cudaMemcpyAsync(coeff, dc.p, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+  SED_CUDA(cudaStreamSynchronize(s));
+}
+
 void sector_readback(const SectorImpl& S, uint64_t* reps, int32_t* stab, int32_t* orbit) {
   const CatalogImpl& c = *S.cat;
   cudaStream_t s = c.stream;

@@ -177,6 +177,7 @@ void catalog_readback(const CatalogImpl& c, int field, void* out, int64_t out_by
 void catalog_update_phases(CatalogImpl& c, std::shared_ptr<GroupImpl> g);
 std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> c, const double* chi, double atol);
 void sector_readback(const SectorImpl& s, uint64_t* reps, int32_t* stab, int32_t* orbit);
+void sector_project(const SectorImpl& s, int64_t n, const uint64_t* masks, int64_t* rows, double* coeff);
 std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> s, int n_bil, const int32_t* bil_ij, const double* bil_t,
                                 int n_den, const int32_t* den_ij, const double* den_v, int precision);
 void build_term_tables(const GroupImpl& G, int n_bil, const int32_t* bil_ij, const double* bil_t, TermTables& tt);

@@ -148,3 +148,60 @@ def test_golden_haldane3x4_ground_energy():
         assert basis.dim == 11240
         vals, _, info = H.solve(4, tol=1e-10)
         assert abs(vals[0] - (-14.301456146831118)) <= tol, (precision, vals[0], info.max_residual)
+
+
+@pytest.mark.parametrize("name", ["checkerboard3x2_f_flux", "checkerboard3x2_b_flux", "hubbard2x3"])
+def test_project_to_sector_bit_exact(oracle, name):
+    """project_to_sector (SRE:627-632) for every basis state, every sector:
+    same row and bit-identical coefficient as the oracle's table path, which
+    itself equals the O(|G|) path (flux_regression.jl:36-44)."""
+    import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300.groups import build_identity_group
+
+    case = case_by_name(name)
+    G = case.group()
+    Gid = build_identity_group(G.n_site)
+    masks = oracle.Catalog(Gid.perm0(), Gid.phases(), 0, case.stats_code, case.spec.n_filled).get(oracle.FIELD_REPS)
+    oc = oracle.Catalog(G.perm0(), G.phases(), G.identity_idx - 1, case.stats_code, case.spec.n_filled)
+    dc = _device(case)
+    for irr in case.irreps():
+        osec = oracle.Sector(oc, irr.array())
+        rows, coeff = A.build_symmetry_sector_basis(dc, irr).project(masks)
+        for m, r, c in zip(masks, rows, coeff):
+            ref = osec.project(int(m), 0)
+            if ref is None:
+                assert r == 0
+            else:
+                assert r == ref[0] + 1
+                assert np.array([c]).view(np.uint64).tolist() == np.array([ref[1]]).view(np.uint64).tolist()
+
+
+def test_flux_refresh_matches_fresh_build(oracle):
+    """update_orbit_stabilizer_phases! (SRE:338-369): a catalog built at zero
+    flux and refreshed to a twisted group equals one built at that twist."""
+    import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300.groups import statistics_from_name
+
+    case = case_by_name("checkerboard3x2_f_flux")
+    spec = case.spec
+    st = statistics_from_name(case.statistics)
+    from realspace_exactdiagonalization_gb300 import lattice as L
+
+    G0 = L.build_translation_group(spec.lattice, (0.0, 0.0))
+    Gt = case.group()
+    dc = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G0, particle_statistics=st)
+    A.update_orbit_stabilizer_phases_(dc, Gt, st)
+    oc = oracle.Catalog(G0.perm0(), G0.phases(), 0, case.stats_code, spec.n_filled)
+    oc.update_phases(Gt.phases())
+    fresh = oracle.Catalog(Gt.perm0(), Gt.phases(), 0, case.stats_code, spec.n_filled)
+    for f in (oracle.FIELD_STAB_PHASE, oracle.FIELD_REP_SYM, oracle.FIELD_REP_AMP):
+        np.testing.assert_array_equal(bits(oc.get(f)), bits(fresh.get(f)))
+        np.testing.assert_array_equal(bits(dc._get(f)), bits(fresh.get(f)))
+    for k, irr in enumerate(case.irreps()):
+        dsec = A.build_symmetry_sector_basis(dc, irr)
+        osec = oracle.Sector(fresh, irr.array())
+        assert dsec.dim == osec.dim
+        H = A.MatrixFreeHamiltonian(dsec, case.bilinear1(), case.density1())
+        op = oracle.Op(osec, case.bilinear0(), case.density0())
+        x = x_random(osec.dim, seed=k)
+        assert np.abs(H(x) - op.apply(x)).max() < 1e-11 * max(1, np.abs(op.apply(x)).max())
