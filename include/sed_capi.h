@@ -140,6 +140,18 @@ int sed_op_set_stream(sed_op* op, void* cuda_stream);
  * sqrt(stab)*x in the op's precision (complex64 or complex128, length
  * n_orbits), y_dev receives complex128 H x (length n_orbits).  Asynchronous. */
 int sed_op_apply_orbit(sed_op* op, const void* xs_dev, double* y_dev);
+/* y = H x for device vectors (sector order, complex128, length n == sector
+ * dim), allocating nothing: no counterpart in the reference.  For callers that
+ * may not call cudaMalloc while they work (a host whose memory pool owns the
+ * device memory, a serving loop that cannot afford cudaMalloc's implicit
+ * device-wide synchronisation, code with a fixed memory budget after set-up).
+ * Its work vectors live in a fixed 32 MiB device array inside this library,
+ * which every GPU that loads it keeps until exit; sectors whose catalog has
+ * more than 1048576 orbits are rejected with SED_ERR_LIMIT.  The first call on
+ * a device looks up that array's device address; make it before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU race:
+ * serialise them.  Asynchronous on the operator's stream. */
+int sed_op_apply_noalloc(sed_op* op, const double* x_dev, double* y_dev, int64_t n);
 void sed_op_destroy(sed_op* op);
 
 /* -------------------------------------------------------------------- solve */

@@ -66,6 +66,7 @@ SIGNATURES = [
     ("sed_op_info", _i32, [_p, _p, _p, _p]),
     ("sed_op_set_stream", _i32, [_p, _p]),
     ("sed_op_apply_orbit", _i32, [_p, _p, _p]),
+    ("sed_op_apply_noalloc", _i32, [_p, _p, _p, _i64]),
     ("sed_op_destroy", None, [_p]),
     ("sed_solve", _i32, [_p, _i32, _dbl, _i32, _i32, _u64, _p, _p, _p]),
     ("sed_batch_create", _i32, [_p, _i32, _p, _i32, _p, _p, _i32, _i32, _i32, _i32, _p]),
