@@ -328,7 +328,10 @@ def run_ours(args, rank, world):
                      "bytes_per_launch": bytes_launch,
                      "note": "algorithmic matvec bytes (D*(8+4+2s)+hops*(4+1+4+s), s=8) of all matvecs of one launch"},
         "cpu_baseline": cpu,
-        "gpu_launches": args.steps,
+        # one k_batch launch per step, plus the FP64 re-solve launch when a
+        # request's polish missed its target (inputs are identical every step)
+        "gpu_launches": args.steps * (1 + (stats["fp64_fallbacks"] > 0)),
+        "fp64_fallbacks_per_step": stats["fp64_fallbacks"],
         "clocks": clocks,
         "plain_fp64_dropin": {"solves_per_s": plain_rate, "sample": n_plain,
                               "p50_ms": 1e3 * plain_s * (n / 2 + 0.5), "p99_ms": 1e3 * plain_s * (0.99 * n + 1),
@@ -356,12 +359,21 @@ def run_large(args):
 
     torch.cuda.set_device(0)
     L1, L2, npart = args.large_shape
-    spec = L.checkerboard(L1, L2, n_filled=npart)
+    if args.large_model == "hubbard":
+        # config 3: Hubbard 4x4, t=1, U=8, 7+7 electrons in the reference's encoding
+        # (fixed total particle number over 2*L1*L2 modes), momentum (pi, 0)
+        spec = L.hubbard_square(L1, L2, n_filled=npart)
+        sector = (L1 // 2) * L2
+        name = f"hubbard{L1}x{L2}_n{npart}_k(pi,0)"
+    else:
+        spec = L.checkerboard(L1, L2, n_filled=npart)
+        sector = 0
+        name = f"checkerboard{L1}x{L2}_np{npart}_k00"
     G = L.build_translation_group(spec.lattice)
     t0 = time.perf_counter()
     cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G, particle_statistics=A.Fermionic())
     t_cat = time.perf_counter() - t0
-    irr = L.build_translation_irrep_list(G, spec.lattice)[0]
+    irr = L.build_translation_irrep_list(G, spec.lattice)[sector]
     t0 = time.perf_counter()
     basis = A.build_symmetry_sector_basis(cat, irr)
     t_sec = time.perf_counter() - t0
@@ -407,9 +419,62 @@ def run_large(args):
     if "evals" in res.get("fp64", {}) and "evals" in res.get("mixed", {}):
         e64, em = np.array(res["fp64"]["evals"]), np.array(res["mixed"]["evals"])
         res["max_rel_dE_mixed_vs_fp64"] = float(np.max(np.abs(em - e64) / np.abs(e64)))
-    line = {"workload": f"checkerboard{L1}x{L2}_np{npart}_k00", "n_states": cat.n_states, "n_orbits": cat.n_orbits,
+    line = {"workload": name, "n_states": cat.n_states, "n_orbits": cat.n_orbits,
             "dim": basis.dim, "catalog_build_s": t_cat, "sector_build_s": t_sec, "peak_gbs": peak,
             "peak_kind": peak_kind, **res}
+    print(json.dumps(line), flush=True)
+
+
+def run_served(args):
+    """Config 5: a seeded Poisson stream of ground-state requests drawn
+    uniformly from rings N in {20, 24, 28}, checkerboard 3x4 / 4x4 and Hubbard
+    3x4 / 4x4 with N_up = N_down in {5, 6}, random momentum and twist; served
+    with continuous batching under a 160 GB device budget, against the plain
+    FP64 drop-in answering the same requests one at a time."""
+    import torch
+
+    import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300 import lattice as L
+    from realspace_exactdiagonalization_gb300.serving import (SectorServer, config5_families, latency_stats,
+                                                              random_requests)
+
+    torch.cuda.set_device(0)
+    fams = config5_families()
+    t0 = time.perf_counter()
+    srv = SectorServer(fams, budget_bytes=160e9, batch_lanes=2, large_workers=args.large_workers)
+    t_setup = time.perf_counter() - t0
+    reqs = random_requests(fams, args.served_n, rate=args.served_rate, seed=20261203)
+    done = sorted(srv.serve(reqs), key=lambda r: r.rid)
+    st = latency_stats(done)
+    bad = [r.rid for r in done if r.status != 0]
+    # the plain FP64 drop-in, one request at a time, on a per-family sample
+    per_fam = {}
+    plain_ev = {}
+    for name in sorted(fams):
+        sample = [r for r in done if r.family == name][: args.plain_per_family]
+        times = []
+        fam = srv.families[name]
+        for r in sample:
+            G = L.build_translation_group(fam.spec.lattice, r.twist)
+            irr = L.build_translation_irrep_list(G, fam.spec.lattice)[r.k_index]
+            t1 = time.perf_counter()
+            basis = A.build_symmetry_sector_basis(fam.catalog, irr, group=G)
+            if basis.dim:
+                H = A.MatrixFreeHamiltonian(basis, fam.spec.bilinear_terms(r.twist), fam.spec.density_terms)
+                vals, _, _ = H.solve(1, tol=1e-10, seed=r.seed, want_vectors=False)
+                plain_ev[r.rid] = vals[0]
+                del H
+            times.append(time.perf_counter() - t1)
+        per_fam[name] = {"plain_fp64_s": float(np.mean(times)) if times else None, "route": fam.route,
+                         "n_orbits": fam.n_orbits, "served": sum(1 for r in done if r.family == name)}
+    mix_s = np.mean([per_fam[r.family]["plain_fp64_s"] for r in done])
+    rel = [abs(done[i].evals[0] - e) / abs(e) for i, e in plain_ev.items()]
+    line = {"workload": "served_config5", "requests": len(done), "rate_per_s": args.served_rate,
+            "served": st, "unconverged": bad, "setup_s": t_setup, "peak_reserved_gb": srv.peak_reserved / 1e9,
+            "resident_gb": srv.resident / 1e9,
+            "plain_fp64_one_at_a_time_solves_per_s": 1.0 / mix_s,
+            "speedup_vs_plain_fp64": st["solves_per_s"] * mix_s,
+            "max_rel_dE_vs_plain_fp64": float(max(rel)) if rel else None, "families": per_fam}
     print(json.dumps(line), flush=True)
 
 
@@ -423,12 +488,20 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=6)
     ap.add_argument("--ref-sample", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="flux_scan", choices=["flux_scan", "large"])
+    ap.add_argument("--workload", default="flux_scan", choices=["flux_scan", "large", "served"])
+    ap.add_argument("--served-n", type=int, default=300)
+    ap.add_argument("--served-rate", type=float, default=50.0)
+    ap.add_argument("--large-workers", type=int, default=3)
+    ap.add_argument("--plain-per-family", type=int, default=2)
     ap.add_argument("--large-shape", type=int, nargs=3, default=[4, 6, 8], metavar=("L1", "L2", "NP"))
     ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--large-model", default="checkerboard", choices=["checkerboard", "hubbard"])
     args = ap.parse_args()
     if args.workload == "large":
         run_large(args)
+        return
+    if args.workload == "served":
+        run_served(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

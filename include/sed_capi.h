@@ -105,6 +105,14 @@ void sed_catalog_destroy(sed_catalog* c);
 /* build_symmetry_sector_basis (SRE:534-556): orbits whose stabilizer phases
  * match chi (|chi(h) - alpha_h(rep)| <= atol), in catalog order. */
 int sed_sector_build(const sed_catalog* c, const double* chi_reim, double atol, sed_sector** out, int64_t* dim);
+/* The same with an explicit group g (same permutations and statistics as the
+ * catalog's, e.g. the flux-twisted group of build_translation_group): the
+ * sector and every operator built on it use g's phases, and the catalog is
+ * left unchanged.  Equivalent to update_orbit_stabilizer_phases! (SRE:338-369)
+ * followed by build_symmetry_sector_basis, without mutating the catalog, so
+ * sectors of different twists can be built and solved concurrently. */
+int sed_sector_build_group(const sed_catalog* c, const sed_group* g, const double* chi_reim, double atol,
+                           sed_sector** out, int64_t* dim);
 /* representative_mask_list, stabilizer_order_list and the catalog orbit index
  * of every sector row (any pointer may be NULL). */
 int sed_sector_get(const sed_sector* s, uint64_t* reps, int32_t* stab_order, int32_t* orbit_index);
@@ -161,8 +169,11 @@ void sed_op_destroy(sed_op* op);
  * restart budget (300), krylovdim the basis size (0 = 30).  seed selects the
  * complex Gaussian start vector.  evecs_reim (nullable) receives nev
  * sector-ordered complex128 vectors, vector-major.  Mixed-precision operators
- * converge with the complex64 matvec, then run one FP64 Rayleigh-Ritz polish
- * over span{x, Hx}. */
+ * converge with the complex64 matvec (with two spare Ritz pairs), then run an
+ * FP64 block-Davidson polish (Rayleigh-Ritz over the Ritz vectors and their
+ * diagonally preconditioned FP64 residuals, at most 16 expansions); if that
+ * misses max(tol, 1e-7 |E|) the sector is solved again entirely in FP64, so
+ * the returned pairs always meet the FP64 residual bound. */
 int sed_solve(sed_op* op, int nev, double tol, int maxiter, int krylovdim, uint64_t seed, double* evals,
               double* evecs_reim, sed_solve_info* info);
 
@@ -177,8 +188,9 @@ int sed_solve(sed_op* op, int nev, double tol, int maxiter, int krylovdim, uint6
  * build_translation_group, SRE:1374-1405), its bilinear amplitudes (n_bil
  * complex, same (i, j) list for every request) and its start-vector seed, so
  * its result does not depend on which other requests share the launch.
- * precision: SED_PREC_MIXED (complex64 matvec + FP64 Rayleigh-Ritz polish) or
- * SED_PREC_FP64.  Outputs per request: nev eigenvalues (ascending), status
+ * precision: SED_PREC_MIXED (complex64 matvec + FP64 block-Davidson polish;
+ * a request whose polish misses its target is re-solved by the FP64 kernel in
+ * a second launch) or SED_PREC_FP64.  Outputs per request: nev eigenvalues (ascending), status
  * (0 ok, SED_ERR_NOT_CONVERGED), sector dimension, |E_polished - E_c64| and
  * the matvec count. */
 typedef struct sed_batch sed_batch;
@@ -192,9 +204,26 @@ int sed_batch_run(sed_batch* b, int n_req, const double* chi_reim, const double*
  * may be NULL): hops evaluated by one matvec of the request's sector, and the
  * device clock (ns) when its block picked it up and when it finished. */
 int sed_batch_last_stats(const sed_batch* b, int64_t* hops, int64_t* t_start_ns, int64_t* t_end_ns);
-/* Same solve with every buffer in device memory (inputs resident in HBM);
- * asynchronous on the batch stream.  Device arrays have the layouts of
- * sed_batch_run; outputs may not be NULL. */
+/* About the last run (any pointer may be NULL): how many requests the FP64
+ * kernel re-solved because the complex64 run could not meet the mixed
+ * precision target (0 for SED_PREC_FP64), whether the matvecs streamed the hop
+ * table, and its size in 8-byte records. */
+int sed_batch_last_info(const sed_batch* b, int32_t* n_fallback, int32_t* hop_table, int64_t* hop_records);
+/* The hop table (on by default): the requests of a batch share the catalog and
+ * the (i, j) term list, hence every sector matrix's sparsity pattern, which is
+ * enumerated once into 8-byte records (column orbit, term x group element,
+ * phase id) and streamed by every matvec of every request, in place of
+ * re-deriving each hop from the representative (rank lookups, state words,
+ * popcounts).  Costs 8 bytes per hop of device memory; rebuilt when a run's
+ * twist-phase classes differ from the last run's.  Runs whose group phases take
+ * more than four distinct values per group element, or whose sectors leave no
+ * shared memory for its coefficient tables, use the on-the-fly matvec. */
+int sed_batch_set_hop_table(sed_batch* b, int enable);
+/* Same solve with every buffer in device memory (inputs resident in HBM),
+ * queued on the batch stream.  Device arrays have the layouts of
+ * sed_batch_run; outputs may not be NULL.  SED_PREC_FP64 returns without
+ * waiting; SED_PREC_MIXED waits once for the statuses of the first launch to
+ * queue the FP64 re-solves. */
 int sed_batch_run_device(sed_batch* b, int n_req, const double* d_chi, const double* d_group_phase,
                          const double* d_bil_t, const uint64_t* d_seeds, double tol, int maxiter, double* d_evals,
                          int32_t* d_status, int64_t* d_dims, double* d_delta, int32_t* d_n_matvec);

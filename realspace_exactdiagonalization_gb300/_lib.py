@@ -57,6 +57,7 @@ SIGNATURES = [
     ("sed_catalog_set_stream", _i32, [_p, _p]),
     ("sed_catalog_destroy", None, [_p]),
     ("sed_sector_build", _i32, [_p, _p, _dbl, _p, _p]),
+    ("sed_sector_build_group", _i32, [_p, _p, _p, _dbl, _p, _p]),
     ("sed_sector_get", _i32, [_p, _p, _p, _p]),
     ("sed_sector_project", _i32, [_p, _i64, _p, _p, _p]),
     ("sed_sector_destroy", None, [_p]),
@@ -72,6 +73,8 @@ SIGNATURES = [
     ("sed_batch_create", _i32, [_p, _i32, _p, _i32, _p, _p, _i32, _i32, _i32, _i32, _p]),
     ("sed_batch_run", _i32, [_p, _i32, _p, _p, _p, _p, _dbl, _i32, _p, _p, _p, _p, _p]),
     ("sed_batch_last_stats", _i32, [_p, _p, _p, _p]),
+    ("sed_batch_last_info", _i32, [_p, _p, _p, _p]),
+    ("sed_batch_set_hop_table", _i32, [_p, _i32]),
     ("sed_batch_run_device", _i32, [_p, _i32, _p, _p, _p, _p, _dbl, _i32, _p, _p, _p, _p, _p]),
     ("sed_batch_set_stream", _i32, [_p, _p]),
     ("sed_batch_info", _i32, [_p, _p, _p, _p]),

@@ -239,14 +239,26 @@ class Symmetry_Sector_Basis(_Handle):
 
 
 def build_symmetry_sector_basis(catalog: Symmetry_Orbit_Catalog, irrep: OneDim_Irrep,
-                                atol: float = 1e-12) -> Symmetry_Sector_Basis:
-    """SRE:544-556."""
+                                atol: float = 1e-12, group: Optional[Finite_Symmetry_Group] = None
+                                ) -> Symmetry_Sector_Basis:
+    """SRE:544-556.  With ``group`` (a twisted copy of the catalog's group,
+    same permutations) the sector uses that group's phases without changing
+    the catalog: update_orbit_stabilizer_phases! + build_symmetry_sector_basis
+    in one step, safe to run for several twists at once."""
     chi = np.ascontiguousarray(irrep.array(), dtype=np.complex128)
     if len(chi) != group_order(catalog.symmetry_group):
         raise ValueError("the irrep needs one value per group element")
     h, dim = C.c_void_p(), C.c_int64()
-    check(_lib.load().sed_sector_build(catalog.handle, ptr(chi), float(atol), C.byref(h), C.byref(dim)))
-    return Symmetry_Sector_Basis(h, catalog, irrep, dim.value)
+    if group is None:
+        check(_lib.load().sed_sector_build(catalog.handle, ptr(chi), float(atol), C.byref(h), C.byref(dim)))
+    else:
+        dg = DeviceGroup(group, catalog.particle_statistics)
+        check(_lib.load().sed_sector_build_group(catalog.handle, dg.handle, ptr(chi), float(atol), C.byref(h),
+                                                 C.byref(dim)))
+    basis = Symmetry_Sector_Basis(h, catalog, irrep, dim.value)
+    if group is not None:
+        basis.symmetry_group = group
+    return basis
 
 
 @dataclass

@@ -113,7 +113,14 @@ class BatchedSectorSolver:
         t0 = np.zeros(n, dtype=np.int64)
         t1 = np.zeros(n, dtype=np.int64)
         check(_lib.load().sed_batch_last_stats(self._h, ptr(hops), ptr(t0), ptr(t1)))
-        return {"hops": hops, "t_start_ns": t0, "t_end_ns": t1}
+        nf, tab, nrec = C.c_int32(0), C.c_int32(0), C.c_int64(0)
+        check(_lib.load().sed_batch_last_info(self._h, C.byref(nf), C.byref(tab), C.byref(nrec)))
+        return {"hops": hops, "t_start_ns": t0, "t_end_ns": t1, "fp64_fallbacks": int(nf.value),
+                "hop_table": bool(tab.value), "hop_records": int(nrec.value)}
+
+    def set_hop_table(self, enable: bool) -> None:
+        """Stream the shared hop table (default) or derive every hop on the fly."""
+        check(_lib.load().sed_batch_set_hop_table(self._h, int(bool(enable))))
 
     def run_device(self, n: int, d_chi: int, d_phase: int, d_amp: int, d_seeds: int, d_evals: int, d_status: int,
                    d_dims: int, d_delta: int, d_nmv: int, tol: float = 1e-10, maxiter: int = 300) -> None:

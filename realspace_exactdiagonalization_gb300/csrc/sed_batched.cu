@@ -21,9 +21,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <unordered_map>
 
 #include "../../include/sed_capi.h"
 #include "sed_internal.cuh"
+
 #include "sed_rowgather.cuh"
 
 namespace sed {
@@ -32,11 +34,13 @@ static constexpr int kBT = 512;      // threads per block
 static constexpr int kMaxM = 32;     // Krylov dimension cap
 static constexpr int kMaxNev = 8;
 static constexpr int kNW = kBT / 32;
+static constexpr int kPolCap = 22;         // polish basis capacity (complex Rayleigh-Ritz matrix <= 22 x 22)
+static constexpr int kPolishFailed = 100;  // internal status: the FP64 polish missed its target
 
 struct BatchArgs {
   int64_t n_orb, ld;
   int N, G, n_bil, n_terms, n_den;
-  int nev, m, maxiter, n_req;
+  int nev, m, maxiter, n_req, kp1;
   double tol, atol;
   const uint64_t* reps;
   const uint8_t* stab;
@@ -52,6 +56,16 @@ struct BatchArgs {
   const double2* phase;  // [n_req][G][N]
   const double2* amp;    // [n_req][n_bil]
   const uint64_t* seeds;
+  const int32_t* req_list;  // requests to solve (NULL: 0..n_req-1)
+  // hop table (use_tab != 0): SELL-32 records, per-slice offsets / widths,
+  // phase-id descriptors and each group element's class representative sites
+  int use_tab, n_phi, phi_cap;
+  const uint64_t* hop;
+  const uint32_t* sl_off;
+  const int32_t* sl_w;
+  const uint32_t* phi_desc;
+  const int8_t* rep_site;  // [G][4]
+  double2* pwc64;          // per-block phase-id coefficients (FP64)
   double2 *V, *R, *W, *X64, *tchi64;
   uint8_t* rowflag;
   double* evals;
@@ -65,7 +79,8 @@ struct BatchArgs {
 };
 
 struct BatchSmem {
-  size_t x, tchi, eta, chi64, T, Z, theta, coef, red, isr, rank, rec, off, inv, perm, misc, total;
+  size_t x, tchi, eta, chi64, T, Z, theta, coef, red, isr, rank, rec, off, inv, perm, misc, pw32, pw64, mask, basek,
+      pwc, total;
 };
 
 template <class VT>
@@ -86,13 +101,13 @@ static BatchSmem batch_layout(const BatchArgs& a, bool x_in_smem) {
   L.Z = o;
   o = al(o + kMaxM * kMaxM * 8);
   L.theta = o;
-  o = al(o + kMaxM * 8);
+  o = al(o + 3 * kMaxM * 8);
   L.coef = o;
   o = al(o + 2 * (kMaxM + 8) * 16);
   L.red = o;
   o = al(o + kNW * 16 * 8);
   L.isr = o;
-  o = al(o + 65 * 8);
+  o = al(o + 130 * 8);
   L.misc = o;
   o = al(o + 64 * 8);
   L.rank = o;
@@ -105,6 +120,16 @@ static BatchSmem batch_layout(const BatchArgs& a, bool x_in_smem) {
   o = al(o + 64);
   L.perm = o;
   o = al(o + (size_t)a.G * 64);
+  L.pw64 = o;
+  o = al(o + (size_t)a.G * kMaxCls * a.kp1 * 16);
+  L.pw32 = o;
+  o = al(o + (size_t)a.G * kMaxCls * a.kp1 * 8);
+  L.mask = o;
+  o = al(o + (size_t)a.G * kMaxCls * 8);
+  L.basek = o;
+  o = al(o + (size_t)a.G * 16);
+  L.pwc = o;
+  o = al(o + (size_t)a.phi_cap * sizeof(VT));
   L.total = o;
   return L;
 }
@@ -140,6 +165,37 @@ __device__ __forceinline__ double block_sum1(double v, double* red, double* out)
   return out[0];
 }
 
+// Jacobi rotation (c, s) for the 2x2 block [[app, apq], [apq, aqq]].  The
+// angle only has to shrink apq, not zero it exactly, so it is computed in
+// FP32 (GB300's FP64 divide and square root are slow); c and s are then
+// normalised to FP64 precision by two Newton steps on 1/sqrt(c^2 + s^2), so
+// the rotation is orthogonal to FP64 rounding and the decomposition keeps
+// FP64 accuracy (unzeroed remainders are removed by the next sweep).
+__device__ __forceinline__ void jacobi_cs(double app, double aqq, double apq, double* c, double* s) {
+  const float th = (float)(aqq - app) / (2.0f * (float)apq);
+  const float t = (th >= 0.f ? 1.f : -1.f) / (fabsf(th) + sqrtf(fmaf(th, th, 1.f)));
+  const float cf = rsqrtf(fmaf(t, t, 1.f));
+  double cc = (double)cf, ss = (double)(t * cf);
+  for (int it = 0; it < 2; ++it) {
+    const double n2 = cc * cc + ss * ss;
+    const double f = 1.5 - 0.5 * n2;  // 1/sqrt(n2) to first order around 1
+    cc *= f;
+    ss *= f;
+  }
+  *c = cc;
+  *s = ss;
+}
+
+// unit phase e = a / |a| of a complex number, normalised the same way
+__device__ __forceinline__ void unit_phase(double2 a, double* er, double* ei, double* r) {
+  const double n2 = a.x * a.x + a.y * a.y;
+  double inv = (double)rsqrtf((float)n2);
+  for (int it = 0; it < 3; ++it) inv = inv * (1.5 - 0.5 * n2 * inv * inv);
+  *er = a.x * inv;
+  *ei = a.y * inv;
+  *r = n2 * inv;
+}
+
 // Warp-parallel cyclic Jacobi for a real symmetric n x n matrix (row stride
 // ld) in shared memory; eigenvalues ascending in w, eigenvectors in Z columns.
 __device__ void warp_jacobi(int n, double* A, double* Z, double* w) {
@@ -158,15 +214,14 @@ __device__ void warp_jacobi(int n, double* A, double* Z, double* w) {
     }
     off = warp_allsum(off);
     tot = warp_allsum(tot);
-    if (off <= 1e-32 * fmax(tot, 1e-300)) break;
+    if (off <= 1e-29 * fmax(tot, 1e-300)) break;  // rounding level of the off-diagonal part
     for (int p = 0; p < n - 1; ++p)
       for (int q = p + 1; q < n; ++q) {
         const double apq = A[p * kMaxM + q];
-        if (apq == 0.0) continue;
         const double app = A[p * kMaxM + p], aqq = A[q * kMaxM + q];
-        const double th = (aqq - app) / (2.0 * apq);
-        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        if (fabs(apq) <= 1e-18 * (fabs(app) + fabs(aqq)) + 1e-300) continue;
+        double c, s;
+        jacobi_cs(app, aqq, apq, &c, &s);
         __syncwarp();
         if (lane < n) {
           const double akp = A[lane * kMaxM + p], akq = A[lane * kMaxM + q];
@@ -207,51 +262,6 @@ __device__ void warp_jacobi(int n, double* A, double* Z, double* w) {
   __syncwarp();
 }
 
-// Complex Hermitian Jacobi (single thread; n <= 2 * kMaxNev).
-__device__ void thread_jacobi_herm(int n, double2* A, double* w) {
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    double off = 0.0, tot = 0.0;
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j) {
-        const double v = A[i * 16 + j].x * A[i * 16 + j].x + A[i * 16 + j].y * A[i * 16 + j].y;
-        tot += v;
-        if (i != j) off += v;
-      }
-    if (off <= 1e-32 * fmax(tot, 1e-300)) break;
-    for (int p = 0; p < n - 1; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double ar = A[p * 16 + q].x, ai = A[p * 16 + q].y;
-        const double r = hypot(ar, ai);
-        if (r == 0.0) continue;
-        const double er = ar / r, ei = ai / r;
-        const double app = A[p * 16 + p].x, aqq = A[q * 16 + q].x;
-        const double th = (aqq - app) / (2.0 * r);
-        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < n; ++k) {
-          const double2 xp = A[k * 16 + p], xq0 = A[k * 16 + q];
-          const double2 xq = make_double2(xq0.x * er + xq0.y * ei, xq0.y * er - xq0.x * ei);
-          A[k * 16 + p] = make_double2(c * xp.x - s * xq.x, c * xp.y - s * xq.y);
-          A[k * 16 + q] = make_double2(s * xp.x + c * xq.x, s * xp.y + c * xq.y);
-        }
-        for (int k = 0; k < n; ++k) {
-          const double2 xp = A[p * 16 + k], xq0 = A[q * 16 + k];
-          const double2 xq = make_double2(xq0.x * er - xq0.y * ei, xq0.y * er + xq0.x * ei);
-          A[p * 16 + k] = make_double2(c * xp.x - s * xq.x, c * xp.y - s * xq.y);
-          A[q * 16 + k] = make_double2(s * xp.x + c * xq.x, s * xp.y + c * xq.y);
-        }
-      }
-  }
-  for (int i = 0; i < n; ++i) w[i] = A[i * 16 + i].x;
-  for (int i = 0; i < n; ++i)
-    for (int j = i + 1; j < n; ++j)
-      if (w[j] < w[i]) {
-        const double t = w[i];
-        w[i] = w[j];
-        w[j] = t;
-      }
-}
-
 __device__ __forceinline__ int64_t global_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -263,6 +273,78 @@ __device__ __forceinline__ uint64_t bsplitmix(uint64_t x) {
   x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
   x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
   return x ^ (x >> 31);
+}
+
+// Warp-parallel complex Hermitian Jacobi with eigenvectors (row stride
+// kPolCap): each rotation makes A_pq real with a phase on column q, then
+// zeroes it with a real 2x2 rotation.  Eigenvalues ascending in w.
+__device__ void warp_jacobi_herm(int n, double2* A, double2* Z, double* w) {
+  const int lane = threadIdx.x & 31;
+  const int S = kPolCap;
+  for (int i = lane; i < n * S; i += 32) Z[i] = make_double2(0.0, 0.0);
+  __syncwarp();
+  for (int i = lane; i < n; i += 32) Z[i * S + i] = make_double2(1.0, 0.0);
+  __syncwarp();
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int e = lane; e < n * n; e += 32) {
+      const int i = e / n, j = e % n;
+      const double v = A[i * S + j].x * A[i * S + j].x + A[i * S + j].y * A[i * S + j].y;
+      tot += v;
+      if (i != j) off += v;
+    }
+    off = warp_allsum(off);
+    tot = warp_allsum(tot);
+    if (off <= 1e-29 * fmax(tot, 1e-300)) break;  // rounding level of the off-diagonal part
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double2 apq = A[p * S + q];
+        if (fabs(apq.x) + fabs(apq.y) <= 1e-18 * (fabs(A[p * S + p].x) + fabs(A[q * S + q].x)) + 1e-300) continue;
+        double er, ei, r;
+        unit_phase(apq, &er, &ei, &r);
+        double c, sn;
+        jacobi_cs(A[p * S + p].x, A[q * S + q].x, r, &c, &sn);
+        __syncwarp();
+        if (lane < n) {
+          const double2 xp = A[lane * S + p], q0 = A[lane * S + q];
+          const double2 xq = make_double2(q0.x * er + q0.y * ei, q0.y * er - q0.x * ei);
+          A[lane * S + p] = make_double2(c * xp.x - sn * xq.x, c * xp.y - sn * xq.y);
+          A[lane * S + q] = make_double2(sn * xp.x + c * xq.x, sn * xp.y + c * xq.y);
+          const double2 zp = Z[lane * S + p], z0 = Z[lane * S + q];
+          const double2 zq = make_double2(z0.x * er + z0.y * ei, z0.y * er - z0.x * ei);
+          Z[lane * S + p] = make_double2(c * zp.x - sn * zq.x, c * zp.y - sn * zq.y);
+          Z[lane * S + q] = make_double2(sn * zp.x + c * zq.x, sn * zp.y + c * zq.y);
+        }
+        __syncwarp();
+        if (lane < n) {
+          const double2 xp = A[p * S + lane], q0 = A[q * S + lane];
+          const double2 xq = make_double2(q0.x * er - q0.y * ei, q0.y * er + q0.x * ei);
+          A[p * S + lane] = make_double2(c * xp.x - sn * xq.x, c * xp.y - sn * xq.y);
+          A[q * S + lane] = make_double2(sn * xp.x + c * xq.x, sn * xp.y + c * xq.y);
+        }
+        __syncwarp();
+      }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    for (int i = 0; i < n; ++i) w[i] = A[i * S + i].x;
+    for (int i = 0; i < n; ++i) {
+      int b = i;
+      for (int j = i + 1; j < n; ++j)
+        if (w[j] < w[b]) b = j;
+      if (b != i) {
+        const double t = w[i];
+        w[i] = w[b];
+        w[b] = t;
+        for (int r = 0; r < n; ++r) {
+          const double2 z = Z[r * S + i];
+          Z[r * S + i] = Z[r * S + b];
+          Z[r * S + b] = z;
+        }
+      }
+    }
+  }
+  __syncwarp();
 }
 
 // ----------------------------------------------------------- block matvec
@@ -283,7 +365,8 @@ __device__ __forceinline__ double block_matvec(const BatchArgs& a, const typenam
                                                const typename P::V* tchi, const typename P::V* eta,
                                                const double* s_isr, const uint32_t* s_rank, const uint32_t* s_rec,
                                                const uint16_t* s_off, const uint8_t* s_inv,
-                                               const uint8_t* __restrict__ rowflag, double2* __restrict__ w) {
+                                               const uint8_t* __restrict__ rowflag, double2* __restrict__ w,
+                                               const PhaseClasses<typename P::V>& pcl) {
   using V = typename P::V;
   using S = typename P::S;
   double nrm = 0.0;
@@ -297,13 +380,53 @@ __device__ __forceinline__ double block_matvec(const BatchArgs& a, const typenam
     S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
     S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
     row_gather<P, FERMI, PHASES, true>(a.reps[o], x, tchi, nullptr, a.G, eta, a.N, s_rank, a.rp, s_rec, s_off, s_inv,
-                                       a.state, ar, ai);
+                                       a.state, ar, ai, pcl);
     const double is = s_isr[a.stab[o]];
     const double2 y = make_double2((double)ar * is, (double)ai * is);
     w[o] = y;
     nrm += y.x * y.x + y.y * y.y;
   }
   return nrm;
+}
+
+// The same matvec through the hop table: one coalesced 8-byte record per hop
+// (thread l of a warp owns row 32s + l of slice s), then the column value,
+// the term-group coefficient and the phase-id coefficient from shared memory
+// or L1; the records carry the signs and phase-class counts, so a hop costs
+// no rank lookup, state word or popcount.
+template <class P>
+__device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typename P::V* x,
+                                                 const typename P::V* tchi, const typename P::V* pwc,
+                                                 const double* s_isr, const uint8_t* __restrict__ rowflag,
+                                                 double2* __restrict__ w) {
+  using V = typename P::V;
+  using S = typename P::S;
+  const int lane = threadIdx.x & 31;
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    const int64_t sl = o >> 5;
+    const uint64_t* rp = a.hop + a.sl_off[sl] + lane;
+    const int wdt = a.sl_w[sl];
+    const double2 dg = a.diag[o];
+    const V xo = x[o];
+    S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
+    S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
+#pragma unroll 4
+    for (int k = 0; k < wdt; ++k) {
+      const uint64_t r = __ldg(rp + 32 * k);
+      const V t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
+      const V ph = pwc[(uint32_t)(r >> 42)];
+      const V xc = x[(uint32_t)r & 0xFFFFFFu];
+      const S cr = t.x * ph.x - t.y * ph.y, ci = t.x * ph.y + t.y * ph.x;
+      ar += cr * xc.x - ci * xc.y;
+      ai += cr * xc.y + ci * xc.x;
+    }
+    if (!rowflag[o]) {
+      w[o] = make_double2(0.0, 0.0);
+      continue;
+    }
+    const double is = s_isr[a.stab[o]];
+    w[o] = make_double2((double)ar * is, (double)ai * is);
+  }
 }
 
 // coef[l0..l0+nv) = V[0..nv)^H w, in chunks of 8 vectors
@@ -371,14 +494,40 @@ __device__ void block_rotate(const BatchArgs& a, const double2* V, int msz, cons
   }
 }
 
+// out_c = sum_l V[l] S[l][c], complex coefficients (row stride kPolCap)
+__device__ void block_rotate_c(const BatchArgs& a, const double2* V, int nb, const double2* S, int nw, double2* out) {
+  for (int c0 = 0; c0 < nw; c0 += 8) {
+    const int cn = min(8, nw - c0);
+    for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+      double ar[8], ai[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) ar[c] = ai[c] = 0.0;
+      for (int l = 0; l < nb; ++l) {
+        const double2 v = V[(size_t)l * a.ld + o];
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          if (c < cn) {
+            const double2 sc = S[l * kPolCap + c0 + c];
+            ar[c] += v.x * sc.x - v.y * sc.y;
+            ai[c] += v.x * sc.y + v.y * sc.x;
+          }
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn) out[(size_t)(c0 + c) * a.ld + o] = make_double2(ar[c], ai[c]);
+    }
+  }
+}
+
 // v = w * inv and the scaled matvec input x = sqrt(stab) v
 template <class VT>
-__device__ __forceinline__ void block_normalize(const BatchArgs& a, const double2* w, double inv, double2* v, VT* x) {
+__device__ __forceinline__ void block_normalize(const BatchArgs& a, const double2* w, double inv, double2* v, VT* x,
+                                                const double* s_sqrt) {
   for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
     const double2 y = make_double2(w[o].x * inv, w[o].y * inv);
-    v[o] = y;
+    if (v) v[o] = y;
     if (x) {
-      const double sq = sqrt((double)a.stab[o]);
+      const double sq = s_sqrt[a.stab[o]];
       x[o].x = y.x * sq;
       x[o].y = y.y * sq;
     }
@@ -396,16 +545,24 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
   double2* s_chi = reinterpret_cast<double2*>(smem + L.chi64);
   double* s_T = reinterpret_cast<double*>(smem + L.T);
   double* s_Z = reinterpret_cast<double*>(smem + L.Z);
-  double* s_theta = reinterpret_cast<double*>(smem + L.theta);
+  double* s_theta = reinterpret_cast<double*>(smem + L.theta);  // Lanczos Ritz values
+  double* s_lam = s_theta + kMaxM;                                // FP64 Rayleigh-Ritz values
+  double* s_arrow = s_theta + 2 * kMaxM;                          // restart arrow column
   double2* s_coef = reinterpret_cast<double2*>(smem + L.coef);
   double* s_red = reinterpret_cast<double*>(smem + L.red);
   double* s_isr = reinterpret_cast<double*>(smem + L.isr);
+  double* s_sqrt = s_isr + 65;
   double* s_misc = reinterpret_cast<double*>(smem + L.misc);
   uint32_t* s_rank = reinterpret_cast<uint32_t*>(smem + L.rank);
   uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem + L.rec);
   uint16_t* s_off = reinterpret_cast<uint16_t*>(smem + L.off);
   uint8_t* s_inv = reinterpret_cast<uint8_t*>(smem + L.inv);
   uint8_t* s_perm = reinterpret_cast<uint8_t*>(smem + L.perm);
+  double2* s_pw64 = reinterpret_cast<double2*>(smem + L.pw64);
+  float2* s_pw32 = reinterpret_cast<float2*>(smem + L.pw32);
+  uint64_t* s_mask = reinterpret_cast<uint64_t*>(smem + L.mask);
+  double2* s_basek = reinterpret_cast<double2*>(smem + L.basek);
+  V* s_pwc = reinterpret_cast<V*>(smem + L.pwc);
   int* s_int = reinterpret_cast<int*>(s_misc + 48);
 
   for (int i = threadIdx.x; i < a.rp.total; i += blockDim.x) s_rank[i] = a.rank_tab[i];
@@ -413,38 +570,155 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
   for (int i = threadIdx.x; i <= a.N; i += blockDim.x) s_off[i] = a.site_off[i];
   for (int i = threadIdx.x; i < a.G; i += blockDim.x) s_inv[i] = a.inv[i];
   for (int i = threadIdx.x; i < a.G * 64; i += blockDim.x) s_perm[i] = a.perm_g[i];
-  for (int i = threadIdx.x; i < 65; i += blockDim.x) s_isr[i] = i ? 1.0 / sqrt((double)i) : 0.0;
+  for (int i = threadIdx.x; i < 65; i += blockDim.x) {
+    s_isr[i] = i ? 1.0 / sqrt((double)i) : 0.0;
+    s_sqrt[i] = sqrt((double)i);
+  }
 
   const size_t slots = (size_t)a.m + 1;
-  const size_t rslots = (size_t)max(a.m, 3 * a.nev);
+  const size_t rslots = (size_t)max(a.m, 5 * (a.nev + 2));
   double2* Vb = a.V + (size_t)blockIdx.x * slots * a.ld;
   double2* Rb = a.R + (size_t)blockIdx.x * rslots * a.ld;
   double2* W = a.W + (size_t)blockIdx.x * a.ld;
   double2* X64 = a.X64 + (size_t)blockIdx.x * a.ld;
   double2* tchi64 = a.tchi64 + (size_t)blockIdx.x * a.n_bil * a.G;
   uint8_t* rowflag = a.rowflag + (size_t)blockIdx.x * a.ld;
+  double2* pwc64 = a.pwc64 ? a.pwc64 + (size_t)blockIdx.x * a.phi_cap : nullptr;
   V* x = X_SMEM ? s_x : reinterpret_cast<V*>(X64);
 
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_int[0] = (int)atomicAdd(a.queue, 1u);
     __syncthreads();
-    const int b = s_int[0];
-    if (b >= a.n_req) break;
-    if (threadIdx.x == 0) a.t_ns[2 * (size_t)b] = global_ns();
+    const int q = s_int[0];
+    if (q >= a.n_req) break;
+    const int b = a.req_list ? a.req_list[q] : q;
+    if (threadIdx.x == 0 && !a.req_list) a.t_ns[2 * (size_t)b] = global_ns();
     const double2* chi = a.chi + (size_t)b * a.G;
     const double2* phase = a.phase + (size_t)b * a.G * a.N;
     const double2* amp = a.amp + (size_t)b * a.n_bil;
     // ---- set-up: tables for this momentum / twist
     for (int i = threadIdx.x; i < a.G; i += blockDim.x) s_chi[i] = chi[i];
+    // phase classes of every twisted group element (see sed_rowgather.cuh)
+    if (threadIdx.x == 0) s_int[1] = 1;
+    __syncthreads();
+    for (int h = threadIdx.x; h < a.G; h += blockDim.x) {
+      const double2* ph = phase + (size_t)h * a.N;
+      double2 val[kMaxCls + 1];
+      uint64_t msk[kMaxCls + 1];
+      int nv = 0;
+      bool over = false;
+      for (int j = 0; j < a.N; ++j) {
+        const double2 e = ph[j];
+        int c = 0;
+        while (c < nv && !(val[c].x == e.x && val[c].y == e.y)) ++c;
+        if (c == nv) {
+          if (nv == kMaxCls + 1) {
+            over = true;
+            break;
+          }
+          val[nv] = e;
+          msk[nv] = 0;
+          ++nv;
+        }
+        msk[c] |= 1ULL << j;
+      }
+      if (over) {
+        s_int[1] = 2;  // per-site product for this request
+        continue;
+      }
+      int bc = 0;
+      for (int c = 1; c < nv; ++c)
+        if (__popcll(msk[c]) > __popcll(msk[bc])) bc = c;
+      const double2 base = val[bc];
+      double2 bk = make_double2(1.0, 0.0);
+      for (int e = 0; e + 1 < a.kp1; ++e) bk = make_double2(bk.x * base.x - bk.y * base.y, bk.x * base.y + bk.y * base.x);
+      s_basek[h] = bk;
+      const double bn = base.x * base.x + base.y * base.y;
+      int slot = 0;
+      for (int c = 0; c < nv; ++c) {
+        if (c == bc) continue;
+        // r = v / base
+        const double2 r = make_double2((val[c].x * base.x + val[c].y * base.y) / bn,
+                                       (val[c].y * base.x - val[c].x * base.y) / bn);
+        s_mask[h * kMaxCls + slot] = msk[c];
+        double2 pw = make_double2(1.0, 0.0);
+        for (int e = 0; e < a.kp1; ++e) {
+          s_pw64[(h * kMaxCls + slot) * a.kp1 + e] = pw;
+          s_pw32[(h * kMaxCls + slot) * a.kp1 + e] = make_float2((float)pw.x, (float)pw.y);
+          pw = make_double2(pw.x * r.x - pw.y * r.y, pw.x * r.y + pw.y * r.x);
+        }
+        ++slot;
+      }
+      for (; slot < kMaxCls; ++slot) {
+        s_mask[h * kMaxCls + slot] = 0;
+        for (int e = 0; e < a.kp1; ++e) {
+          s_pw64[(h * kMaxCls + slot) * a.kp1 + e] = make_double2(e == 0 ? 1.0 : 0.0, 0.0);
+          s_pw32[(h * kMaxCls + slot) * a.kp1 + e] = make_float2(e == 0 ? 1.f : 0.f, 0.f);
+        }
+      }
+    }
+    __syncthreads();
+    if (a.use_tab) {
+      // family phase classes of the hop table: this request's phase on each
+      // class (read at the class's first site; constant on the class by
+      // construction), P_h(new) = v0^k prod_c (v_c / v0)^(n_c)
+      for (int h = threadIdx.x; h < a.G; h += blockDim.x) {
+        const double2* ph = phase + (size_t)h * a.N;
+        const int8_t* rs = a.rep_site + h * 4;
+        const double2 v0 = ph[rs[0]];
+        double2 bk = make_double2(1.0, 0.0);
+        for (int e = 0; e + 1 < a.kp1; ++e) bk = make_double2(bk.x * v0.x - bk.y * v0.y, bk.x * v0.y + bk.y * v0.x);
+        s_basek[h] = bk;
+        const double bn = v0.x * v0.x + v0.y * v0.y;
+        for (int c = 0; c < kMaxCls; ++c) {
+          double2 r = make_double2(1.0, 0.0);
+          if (rs[c + 1] >= 0) {
+            const double2 v = ph[rs[c + 1]];
+            r = make_double2((v.x * v0.x + v.y * v0.y) / bn, (v.y * v0.x - v.x * v0.y) / bn);
+          }
+          double2 pw = make_double2(1.0, 0.0);
+          for (int e = 0; e < a.kp1; ++e) {
+            s_pw64[(h * kMaxCls + c) * a.kp1 + e] = pw;
+            pw = make_double2(pw.x * r.x - pw.y * r.y, pw.x * r.y + pw.y * r.x);
+          }
+        }
+      }
+      __syncthreads();
+      // phase-id coefficients: +-conj(prod_c r_c^(n_c)); entry n_phi is the
+      // zero coefficient of the padding records
+      for (int f = threadIdx.x; f <= a.n_phi; f += blockDim.x) {
+        double2 p = make_double2(0.0, 0.0);
+        if (f < a.n_phi) {
+          const uint32_t d = a.phi_desc[f];
+          const int h = d & 0x3F, n1 = (d >> 6) & 0x3F, n2 = (d >> 12) & 0x3F, n3 = (d >> 18) & 0x3F;
+          const double2* pw = s_pw64 + (size_t)h * kMaxCls * a.kp1;
+          const double2 p1 = pw[n1], p2 = pw[a.kp1 + n2], p3 = pw[2 * a.kp1 + n3];
+          const double2 q = make_double2(p1.x * p2.x - p1.y * p2.y, p1.x * p2.y + p1.y * p2.x);
+          p = make_double2(q.x * p3.x - q.y * p3.y, -(q.x * p3.y + q.y * p3.x));
+          if ((d >> 24) & 1) p = make_double2(-p.x, -p.y);
+        }
+        pwc64[f] = p;
+        s_pwc[f].x = p.x;
+        s_pwc[f].y = p.y;
+      }
+    }
+    __syncthreads();
+    const int pmode = s_int[1];
+    if (pmode == 2 && !a.use_tab)
+      for (int h = threadIdx.x; h < a.G; h += blockDim.x) s_basek[h] = make_double2(1.0, 0.0);
+    __syncthreads();
     for (int i = threadIdx.x; i < a.n_bil * a.G; i += blockDim.x) {
       const int k = i / a.G, h = i % a.G;
-      const double2 t = amp[k], c = chi[h];
-      const double2 v = make_double2(t.x * c.x + t.y * c.y, t.x * c.y - t.y * c.x);  // conj(t) chi
+      const double2 t = amp[k], c0 = chi[h], bk = s_basek[h];
+      const double2 c = make_double2(c0.x * bk.x + c0.y * bk.y, c0.y * bk.x - c0.x * bk.y);  // chi conj(base^k)
+      const double2 v = make_double2(t.x * c.x + t.y * c.y, t.x * c.y - t.y * c.x);          // conj(t) chi'
       tchi64[i] = v;
       s_tchi[i].x = v.x;
       s_tchi[i].y = v.y;
     }
+    const PhaseClasses<V> pcl{pmode, a.kp1, s_mask, reinterpret_cast<const V*>(sizeof(V) == 8 ? (void*)s_pw32 : (void*)s_pw64)};
+    const PhaseClasses<double2> pcl64{pmode, a.kp1, s_mask, s_pw64};
     for (int i = threadIdx.x; i < a.G * a.N; i += blockDim.x) {
       s_eta[i].x = phase[i].x;
       s_eta[i].y = phase[i].y;
@@ -470,7 +744,10 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
     block_sum<2>(sums, s_red, s_misc);
     const int64_t dim = (int64_t)s_misc[0];
     if (threadIdx.x == 0) a.hops[b] = (int64_t)s_misc[1];
-    const int nev = (int)min((int64_t)a.nev, dim);
+    // mixed precision carries two spare Ritz pairs into the FP64 polish;
+    // convergence is judged on the requested pairs only
+    const int nev_out = (int)min((int64_t)a.nev, dim);
+    const int nev = (int)min((int64_t)(sizeof(typename P::S) == 4 ? a.nev + 2 : a.nev), dim);
     const int m = (int)min((int64_t)a.m, dim);
     if (threadIdx.x == 0) a.dims[b] = dim;
     if (dim == 0) {
@@ -502,34 +779,46 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       nrm += v.x * v.x + v.y * v.y;
     }
     nrm = block_sum1(nrm, s_red, s_misc);
-    block_normalize<V>(a, W, 1.0 / sqrt(nrm), Vb, x);
+    block_normalize<V>(a, W, 1.0 / sqrt(nrm), Vb, x, s_sqrt);
     for (int i = threadIdx.x; i < kMaxM * kMaxM; i += blockDim.x) s_T[i] = 0.0;
     __syncthreads();
 
-    int k = 0, restarts = 0, nmv = 0, status = 0;
-    double beta = 0.0, prev_res = 1e300, best_prev = 1e300;
+    int k = 0, restarts = 0, nmv = 0, n64 = 0, status = 0;
+    double beta = 0.0, prev_res = 1e300, best_prev = 1e300, dmax = 0.0;
+    double tau = 1e-6;  // mixed: relative Ritz-estimate threshold of the complex64 run
+    const bool mixed = sizeof(typename P::S) == 4;
     for (;;) {
       int jend = m;
       for (int j = k; j < m; ++j) {
         double2* vj = Vb + (size_t)j * a.ld;
-        double n0 = block_matvec<P, FERMI, PHASES>(a, x, s_tchi, s_eta, s_isr, s_rank, s_rec, s_off, s_inv, rowflag, W);
+        if (a.use_tab)
+          block_matvec_tab<P>(a, x, s_tchi, s_pwc, s_isr, rowflag, W);
+        else
+          block_matvec<P, FERMI, PHASES>(a, x, s_tchi, s_eta, s_isr, s_rank, s_rec, s_off, s_inv, rowflag, W, pcl);
         __syncthreads();
         ++nmv;
+        // local step: CGS against the two newest basis vectors (they carry
+        // the large alpha_j, beta_{j-1} components), then one full CGS pass;
+        // a second full pass only when the first removed more than half of
+        // the norm (Daniel-Gragg-Kaufman-Stewart).
+        const int l0 = j > 0 ? j - 1 : 0;
+        block_dots(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, W, s_red, s_coef);
+        double n0 = block_axpy(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, s_coef, W);
+        double alpha = s_coef[j - l0].x;
+        __syncthreads();
         n0 = block_sum1(n0, s_red, s_misc);
-        // full reorthogonalisation: CGS, second pass only when the first
-        // removed more than half of the norm (Daniel-Gragg-Kaufman-Stewart)
-        block_dots(a, Vb, j + 1, W, s_red, s_coef);
-        double n1 = block_axpy(a, Vb, j + 1, s_coef, W);
+        block_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
+        double n1 = block_axpy(a, Vb, j + 1, s_coef + kMaxM + 8, W);
+        alpha += s_coef[kMaxM + 8 + j].x;
         __syncthreads();
         n1 = block_sum1(n1, s_red, s_misc + 1);
-        double alpha = s_coef[j].x;
         double nf = n1;
         if (n1 < 0.5 * n0) {
           block_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
           double n2 = block_axpy(a, Vb, j + 1, s_coef + kMaxM + 8, W);
+          alpha += s_coef[kMaxM + 8 + j].x;
           __syncthreads();
           nf = block_sum1(n2, s_red, s_misc + 2);
-          alpha += s_coef[kMaxM + 8 + j].x;
         }
         beta = sqrt(nf);
         if (threadIdx.x == 0) {
@@ -540,23 +829,14 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           jend = j + 1;
           break;
         }
-        block_normalize<V>(a, W, 1.0 / beta, vj + a.ld, x);
+        block_normalize<V>(a, W, 1.0 / beta, vj + a.ld, x, s_sqrt);
         __syncthreads();
         (void)vj;
       }
       __syncthreads();
       const int msz = jend;
-      // ---- Ritz values of the projected matrix (warp 0)
-      if (threadIdx.x < 32) {
-        double* A = s_Z + 0;  // scratch copy: Jacobi destroys its input
-        (void)A;
-      }
-      if (threadIdx.x < 32) {
-        // copy T into coef area as scratch? use s_T directly on a copy in s_red is too small;
-        // Jacobi works on a copy placed in the second half of s_Z's rows.
-      }
-      __syncthreads();
-      // copy T -> Zin (s_Z reused as input then overwritten), eigenvectors go to s_T
+      // ---- Ritz values of the projected matrix (warp 0): Jacobi works on a
+      // copy of T in s_Z and leaves the eigenvectors in s_T
       for (int i = threadIdx.x; i < kMaxM * kMaxM; i += blockDim.x) s_Z[i] = s_T[i];
       __syncthreads();
       if (threadIdx.x < 32) warp_jacobi(msz, s_Z, s_T, s_theta);
@@ -565,120 +845,128 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       const bool invariant = msz < m || (int64_t)msz == dim;
       double scale = 1.0;
       for (int i = 0; i < min(nev, msz); ++i) scale = fmax(scale, fabs(s_theta[i]));
-      const bool mixed = sizeof(typename P::S) == 4;
-      const double tol_w = mixed ? fmax(a.tol, 2e-6 * scale) : a.tol;
+      const double tol_w = mixed ? fmax(a.tol, tau * scale) : a.tol;
       int nconv = 0;
       double maxr = 0.0;
-      for (int i = 0; i < min(nev, msz); ++i) {
+      for (int i = 0; i < min(nev_out, msz); ++i) {
         const double r = invariant ? 0.0 : fabs(beta * s_T[(msz - 1) * kMaxM + i]);
         maxr = fmax(maxr, r);
         if (r <= tol_w) ++nconv;
       }
-      bool stagnated = mixed && restarts >= 6 && maxr < 1e-3 * scale && maxr > 0.7 * best_prev;
+      // FP32 noise floor: stop once the residual sits near it and no longer improves
+      bool stagnated = mixed && restarts >= 6 && maxr < 5e-5 * scale && maxr > 0.7 * best_prev;
       best_prev = prev_res;
       prev_res = fmin(prev_res, maxr);
-      const bool done = nconv >= nev || invariant || stagnated || restarts >= a.maxiter;
-      const int keep = done ? min(nev, msz) : min(msz - 1, max(nev + (m - nev) / 2, nev + 1));
+      const bool done = nconv >= nev_out || invariant || stagnated || restarts >= a.maxiter;
+      // a mixed-precision candidate keeps the full restart basis, so the
+      // iteration can resume if the FP64 check rejects it
+      const bool final_rot = done && (!mixed || invariant);
+      const int keep = final_rot ? min(nev, msz) : min(msz - 1, max(nev + (m - nev) / 2, nev + 1));
+      if (threadIdx.x < keep) s_arrow[threadIdx.x] = beta * s_T[(msz - 1) * kMaxM + threadIdx.x];
       block_rotate(a, Vb, msz, s_T, keep, Rb);
       __syncthreads();
       for (int c = 0; c < keep; ++c)
         for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
           Vb[(size_t)c * a.ld + o] = Rb[(size_t)c * a.ld + o];
-      if (done) {
-        status = (nconv >= nev || invariant || stagnated) ? 0 : SED_ERR_NOT_CONVERGED;
-        __syncthreads();
+      if (!final_rot)  // the last normalised residual direction continues the basis
+        for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
+          Vb[(size_t)keep * a.ld + o] = Vb[(size_t)m * a.ld + o];
+      __syncthreads();
+      if (done && !mixed) {
+        status = (nconv >= nev_out || invariant || stagnated) ? 0 : SED_ERR_NOT_CONVERGED;
         break;
       }
-      for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
-        Vb[(size_t)keep * a.ld + o] = Vb[(size_t)m * a.ld + o];
-      __syncthreads();
+      if (done) {
+        // FP64 check of the complex64 candidate: one Rayleigh-Ritz step with
+        // FP64 matvecs over its nev + 2 Ritz vectors B = Vb[0..nw); accepted
+        // when every requested pair meets the residual tolerance or the
+        // quadratic bound |dE| <= |r|^2 / gap (gap to the first Lanczos Ritz
+        // value outside the block) is below kMixedRelTarget |E|.  Otherwise
+        // the Lanczos resumes with a tighter threshold; a stagnated run is
+        // re-solved by the FP64 kernel (status kPolishFailed).
+        const int nw = min(nev, msz);
+        double2* HB = Rb;
+        double2* Yr = Rb + (size_t)nw * a.ld;
+        double2* HYr = Rb + (size_t)(2 * nw) * a.ld;
+        double2* M = reinterpret_cast<double2*>(s_Z);  // kPolCap^2 complex fit in kMaxM^2 doubles
+        double2* Zc = reinterpret_cast<double2*>(s_T);
+        for (int i = 0; i < nw; ++i) {
+          block_normalize<double2>(a, Vb + (size_t)i * a.ld, 1.0, nullptr, X64, s_sqrt);
+          __syncthreads();
+          if (a.use_tab)
+            block_matvec_tab<P64>(a, X64, tchi64, pwc64, s_isr, rowflag, HB + (size_t)i * a.ld);
+          else
+            block_matvec<P64, FERMI, PHASES>(a, X64, tchi64, phase, s_isr, s_rank, s_rec, s_off, s_inv, rowflag,
+                                             HB + (size_t)i * a.ld, pcl64);
+          __syncthreads();
+        }
+        n64 += nw;
+        for (int bcol = 0; bcol < nw; ++bcol) {
+          block_dots(a, Vb, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
+          if (threadIdx.x < nw) M[threadIdx.x * kPolCap + bcol] = s_coef[threadIdx.x];
+          __syncthreads();
+        }
+        if (threadIdx.x == 0)
+          for (int i = 0; i < nw; ++i)
+            for (int j = i; j < nw; ++j) {
+              const double re = 0.5 * (M[i * kPolCap + j].x + M[j * kPolCap + i].x);
+              const double im = 0.5 * (M[i * kPolCap + j].y - M[j * kPolCap + i].y);
+              M[i * kPolCap + j] = make_double2(re, im);
+              M[j * kPolCap + i] = make_double2(re, -im);
+            }
+        __syncthreads();
+        if (threadIdx.x < 32) warp_jacobi_herm(nw, M, Zc, s_lam);
+        __syncthreads();
+        block_rotate_c(a, Vb, nw, Zc, nw, Yr);
+        block_rotate_c(a, HB, nw, Zc, nw, HYr);
+        double rr[kMaxNev];
+#pragma unroll
+        for (int i = 0; i < kMaxNev; ++i) rr[i] = 0.0;
+        for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
+          for (int i = 0; i < nev_out; ++i) {
+            const double2 hy = HYr[(size_t)i * a.ld + o], y = Yr[(size_t)i * a.ld + o];
+            const double rx = hy.x - s_lam[i] * y.x, ry = hy.y - s_lam[i] * y.y;
+            rr[i] += rx * rx + ry * ry;
+          }
+        block_sum<kMaxNev>(rr, s_red, s_misc + 8);
+        const double thL = msz > nw ? s_theta[nw] : HUGE_VAL;
+        bool ok = true;
+        dmax = 0.0;
+        for (int i = 0; i < nev_out; ++i) {
+          const double r2 = s_misc[8 + i], gap = thL - s_lam[i];
+          dmax = fmax(dmax, fabs(s_lam[i] - s_theta[i]));
+          ok = ok && (sqrt(r2) <= a.tol ||
+                      (gap > 0.0 && r2 <= kMixedRelTarget * fmax(fabs(s_lam[i]), 1e-6 * scale) * gap));
+        }
+        __syncthreads();
+        if (ok) {
+          if (threadIdx.x < nw) s_theta[threadIdx.x] = s_lam[threadIdx.x];
+          __syncthreads();
+          break;
+        }
+        if (invariant || stagnated || restarts >= a.maxiter || tau <= 1e-9) {
+          status = kPolishFailed;  // the host re-solves this request in FP64
+          break;
+        }
+        tau *= 0.1;
+      }
       // arrowhead restart matrix
-      const double bet = beta;
       __syncthreads();
       if (threadIdx.x == 0) {
-        double arrow[kMaxM];
-        for (int c = 0; c < keep; ++c) arrow[c] = bet * s_T[(msz - 1) * kMaxM + c];
         for (int i = 0; i < kMaxM * kMaxM; ++i) s_T[i] = 0.0;
         for (int c = 0; c < keep; ++c) {
           s_T[c * kMaxM + c] = s_theta[c];
-          s_T[c * kMaxM + keep] = s_T[keep * kMaxM + c] = arrow[c];
+          s_T[c * kMaxM + keep] = s_T[keep * kMaxM + c] = s_arrow[c];
         }
       }
       __syncthreads();
       k = keep;
       ++restarts;
     }
-    // ---- results (and the FP64 polish in mixed precision)
-    double dmax = 0.0;
-    if (sizeof(typename P::S) == 4 && status == 0) {
-      // H Y in FP64 (x = X64, tables in global FP64)
-      for (int i = 0; i < nev; ++i) {
-        block_normalize<double2>(a, Vb + (size_t)i * a.ld, 1.0, Rb + (size_t)(2 * kMaxNev) * 0 + (size_t)i * a.ld,
-                                 X64);
-        __syncthreads();
-        block_matvec<P64, FERMI, PHASES>(a, X64, tchi64, phase, s_isr, s_rank, s_rec, s_off, s_inv, rowflag,
-                                         Rb + (size_t)i * a.ld);
-        __syncthreads();
-      }
-      // Q = orthonormal residual directions into V[nev + q]
-      int q = 0;
-      for (int i = 0; i < nev; ++i) {
-        double2* Wq = W;
-        double r0 = 0.0;
-        for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
-          const double2 hy = Rb[(size_t)i * a.ld + o], y = Vb[(size_t)i * a.ld + o];
-          const double2 r = make_double2(hy.x - s_theta[i] * y.x, hy.y - s_theta[i] * y.y);
-          Wq[o] = r;
-          r0 += r.x * r.x + r.y * r.y;
-        }
-        __syncthreads();
-        r0 = block_sum1(r0, s_red, s_misc);
-        block_dots(a, Vb, nev + q, Wq, s_red, s_coef);
-        block_axpy(a, Vb, nev + q, s_coef, Wq);
-        __syncthreads();
-        block_dots(a, Vb, nev + q, Wq, s_red, s_coef);
-        double r1 = block_axpy(a, Vb, nev + q, s_coef, Wq);
-        __syncthreads();
-        r1 = block_sum1(r1, s_red, s_misc);
-        // nothing left to add when the residual is at rounding level or lies in span(Y, Q)
-        if (!(r1 > 1e-28) || !(r1 > 1e-6 * r0)) continue;
-        block_normalize<double2>(a, Wq, 1.0 / sqrt(r1), Vb + (size_t)(nev + q) * a.ld, X64);
-        __syncthreads();
-        block_matvec<P64, FERMI, PHASES>(a, X64, tchi64, phase, s_isr, s_rank, s_rec, s_off, s_inv, rowflag,
-                                         Rb + (size_t)(nev + q) * a.ld);
-        __syncthreads();
-        ++q;
-      }
-      const int nb = nev + q;
-      double2* M = reinterpret_cast<double2*>(s_Z);  // 16 x 16 complex fits in kMaxM^2 doubles
-      for (int bcol = 0; bcol < nb; ++bcol) {
-        block_dots(a, Vb, nb, Rb + (size_t)bcol * a.ld, s_red, s_coef);
-        if (threadIdx.x < nb) M[threadIdx.x * 16 + bcol] = s_coef[threadIdx.x];
-        __syncthreads();
-      }
-      if (threadIdx.x == 0) {
-        for (int i = 0; i < nb; ++i)
-          for (int j = i; j < nb; ++j) {
-            const double re = 0.5 * (M[i * 16 + j].x + M[j * 16 + i].x);
-            const double im = 0.5 * (M[i * 16 + j].y - M[j * 16 + i].y);
-            M[i * 16 + j] = make_double2(re, im);
-            M[j * 16 + i] = make_double2(re, -im);
-          }
-        double lam[16];
-        thread_jacobi_herm(nb, M, lam);
-        for (int i = 0; i < nev; ++i) {
-          dmax = fmax(dmax, fabs(lam[i] - s_theta[i]));
-          s_theta[i] = lam[i];
-        }
-        s_misc[3] = dmax;
-      }
-      __syncthreads();
-      dmax = s_misc[3];
-    }
     if (threadIdx.x == 0) {
-      for (int i = 0; i < a.nev; ++i) a.evals[(size_t)b * a.nev + i] = i < nev ? s_theta[i] : nan("");
+      for (int i = 0; i < a.nev; ++i) a.evals[(size_t)b * a.nev + i] = i < nev_out ? s_theta[i] : nan("");
       a.status[b] = status;
-      a.nmv[b] = nmv;
+      a.nmv[b] = nmv + n64;
       a.delta[b] = dmax;
       a.t_ns[2 * (size_t)b + 1] = global_ns();
     }
@@ -693,7 +981,19 @@ struct BatchImpl {
   TermTables tt;
   DevBuf site_off, rec, diag, V, R, W, X64, tchi64, rowflag;
   DevBuf in_chi, in_phase, in_amp, in_seed, o_evals, o_status, o_dims, o_delta, o_nmv, o_hops, o_tns, queue;
-  int last_n = 0;
+  int last_n = 0, n_fallback = 0;
+  DevBuf redo;
+  // hop table (built at the first run, rebuilt when the phase classes change)
+  int phi_cap = 0;       // phase-id capacity of the shared-memory layout (0: no table)
+  bool tab_valid = false;
+  int n_phi = 0;
+  std::vector<uint64_t> tab_fmask;  // [G][3] family class masks of the table
+  std::vector<int8_t> tab_rep;      // [G][4] class representative sites
+  std::vector<int32_t> row_cnt;     // hops per orbit row
+  DevBuf hop, sl_off, sl_w, phi_desc, rep_site, pwc64, fmask_dev;
+  int64_t hop_records = 0;
+  int last_tab = 0;
+  bool tab_enabled = true;
   size_t smem = 0;
   int64_t ld = 0;
   size_t footprint = 0;
@@ -746,11 +1046,13 @@ static BatchArgs base_args(BatchImpl& B) {
   a.inv = C.inv_u8.as<uint8_t>();
   a.diag = B.diag.as<double2>();
   a.atol = 1e-12;
+  a.kp1 = C.n_filled + 1;
+  a.phi_cap = B.phi_cap;
   return a;
 }
 
-static void dispatch_prepare(BatchImpl& B, const BatchArgs& a, BatchSmem& L, int& ncta, bool phases) {
-  const bool mixed = B.precision == 1;
+static void dispatch_prepare(BatchImpl& B, const BatchArgs& a, BatchSmem& L, int& ncta, bool fp64) {
+  const bool mixed = !fp64;
   // Each (precision, statistics) pair is compiled with the twisted-phase
   // product; untwisted requests multiply by exactly 1.
   if (mixed) {
@@ -760,11 +1062,11 @@ static void dispatch_prepare(BatchImpl& B, const BatchArgs& a, BatchSmem& L, int
     if (B.fermi) batch_prepare<P64, true, true, false>(B, a, L, ncta);
     else batch_prepare<P64, false, true, false>(B, a, L, ncta);
   }
-  (void)phases;
 }
 
-static void dispatch_launch(BatchImpl& B, const BatchArgs& a, const BatchSmem& L, int ncta, cudaStream_t s) {
-  if (B.precision == 1) {
+static void dispatch_launch(BatchImpl& B, const BatchArgs& a, const BatchSmem& L, int ncta, cudaStream_t s,
+                            bool fp64) {
+  if (!fp64) {
     if (B.fermi) batch_launch<P32, true, true, true>(a, L, ncta, s);
     else batch_launch<P32, false, true, true>(a, L, ncta, s);
   } else {
@@ -773,13 +1075,242 @@ static void dispatch_launch(BatchImpl& B, const BatchArgs& a, const BatchSmem& L
   }
 }
 
+// ------------------------------------------------------------ hop table
+// Every request of a batch shares the catalog and the (i, j) term list, so the
+// sparsity pattern of its sector matrix -- for each orbit row, the column
+// orbit, group element, sign and twist-phase class counts of every hop -- is
+// the same for all of them.  It is enumerated once into 64-bit records
+//   c (24 bits) | u*G + h (18 bits) << 24 | phi (22 bits) << 42,
+// phi indexing the distinct (h, class counts n_1..n_3, sign) combinations, and
+// stored SELL-32: slice s holds rows 32s..32s+31, record k of row 32s+l at
+// sl_off[s] + 32k + l, padded to the slice's longest row with records whose
+// phi is the zero coefficient.  A request then only builds its coefficient
+// tables; this is the batched counterpart of the reference's projection table
+// (build_projection_table / _apply_table!, SRE:680-765), kept per hop.
+static constexpr int kPhiCap = 2048;  // phase-id entries, the zero entry included
+
+__global__ void k_hop_count(int64_t n_orb, const uint64_t* __restrict__ reps, const uint16_t* off,
+                            const uint32_t* rec, int32_t* __restrict__ cnt) {
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_orb; o += (int64_t)gridDim.x * blockDim.x)
+    cnt[o] = (int32_t)count_row_hops(reps[o], off, rec);
+}
+
+// records in HopIter order; phase key = h | n1 << 6 | n2 << 12 | n3 << 18 |
+// sign << 24 (the host compacts the keys into phase ids)
+template <bool FERMI>
+__global__ void k_hop_fill(int64_t n_orb, const uint64_t* __restrict__ reps, const uint64_t* __restrict__ state,
+                           const uint32_t* __restrict__ rank_tab, RankParams rp, const uint16_t* off,
+                           const uint32_t* rec, const uint8_t* __restrict__ inv, int G,
+                           const uint64_t* __restrict__ fmask, const uint32_t* __restrict__ sl_off,
+                           const int32_t* __restrict__ sl_w, uint64_t* __restrict__ out,
+                           uint32_t* __restrict__ key) {
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_orb; o += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t base = (int64_t)sl_off[o >> 5] + (o & 31);
+    const int wdt = sl_w[o >> 5];
+    const uint64_t m = reps[o];
+    HopIter it;
+    it.init(m, off);
+    uint32_t r;
+    int from, k = 0;
+    while (it.next(off, rec, r, from)) {
+      const int j = r & 0xFF;
+      const uint64_t nw = m ^ ((1ULL << from) | (1ULL << j));
+      const uint64_t wd = state[dev::rank_of(nw, rank_tab, rp)];
+      int neg = (int)((wd >> 40) & 1);
+      if (FERMI) neg ^= __popcll(m & dev::bits_between(from, j)) & 1;
+      const int h = inv[(wd >> 32) & 0xFF];
+      const uint64_t* fm = fmask + 3 * h;
+      const uint32_t n1 = __popcll(nw & fm[0]), n2 = __popcll(nw & fm[1]), n3 = __popcll(nw & fm[2]);
+      out[base + 32 * (int64_t)k] = (uint64_t)(uint32_t)wd | ((uint64_t)((r >> 8) * G + h) << 24);
+      key[base + 32 * (int64_t)k] = (uint32_t)h | n1 << 6 | n2 << 12 | n3 << 18 | (uint32_t)neg << 24;
+      ++k;
+    }
+    for (; k < wdt; ++k) {
+      out[base + 32 * (int64_t)k] = 0;
+      key[base + 32 * (int64_t)k] = 0xFFFFFFFFu;
+    }
+  }
+}
+
+// Phase classes shared by the requests of one run: for every group element h,
+// the coarsest partition of the sites on which every request's phase eta_h is
+// constant (the common refinement of the requests' own partitions).  The
+// largest class is the base; up to three others get masks.  False when some h
+// needs more than four classes (the run then uses the on-the-fly matvec).
+static bool family_classes(const GroupImpl& G, int n_req, const double* phase, const std::vector<uint64_t>& init,
+                           std::vector<uint64_t>& fmask, std::vector<int8_t>& rep) {
+  const int N = G.n_site, nG = G.n_ops;
+  fmask.assign((size_t)nG * 3, 0);
+  rep.assign((size_t)nG * 4, -1);
+  std::vector<int> cls(N), ncls(N);
+  struct Key {
+    int c;
+    double re, im;
+    int id;
+  };
+  std::vector<Key> keys;
+  for (int h = 0; h < nG; ++h) {
+    // start from the given partition (the current table's), so a compatible
+    // run keeps it
+    int nc = 1;
+    for (int q = 0; q < N; ++q) {
+      cls[q] = 0;
+      for (int c = 0; c < 3 && !init.empty(); ++c)
+        if ((init[(size_t)h * 3 + c] >> q) & 1ULL) {
+          cls[q] = c + 1;
+          nc = std::max(nc, c + 2);
+        }
+    }
+    for (int b = 0; b < n_req; ++b) {
+      const double* ph = phase + ((size_t)b * nG + h) * N * 2;
+      keys.clear();
+      for (int q = 0; q < N; ++q) {
+        const double re = ph[2 * q], im = ph[2 * q + 1];
+        int id = -1;
+        for (const Key& k : keys)
+          if (k.c == cls[q] && k.re == re && k.im == im) id = k.id;
+        if (id < 0) {
+          id = (int)keys.size();
+          if (id >= 4) return false;
+          keys.push_back({cls[q], re, im, id});
+        }
+        ncls[q] = id;
+      }
+      cls.swap(ncls);
+      nc = (int)keys.size();
+    }
+    std::vector<int> size(nc, 0);
+    for (int q = 0; q < N; ++q) ++size[cls[q]];
+    int bc = 0;
+    for (int c = 1; c < nc; ++c)
+      if (size[c] > size[bc]) bc = c;
+    int slot = 0;
+    for (int c = 0; c < nc; ++c) {
+      int first = -1;
+      uint64_t msk = 0;
+      for (int q = 0; q < N; ++q)
+        if (cls[q] == c) {
+          if (first < 0) first = q;
+          msk |= 1ULL << q;
+        }
+      if (c == bc) {
+        rep[(size_t)h * 4] = (int8_t)first;
+      } else {
+        fmask[(size_t)h * 3 + slot] = msk;
+        rep[(size_t)h * 4 + 1 + slot] = (int8_t)first;
+        ++slot;
+      }
+    }
+  }
+  return true;
+}
+
+// Make the hop table match this run's phase classes; returns whether the run
+// can use it.  phase is the host copy of the requests' group phases.
+static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStream_t s) {
+  if (B.phi_cap == 0 || !B.tab_enabled) return false;
+  const CatalogImpl& C = *B.cat;
+  const GroupImpl& G = *C.group;
+  if (C.n_orbits >= (1 << 24) || (int64_t)B.n_bil * G.n_ops >= (1 << 18) || C.n_filled > 63) return false;
+  std::vector<uint64_t> fmask;
+  std::vector<int8_t> rep;
+  // refine the current table's partition; if that needs too many classes,
+  // partition this run alone
+  const std::vector<uint64_t> none;
+  if (!(B.tab_valid && family_classes(G, n_req, phase, B.tab_fmask, fmask, rep)) &&
+      !family_classes(G, n_req, phase, none, fmask, rep))
+    return false;
+  if (B.tab_valid && fmask == B.tab_fmask) {
+    if (rep != B.tab_rep) {
+      B.tab_rep = rep;
+      upload(B.rep_site, B.tab_rep, s);
+    }
+    return true;
+  }
+  B.tab_valid = false;
+  const int64_t n = C.n_orbits;
+  const int64_t n_sl = (n + 31) / 32;
+  const int grid = grid1(n, 256);
+  if (B.row_cnt.empty()) {
+    DevBuf cnt((size_t)std::max<int64_t>(n, 1) * 4);
+    k_hop_count<<<grid, 256, 0, s>>>(n, C.reps.as<uint64_t>(), B.site_off.as<uint16_t>(), B.rec.as<uint32_t>(),
+                                     cnt.as<int32_t>());
+    SED_CUDA(cudaGetLastError());
+    B.row_cnt.resize(n);
+    SED_CUDA(cudaMemcpyAsync(B.row_cnt.data(), cnt.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    SED_CUDA(cudaStreamSynchronize(s));
+    std::vector<uint32_t> off(n_sl);
+    std::vector<int32_t> w(n_sl);
+    int64_t tot = 0;
+    for (int64_t sl = 0; sl < n_sl; ++sl) {
+      int mx = 0;
+      for (int64_t o = sl * 32; o < std::min(n, sl * 32 + 32); ++o) mx = std::max(mx, B.row_cnt[o]);
+      SED_REQUIRE(tot < (int64_t)UINT32_MAX, 5, "hop table too large");
+      off[sl] = (uint32_t)tot;
+      w[sl] = mx;
+      tot += 32 * (int64_t)mx;
+    }
+    B.hop_records = tot;
+    upload(B.sl_off, off, s);
+    upload(B.sl_w, w, s);
+    B.hop.alloc((size_t)std::max<int64_t>(tot, 1) * 8);
+  }
+  upload(B.fmask_dev, fmask, s);
+  const int64_t tot = B.hop_records;
+  DevBuf keyd((size_t)std::max<int64_t>(tot, 1) * 4);
+  if (G.stats == 1)
+    k_hop_fill<true><<<grid, 256, 0, s>>>(n, C.reps.as<uint64_t>(), C.state.as<uint64_t>(), C.rank.dev.as<uint32_t>(),
+                                          C.rank.rp, B.site_off.as<uint16_t>(), B.rec.as<uint32_t>(),
+                                          C.inv_u8.as<uint8_t>(), G.n_ops, B.fmask_dev.as<uint64_t>(),
+                                          B.sl_off.as<uint32_t>(), B.sl_w.as<int32_t>(), B.hop.as<uint64_t>(),
+                                          keyd.as<uint32_t>());
+  else
+    k_hop_fill<false><<<grid, 256, 0, s>>>(n, C.reps.as<uint64_t>(), C.state.as<uint64_t>(), C.rank.dev.as<uint32_t>(),
+                                           C.rank.rp, B.site_off.as<uint16_t>(), B.rec.as<uint32_t>(),
+                                           C.inv_u8.as<uint8_t>(), G.n_ops, B.fmask_dev.as<uint64_t>(),
+                                           B.sl_off.as<uint32_t>(), B.sl_w.as<int32_t>(), B.hop.as<uint64_t>(),
+                                           keyd.as<uint32_t>());
+  SED_CUDA(cudaGetLastError());
+  std::vector<uint64_t> recs(tot);
+  std::vector<uint32_t> keys(tot);
+  SED_CUDA(cudaMemcpyAsync(recs.data(), B.hop.p, (size_t)tot * 8, cudaMemcpyDeviceToHost, s));
+  SED_CUDA(cudaMemcpyAsync(keys.data(), keyd.p, (size_t)tot * 4, cudaMemcpyDeviceToHost, s));
+  SED_CUDA(cudaStreamSynchronize(s));
+  // compact the phase keys (first-appearance order) into phase ids
+  std::unordered_map<uint32_t, uint32_t> id;
+  std::vector<uint32_t> desc;
+  for (int64_t t = 0; t < tot; ++t) {
+    if (keys[t] == 0xFFFFFFFFu) continue;
+    auto it = id.find(keys[t]);
+    if (it == id.end()) {
+      if ((int)desc.size() + 1 >= B.phi_cap) return false;
+      it = id.emplace(keys[t], (uint32_t)desc.size()).first;
+      desc.push_back(keys[t]);
+    }
+  }
+  const uint64_t zero_id = desc.size();
+  for (int64_t t = 0; t < tot; ++t) {
+    const uint64_t phi = keys[t] == 0xFFFFFFFFu ? zero_id : id[keys[t]];
+    recs[t] = (recs[t] & ((1ULL << 42) - 1)) | (phi << 42);
+  }
+  SED_CUDA(cudaMemcpyAsync(B.hop.p, recs.data(), (size_t)tot * 8, cudaMemcpyHostToDevice, s));
+  upload(B.phi_desc, desc, s);
+  B.n_phi = (int)desc.size();
+  B.tab_fmask = fmask;
+  B.tab_rep = rep;
+  upload(B.rep_site, B.tab_rep, s);
+  SED_CUDA(cudaStreamSynchronize(s));
+  B.tab_valid = true;
+  return true;
+}
+
 std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil, const int32_t* bil_ij, int n_den,
                                       const int32_t* den_ij, const double* den_v, int precision, int nev,
                                       int krylovdim, int max_req) {
   const CatalogImpl& C = *cp;
   const GroupImpl& G = *C.group;
   SED_REQUIRE(precision == 0 || precision == 1, 1, "precision must be SED_PREC_FP64 or SED_PREC_MIXED");
-  SED_REQUIRE(nev >= 1 && nev <= kMaxNev, 5, "batched solves support 1 <= nev <= 8");
+  SED_REQUIRE(nev >= 1 && nev <= kMaxNev - 2, 5, "batched solves support 1 <= nev <= 6");
   SED_REQUIRE(max_req >= 1, 1, "max_requests must be positive");
   SED_REQUIRE(n_bil >= 0 && n_bil < 65535, 5, "at most 65534 bilinear terms");
   SED_REQUIRE(n_bil == 0 || bil_ij, 1, "bilinear index array must not be NULL");
@@ -789,7 +1320,7 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   B->cat = cp;
   B->precision = precision;
   B->nev = nev;
-  B->m = std::min(std::max(krylovdim, 2 * nev + 1), kMaxM);
+  B->m = std::min(std::max(krylovdim, 2 * (nev + 2) + 1), kMaxM);
   B->max_req = max_req;
   B->n_bil = n_bil;
   B->n_den = n_den;
@@ -829,23 +1360,33 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   B->diag.alloc((size_t)std::max<int64_t>(n, 1) * 16);
   compute_diag(n, C.reps.as<uint64_t>(), nullptr, n_den, ddij.as<int32_t>(), ddv.as<double2>(), B->diag.as<double2>(),
                s);
+  // the hop table's phase-id coefficients need shared memory; a sector too
+  // large for both keeps the on-the-fly matvec
+  B->phi_cap = kPhiCap;
   BatchArgs a = base_args(*B);
+  const size_t with_tab =
+      precision == 1 ? batch_layout<float2>(a, true).total : batch_layout<double2>(a, false).total;
+  if (with_tab > 220 * 1024) {
+    B->phi_cap = 0;
+    a.phi_cap = 0;
+  }
   BatchSmem L;
   int ncta = 1;
-  dispatch_prepare(*B, a, L, ncta, true);
+  dispatch_prepare(*B, a, L, ncta, precision == 0);
   B->smem = L.total;
   // per-block workspace, bounded to 16 GB
-  const size_t per_cta = ((size_t)(B->m + 1) + (size_t)std::max(B->m, 3 * nev) + 2) * B->ld * 16 +
+  const size_t per_cta = ((size_t)(B->m + 1) + (size_t)std::max(B->m, 5 * (nev + 2)) + 2) * B->ld * 16 +
                          (size_t)n_bil * G.n_ops * 16 + B->ld;
   ncta = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)ncta, (int64_t)max_req,
                                                       (int64_t)((16ull << 30) / std::max<size_t>(per_cta, 1))}));
   B->n_cta = ncta;
   B->V.alloc((size_t)ncta * (B->m + 1) * B->ld * 16);
-  B->R.alloc((size_t)ncta * std::max(B->m, 3 * nev) * B->ld * 16);
+  B->R.alloc((size_t)ncta * std::max(B->m, 5 * (nev + 2)) * B->ld * 16);
   B->W.alloc((size_t)ncta * B->ld * 16);
   B->X64.alloc((size_t)ncta * B->ld * 16);
   B->tchi64.alloc((size_t)ncta * std::max(n_bil * G.n_ops, 1) * 16);
   B->rowflag.alloc((size_t)ncta * B->ld);
+  if (B->phi_cap) B->pwc64.alloc((size_t)ncta * B->phi_cap * 16);
   B->in_chi.alloc((size_t)max_req * G.n_ops * 16);
   B->in_phase.alloc((size_t)max_req * G.n_ops * G.n_site * 16);
   B->in_amp.alloc((size_t)max_req * std::max(n_bil, 1) * 16);
@@ -875,12 +1416,13 @@ static void validate_requests(BatchImpl& B, int n_req, const double* phase, cons
 // Launch on device-resident buffers (asynchronous on the batch stream).
 void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const double* phase, const double* amp,
                          const uint64_t* seeds, double tol, int maxiter, double* evals, int32_t* status,
-                         int64_t* dims, double* delta, int32_t* nmv) {
+                         int64_t* dims, double* delta, int32_t* nmv, const double* phase_host = nullptr) {
   SED_REQUIRE(n_req >= 0 && n_req <= B.max_req, 1, "n_req exceeds max_requests");
   SED_REQUIRE(tol > 0.0 && maxiter >= 1, 1, "tol and maxiter must be positive");
   SED_REQUIRE(chi && phase && seeds && evals && status && dims && delta && nmv, 1, "NULL argument");
   SED_REQUIRE(B.n_bil == 0 || amp, 1, "NULL bilinear amplitudes");
   B.last_n = n_req;
+  B.n_fallback = 0;
   if (n_req == 0) return;
   cudaStream_t s = B.stream;
   SED_CUDA(cudaMemsetAsync(B.queue.p, 0, 16, s));
@@ -906,11 +1448,55 @@ void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const doubl
   a.hops = B.o_hops.as<int64_t>();
   a.t_ns = B.o_tns.as<int64_t>();
   a.queue = B.queue.as<unsigned int>();
+  // hop table for this run's phase classes (needs the phases on the host)
+  std::vector<double> ph_h;
+  if (B.phi_cap > 0 && B.tab_enabled && !phase_host) {
+    const GroupImpl& G = *B.cat->group;
+    ph_h.resize((size_t)n_req * G.n_ops * G.n_site * 2);
+    SED_CUDA(cudaMemcpyAsync(ph_h.data(), phase, ph_h.size() * 8, cudaMemcpyDeviceToHost, s));
+    SED_CUDA(cudaStreamSynchronize(s));
+    phase_host = ph_h.data();
+  }
+  a.use_tab = phase_host && prepare_table(B, n_req, phase_host, s) ? 1 : 0;
+  if (a.use_tab) {
+    a.n_phi = B.n_phi;
+    a.hop = B.hop.as<uint64_t>();
+    a.sl_off = B.sl_off.as<uint32_t>();
+    a.sl_w = B.sl_w.as<int32_t>();
+    a.phi_desc = B.phi_desc.as<uint32_t>();
+    a.rep_site = B.rep_site.as<int8_t>();
+    a.pwc64 = B.pwc64.as<double2>();
+  }
+  B.last_tab = a.use_tab;
   BatchSmem L;
   int ncta = 1;
-  dispatch_prepare(B, a, L, ncta, true);
+  dispatch_prepare(B, a, L, ncta, B.precision == 0);
   ncta = std::min(B.n_cta, n_req);
-  dispatch_launch(B, a, L, ncta, s);
+  dispatch_launch(B, a, L, ncta, s, B.precision == 0);
+  if (B.precision == 1) {
+    // requests whose FP64 polish missed its residual target are answered by
+    // the all-FP64 kernel (same inputs, same seed), so no unconverged pair is
+    // ever returned
+    std::vector<int32_t> st(n_req);
+    SED_CUDA(cudaMemcpyAsync(st.data(), status, (size_t)n_req * 4, cudaMemcpyDeviceToHost, s));
+    SED_CUDA(cudaStreamSynchronize(s));
+    std::vector<int32_t> redo;
+    for (int i = 0; i < n_req; ++i)
+      if (st[i] == kPolishFailed) redo.push_back(i);
+    B.n_fallback = (int)redo.size();
+    if (!redo.empty()) {
+      upload(B.redo, redo, s);
+      SED_CUDA(cudaMemsetAsync(B.queue.p, 0, 16, s));
+      BatchArgs a2 = a;
+      a2.n_req = (int)redo.size();
+      a2.req_list = B.redo.as<int32_t>();
+      BatchSmem L2;
+      int nc2 = 1;
+      dispatch_prepare(B, a2, L2, nc2, true);
+      nc2 = std::min(B.n_cta, a2.n_req);
+      dispatch_launch(B, a2, L2, nc2, s, true);
+    }
+  }
 }
 
 void batch_run(BatchImpl& B, int n_req, const double* chi, const double* phase, const double* amp,
@@ -931,7 +1517,7 @@ void batch_run(BatchImpl& B, int n_req, const double* chi, const double* phase, 
   SED_CUDA(cudaMemcpyAsync(B.in_seed.p, seeds, (size_t)n_req * 8, cudaMemcpyHostToDevice, s));
   batch_launch_device(B, n_req, B.in_chi.as<double>(), B.in_phase.as<double>(), B.in_amp.as<double>(),
                       B.in_seed.as<uint64_t>(), tol, maxiter, B.o_evals.as<double>(), B.o_status.as<int32_t>(),
-                      B.o_dims.as<int64_t>(), B.o_delta.as<double>(), B.o_nmv.as<int32_t>());
+                      B.o_dims.as<int64_t>(), B.o_delta.as<double>(), B.o_nmv.as<int32_t>(), phase);
   SED_CUDA(cudaMemcpyAsync(evals, B.o_evals.p, (size_t)n_req * B.nev * 8, cudaMemcpyDeviceToHost, s));
   if (status) SED_CUDA(cudaMemcpyAsync(status, B.o_status.p, (size_t)n_req * 4, cudaMemcpyDeviceToHost, s));
   if (dims) SED_CUDA(cudaMemcpyAsync(dims, B.o_dims.p, (size_t)n_req * 8, cudaMemcpyDeviceToHost, s));
@@ -1007,6 +1593,22 @@ int sed_batch_last_stats(const sed_batch* b, int64_t* hops, int64_t* t_start_ns,
   return bguard([&] {
     SED_REQUIRE(b, 1, "NULL batch");
     sed::batch_last_stats(*b->p, hops, t_start_ns, t_end_ns);
+  });
+}
+
+int sed_batch_last_info(const sed_batch* b, int32_t* n_fallback, int32_t* hop_table, int64_t* hop_records) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    if (n_fallback) *n_fallback = b->p->n_fallback;
+    if (hop_table) *hop_table = b->p->last_tab;
+    if (hop_records) *hop_records = b->p->last_tab ? b->p->hop_records : 0;
+  });
+}
+
+int sed_batch_set_hop_table(sed_batch* b, int enable) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    b->p->tab_enabled = enable != 0;
   });
 }
 

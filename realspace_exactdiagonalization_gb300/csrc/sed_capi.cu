@@ -127,6 +127,17 @@ int sed_sector_build(const sed_catalog* c, const double* chi_reim, double atol, 
     *out = new sed_sector{s};
   });
 }
+int sed_sector_build_group(const sed_catalog* c, const sed_group* g, const double* chi_reim, double atol,
+                           sed_sector** out, int64_t* dim) {
+  return guarded([&] {
+    REQ(c && g && out, "NULL argument");
+    REQ(atol >= 0.0, "atol must be non-negative");
+    *out = nullptr;
+    auto s = sed::build_sector(c->p, chi_reim, atol, g->p);
+    if (dim) *dim = s->dim;
+    *out = new sed_sector{s};
+  });
+}
 int sed_sector_get(const sed_sector* s, uint64_t* reps, int32_t* stab_order, int32_t* orbit_index) {
   return guarded([&] {
     REQ(s, "NULL sector");

@@ -374,7 +374,8 @@ std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> gp, int n_
   c->reps.alloc((size_t)c->n_orbits * 8);
   c->stab.alloc((size_t)c->n_orbits);
   const size_t smem = (size_t)c->rank.rp.total * 4;
-  if (smem > 48 * 1024) SED_CUDA(cudaFuncSetAttribute(k_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // the opt-in covers the dynamic part; the kernel also holds 4 KB of static shared memory
+  SED_CUDA(cudaFuncSetAttribute(k_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_expand<<<grid_for(nw, 256), 256, smem, s>>>(n_states, G.n_site, n_filled, G.n_ops, G.stats,
                                                 c->perm_u8.as<uint8_t>(), c->binom.as<uint64_t>(),
                                                 flags.as<uint32_t>(), offs.as<uint32_t>(),
@@ -565,15 +566,23 @@ __global__ void k_sector_rows(int64_t nw, const uint32_t* __restrict__ words, co
   }
 }
 
-std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> cp, const double* chi, double atol) {
+std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> cp, const double* chi, double atol,
+                                         std::shared_ptr<GroupImpl> gp) {
   CatalogImpl& c = *cp;
-  const GroupImpl& G = *c.group;
+  if (!gp) gp = c.group;
+  const GroupImpl& G = *gp;
+  const GroupImpl& CG = *c.group;
+  SED_REQUIRE(G.n_site == CG.n_site && G.n_ops == CG.n_ops && G.perm == CG.perm && G.stats == CG.stats &&
+                  G.inv == CG.inv,
+              1, "the sector's group must have the catalog's permutations and statistics");
   SED_REQUIRE(chi != nullptr, 1, "chi must not be NULL");
   auto S = std::make_shared<SectorImpl>();
   S->cat = cp;
+  S->group = gp;
   S->chi.assign(chi, chi + 2 * G.n_ops);
   S->atol = atol;
   cudaStream_t s = c.stream;
+  upload(S->phase, G.phase, s);
   const int64_t n = c.n_orbits;
   const int64_t nw = (n + 31) / 32;
   S->rowflag.alloc((size_t)std::max<int64_t>(n, 1));
@@ -582,7 +591,7 @@ std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> cp, const 
   if (n > 0) {
     const int blocks = (int)std::min<int64_t>((nw * 32 + 255) / 256, (int64_t)device_sm_count() * 16);
     k_sector_compat<<<blocks, 256, 0, s>>>(n, G.n_ops, G.n_site, G.stats, c.reps.as<uint64_t>(),
-                                           c.perm_u8.as<uint8_t>(), c.phase.as<double2>(), dchi.as<double2>(), atol,
+                                           c.perm_u8.as<uint8_t>(), S->phase.as<double2>(), dchi.as<double2>(), atol,
                                            S->rowflag.as<uint8_t>(), words.as<uint32_t>());
     SED_CUDA(cudaGetLastError());
   }
@@ -644,7 +653,7 @@ __global__ void k_orbit_row(int64_t dim, const uint32_t* __restrict__ row_orbit,
 
 void sector_project(const SectorImpl& S, int64_t n, const uint64_t* masks, int64_t* rows, double* coeff) {
   const CatalogImpl& c = *S.cat;
-  const GroupImpl& G = *c.group;
+  const GroupImpl& G = *S.group;
   SED_REQUIRE(n >= 0 && (n == 0 || (masks && rows && coeff)), 1, "NULL argument");
   const uint64_t valid = G.n_site == 64 ? ~0ULL : ((1ULL << G.n_site) - 1ULL);
   for (int64_t i = 0; i < n; ++i)
@@ -662,7 +671,7 @@ void sector_project(const SectorImpl& S, int64_t n, const uint64_t* masks, int64
   k_sector_project<<<grid_for(n, 256), 256, 0, s>>>(n, dm.as<uint64_t>(), c.state.as<uint64_t>(), c.reps.as<uint64_t>(),
                                                     orow.as<int32_t>(), G.n_ops, G.n_site, G.stats,
                                                     c.perm_u8.as<uint8_t>(), c.inv_u8.as<uint8_t>(),
-                                                    c.phase.as<double2>(), dchi.as<double2>(),
+                                                    S.phase.as<double2>(), dchi.as<double2>(),
                                                     c.rank.dev.as<uint32_t>(), c.rank.rp, dr.as<int64_t>(),
                                                     dc.as<double2>());
   SED_CUDA(cudaGetLastError());

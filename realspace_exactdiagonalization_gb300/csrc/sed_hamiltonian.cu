@@ -17,6 +17,7 @@
 // P_h(new) is the per-site phase product of a flux-twisted group (1 otherwise).
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <map>
 
 #include "sed_internal.cuh"
@@ -101,6 +102,67 @@ void check_hermitian_symmetric(const GroupImpl& G, int n_bil, const int32_t* bil
   }
 }
 
+void compute_phase_classes(const GroupImpl& G, int k, PhaseClassTables& pc) {
+  const int nG = G.n_ops, N = G.n_site;
+  pc.kp1 = k + 1;
+  pc.mask.assign((size_t)nG * kMaxCls, 0);
+  pc.pw.assign((size_t)nG * kMaxCls * pc.kp1 * 2, 0.0);
+  pc.base_k.assign((size_t)nG * 2, 0.0);
+  for (int h = 0; h < nG; ++h) pc.base_k[2 * h] = 1.0;
+  for (size_t i = 0; i < pc.pw.size() / 2; i += pc.kp1) pc.pw[2 * i] = 1.0;  // r^0 = 1 for every class
+  if (!G.has_phases) {
+    pc.mode = 0;
+    return;
+  }
+  pc.mode = 1;
+  for (int h = 0; h < nG && pc.mode == 1; ++h) {
+    std::vector<std::pair<double, double>> val;
+    std::vector<uint64_t> msk;
+    for (int j = 0; j < N; ++j) {
+      const double re = G.phase[((size_t)h * N + j) * 2], im = G.phase[((size_t)h * N + j) * 2 + 1];
+      size_t c = 0;
+      while (c < val.size() && !(val[c].first == re && val[c].second == im)) ++c;
+      if (c == val.size()) {
+        val.push_back({re, im});
+        msk.push_back(0);
+      }
+      msk[c] |= 1ULL << j;
+    }
+    if (val.size() > (size_t)kMaxCls + 1) {
+      pc.mode = 2;
+      break;
+    }
+    size_t b = 0;
+    for (size_t c = 1; c < val.size(); ++c)
+      if (__builtin_popcountll(msk[c]) > __builtin_popcountll(msk[b])) b = c;
+    const std::complex<double> base(val[b].first, val[b].second);
+    std::complex<double> bk(1.0, 0.0);
+    for (int e = 0; e < k; ++e) bk *= base;
+    pc.base_k[2 * h] = bk.real();
+    pc.base_k[2 * h + 1] = bk.imag();
+    int slot = 0;
+    for (size_t c = 0; c < val.size(); ++c) {
+      if (c == b) continue;
+      const std::complex<double> r = std::complex<double>(val[c].first, val[c].second) / base;
+      pc.mask[(size_t)h * kMaxCls + slot] = msk[c];
+      std::complex<double> pw(1.0, 0.0);
+      for (int e = 0; e <= k; ++e) {
+        const size_t idx = (((size_t)h * kMaxCls + slot) * pc.kp1 + e) * 2;
+        pc.pw[idx] = pw.real();
+        pc.pw[idx + 1] = pw.imag();
+        pw *= r;
+      }
+      ++slot;
+    }
+  }
+  if (pc.mode == 2) {  // per-site product: no folding, tables unused
+    for (int h = 0; h < nG; ++h) {
+      pc.base_k[2 * h] = 1.0;
+      pc.base_k[2 * h + 1] = 0.0;
+    }
+  }
+}
+
 struct ApplyArgs {
   int64_t n_orb;
   int N, G, n_class, n_terms;
@@ -117,13 +179,16 @@ struct ApplyArgs {
   const void* amp;   // [n_class] V     (on-the-fly mode)
   const void* chi;   // [G] V
   const uint8_t* inv;
-  const void* eta;   // [G][N] V        (twisted groups)
+  const void* eta;   // [G][N] V        (twisted groups, per-site product)
+  const uint64_t* cls_mask;  // [G][3]
+  const void* cls_pw;        // [G][3][k+1] V
+  int phase_mode, kp1;
 };
 
 // Shared-memory image of the tables, 16-byte aligned pieces first.
 template <class V>
 struct SmemLayout {
-  size_t tchi, chi, isr, rank, rec, site_off, inv, total;
+  size_t tchi, chi, isr, pw, mask, rank, rec, site_off, inv, total;
   static SmemLayout make(const ApplyArgs& a, bool table) {
     SmemLayout L;
     size_t o = 0;
@@ -134,6 +199,10 @@ struct SmemLayout {
     o = al(o + (size_t)a.G * sizeof(V));
     L.isr = o;
     o = al(o + 65 * sizeof(double));
+    L.pw = o;
+    o = al(o + (a.phase_mode == 1 ? (size_t)a.G * kMaxCls * a.kp1 * sizeof(V) : 0));
+    L.mask = o;
+    o = al(o + (a.phase_mode == 1 ? (size_t)a.G * kMaxCls * 8 : 0));
     L.rank = o;
     o = al(o + (size_t)a.rp.total * 4);
     L.rec = o;
@@ -147,8 +216,12 @@ struct SmemLayout {
   }
 };
 
+// 512-thread blocks: the shared tables (~50 KB for 48 sites) allow three
+// resident blocks per SM, i.e. 1536 threads keeping random loads in flight.
+static constexpr int kApplyBS = 512;
+
 template <class P, bool FERMI, bool PHASES, bool TABLE>
-__global__ void __launch_bounds__(256) k_apply(ApplyArgs a, SmemLayout<typename P::V> L,
+__global__ void __launch_bounds__(kApplyBS) k_apply(ApplyArgs a, SmemLayout<typename P::V> L,
                                                const typename P::V* __restrict__ xs, double2* __restrict__ y) {
   using V = typename P::V;
   using S = typename P::S;
@@ -160,7 +233,14 @@ __global__ void __launch_bounds__(256) k_apply(ApplyArgs a, SmemLayout<typename 
   uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem + L.rec);
   uint16_t* s_off = reinterpret_cast<uint16_t*>(smem + L.site_off);
   uint8_t* s_inv = reinterpret_cast<uint8_t*>(smem + L.inv);
+  V* s_pw = reinterpret_cast<V*>(smem + L.pw);
+  uint64_t* s_mask = reinterpret_cast<uint64_t*>(smem + L.mask);
   {
+    if (PHASES && a.phase_mode == 1) {
+      const V* pw = reinterpret_cast<const V*>(a.cls_pw);
+      for (int i = threadIdx.x; i < a.G * kMaxCls * a.kp1; i += blockDim.x) s_pw[i] = pw[i];
+      for (int i = threadIdx.x; i < a.G * kMaxCls; i += blockDim.x) s_mask[i] = a.cls_mask[i];
+    }
     const int nt = TABLE ? a.n_class * a.G : a.n_class;
     const V* src = reinterpret_cast<const V*>(TABLE ? a.tchi : a.amp);
     for (int i = threadIdx.x; i < nt; i += blockDim.x) s_tchi[i] = src[i];
@@ -174,6 +254,7 @@ __global__ void __launch_bounds__(256) k_apply(ApplyArgs a, SmemLayout<typename 
   }
   __syncthreads();
   const V* __restrict__ eta = reinterpret_cast<const V*>(a.eta);
+  const PhaseClasses<V> pcl{a.phase_mode, a.kp1, s_mask, s_pw};
   for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < a.n_orb; o += (int64_t)gridDim.x * blockDim.x) {
     if (!a.rowflag[o]) {
       y[o] = make_double2(0.0, 0.0);
@@ -184,7 +265,7 @@ __global__ void __launch_bounds__(256) k_apply(ApplyArgs a, SmemLayout<typename 
     S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
     S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
     row_gather<P, FERMI, PHASES, TABLE>(a.reps[o], xs, s_tchi, s_chi, a.G, eta, a.N, s_rank, a.rp, s_rec, s_off,
-                                        s_inv, a.state, ar, ai);
+                                        s_inv, a.state, ar, ai, pcl);
     const double is = s_isr[a.stab[o]];
     y[o] = make_double2((double)ar * is, (double)ai * is);
   }
@@ -272,7 +353,7 @@ std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> sp, int n_bil, const
   SED_REQUIRE(n_den == 0 || (den_ij && den_v), 1, "density arrays must not be NULL");
   const SectorImpl& S = *sp;
   const CatalogImpl& C = *S.cat;
-  const GroupImpl& G = *C.group;
+  const GroupImpl& G = *S.group;
   check_hermitian_symmetric(G, n_bil, bil_ij, bil_t);
   for (int k = 0; k < n_den; ++k)
     SED_REQUIRE(den_ij[2 * k] >= 0 && den_ij[2 * k] < G.n_site && den_ij[2 * k + 1] >= 0 &&
@@ -288,13 +369,18 @@ std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> sp, int n_bil, const
   const TermTables& tt = op->terms;
   upload(op->site_off, tt.site_off, s);
   upload(op->rec, tt.rec, s);
-  // tchi[u][h] = conj(t_u) * chi(h), and the plain amplitude / chi tables
+  // phase classes of the (twisted) group; base^k folds into tchi
+  compute_phase_classes(G, C.n_filled, op->pc);
+  upload(op->cls_mask, op->pc.mask, s);
+  // tchi[u][h] = conj(t_u) * chi(h) * conj(base_h^k), and the plain amplitude / chi tables
   const int nG = G.n_ops;
   std::vector<double> tchi((size_t)tt.n_class * nG * 2);
   for (int u = 0; u < tt.n_class; ++u)
     for (int h = 0; h < nG; ++h) {
       const double tr = tt.amp[2 * u], ti = -tt.amp[2 * u + 1];
-      const double cr = S.chi[2 * h], ci = S.chi[2 * h + 1];
+      const double br = op->pc.base_k[2 * h], bi = -op->pc.base_k[2 * h + 1];
+      const double cr0 = S.chi[2 * h], ci0 = S.chi[2 * h + 1];
+      const double cr = cr0 * br - ci0 * bi, ci = cr0 * bi + ci0 * br;  // chi(h) * conj(base^k)
       tchi[((size_t)u * nG + h) * 2] = tr * cr - ti * ci;
       tchi[((size_t)u * nG + h) * 2 + 1] = tr * ci + ti * cr;
     }
@@ -310,8 +396,16 @@ std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> sp, int n_bil, const
   std::vector<double> pack;
   pack.insert(pack.end(), tchi.begin(), tchi.end());
   pack.insert(pack.end(), ampc.begin(), ampc.end());
-  pack.insert(pack.end(), S.chi.begin(), S.chi.end());
+  std::vector<double> chib(S.chi);  // chi * conj(base^k) for the on-the-fly coefficient
+  for (int h = 0; h < nG; ++h) {
+    const double br = op->pc.base_k[2 * h], bi = -op->pc.base_k[2 * h + 1];
+    const double cr0 = S.chi[2 * h], ci0 = S.chi[2 * h + 1];
+    chib[2 * h] = cr0 * br - ci0 * bi;
+    chib[2 * h + 1] = cr0 * bi + ci0 * br;
+  }
+  pack.insert(pack.end(), chib.begin(), chib.end());
   pack.insert(pack.end(), eta.begin(), eta.end());
+  pack.insert(pack.end(), op->pc.pw.begin(), op->pc.pw.end());
   upload(op->tchi64, pack, s);
   upload(op->tchi32, to32(pack), s);
   // density-density diagonal (SRE:697-703)
@@ -334,7 +428,7 @@ std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> sp, int n_bil, const
 static ApplyArgs make_args(const OpImpl& op, bool fp32) {
   const SectorImpl& S = *op.sec;
   const CatalogImpl& C = *S.cat;
-  const GroupImpl& G = *C.group;
+  const GroupImpl& G = *S.group;
   const TermTables& tt = op.terms;
   ApplyArgs a{};
   a.n_orb = C.n_orbits;
@@ -357,6 +451,10 @@ static ApplyArgs make_args(const OpImpl& op, bool fp32) {
   a.amp = base + (size_t)tt.n_class * G.n_ops * el;
   a.chi = base + ((size_t)tt.n_class * G.n_ops + tt.n_class) * el;
   a.eta = base + ((size_t)tt.n_class * G.n_ops + tt.n_class + G.n_ops) * el;
+  a.cls_pw = base + ((size_t)tt.n_class * G.n_ops + tt.n_class + G.n_ops + (size_t)G.n_ops * G.n_site) * el;
+  a.cls_mask = op.cls_mask.as<uint64_t>();
+  a.phase_mode = op.pc.mode;
+  a.kp1 = op.pc.kp1;
   a.inv = C.inv_u8.as<uint8_t>();
   return a;
 }
@@ -367,17 +465,17 @@ static void launch_apply(const ApplyArgs& a, const void* xs, double* y, cudaStre
   const SmemLayout<V> L = SmemLayout<V>::make(a, T);
   auto kern = k_apply<P, F, PH, T>;
   static size_t configured = 0;
-  if (L.total > 48 * 1024 && L.total > configured) {
+  if (L.total > configured) {
     SED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
     configured = L.total;
   }
   SED_REQUIRE(L.total <= 200 * 1024, 5, "operator tables exceed the shared-memory budget");
   int blocks_per_sm = 0;
-  SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, 256, L.total));
+  SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kApplyBS, L.total));
   blocks_per_sm = std::max(blocks_per_sm, 1);
-  const int64_t want = (a.n_orb + 255) / 256;
+  const int64_t want = (a.n_orb + kApplyBS - 1) / kApplyBS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * blocks_per_sm));
-  kern<<<grid, 256, L.total, s>>>(a, L, reinterpret_cast<const V*>(xs), reinterpret_cast<double2*>(y));
+  kern<<<grid, kApplyBS, L.total, s>>>(a, L, reinterpret_cast<const V*>(xs), reinterpret_cast<double2*>(y));
   SED_CUDA(cudaGetLastError());
 }
 
@@ -404,7 +502,7 @@ static void dispatch_apply(const ApplyArgs& a, bool fermi, bool phases, bool tab
 }
 
 static void apply_impl(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s) {
-  const GroupImpl& G = *op.sec->cat->group;
+  const GroupImpl& G = *op.sec->group;
   if (op.sec->cat->n_orbits == 0) return;
   const ApplyArgs a = make_args(op, fp32);
   if (fp32)

@@ -130,6 +130,10 @@ struct CatalogImpl {
 
 struct SectorImpl {
   std::shared_ptr<CatalogImpl> cat;
+  // the group whose per-site phases define this sector (the catalog's group,
+  // or a twisted copy with the same permutations) and its device phases
+  std::shared_ptr<GroupImpl> group;
+  DevBuf phase;
   std::vector<double> chi;  // n_ops * 2
   double atol = 1e-12;
   int64_t dim = 0;
@@ -147,7 +151,15 @@ struct TermTables {
   std::vector<double> amp;         // n_class * 2: distinct amplitudes t
 };
 
-struct ApplyWork;
+// Phase classes of every group element (see sed_rowgather.cuh): mode 0 = no
+// phases, 1 = class tables, 2 = per-site product.
+struct PhaseClassTables {
+  int mode = 0, kp1 = 1;
+  std::vector<uint64_t> mask;  // [G][3]
+  std::vector<double> pw;      // [G][3][k+1] complex
+  std::vector<double> base_k;  // [G] complex: base^k, folded into tchi
+};
+void compute_phase_classes(const GroupImpl& G, int k, PhaseClassTables& pc);
 
 struct OpImpl {
   std::shared_ptr<SectorImpl> sec;
@@ -158,7 +170,8 @@ struct OpImpl {
   std::vector<double> den_v;
   DevBuf site_off, rec;           // term tables
   DevBuf tchi64, tchi32;          // [n_class][n_ops] conj(t_u) * chi(h)
-  DevBuf eta64, eta32;            // [n_ops][n_site] per-site phases (twisted groups)
+  DevBuf cls_mask;                // [n_ops][3] phase-class masks
+  PhaseClassTables pc;
   DevBuf diag;                    // double2[n_orbits] density-density diagonal
   DevBuf xs, ypad, xsec, ysec;    // work vectors for sed_op_apply
   int64_t hops = -1;
@@ -175,7 +188,8 @@ std::shared_ptr<GroupImpl> make_group(int n_site, int n_ops, const int32_t* perm
 std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> g, int n_filled);
 void catalog_readback(const CatalogImpl& c, int field, void* out, int64_t out_bytes);
 void catalog_update_phases(CatalogImpl& c, std::shared_ptr<GroupImpl> g);
-std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> c, const double* chi, double atol);
+std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> c, const double* chi, double atol,
+                                         std::shared_ptr<GroupImpl> g = nullptr);
 void sector_readback(const SectorImpl& s, uint64_t* reps, int32_t* stab, int32_t* orbit);
 void sector_project(const SectorImpl& s, int64_t n, const uint64_t* masks, int64_t* rows, double* coeff);
 std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> s, int n_bil, const int32_t* bil_ij, const double* bil_t,
@@ -196,6 +210,14 @@ struct SolveResult {
 };
 SolveResult solve(OpImpl& op, int nev, double tol, int maxiter, int krylovdim, uint64_t seed, double* evals,
                   double* evecs);
+
+// diagonalize_block_matrixfree's n <= 500 branch: dense block + Hermitian eigen
+SolveResult solve_dense(OpImpl& op, int nev, double* evals, double* evecs);
+static constexpr int64_t kDenseMaxDim = 500;
+// Mixed precision: a polished eigenvalue is accepted when its quadratic error
+// bound |r|^2 / gap is below this fraction of |E| (one tenth of the 1e-9
+// relative accuracy the mixed path promises).
+static constexpr double kMixedRelTarget = 1e-10;
 
 // small dense eigen-solvers (host)
 void eigh_real_sym(int n, std::vector<double>& A, std::vector<double>& w, std::vector<double>& Z);

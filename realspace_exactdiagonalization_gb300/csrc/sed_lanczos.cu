@@ -10,9 +10,10 @@
 // complex128; the projected matrix and its eigen-decomposition stay on the host.
 //
 // Mixed precision (SED_PREC_MIXED): the matvec reads complex64 inputs and
-// accumulates in FP32, everything else stays FP64; once the Ritz residuals
-// reach the FP32 floor, one Rayleigh-Ritz step with FP64 matvecs over
-// span{x_i, H x_i - theta_i x_i} polishes the eigenvalues.
+// accumulates in FP32, everything else stays FP64.  Once the Ritz estimates of
+// the requested pairs fall below 1e-6 |E|, one Rayleigh-Ritz step with FP64
+// matvecs over the nev + 2 Ritz vectors polishes the eigenvalues, and the
+// result is accepted by the quadratic bound |dE| <= |r|^2 / gap (see solve).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -38,12 +39,12 @@ void eigh_real_sym(int n, std::vector<double>& A, std::vector<double>& w, std::v
         tot += v;
         if (i != j) off += v;
       }
-    if (off <= 1e-32 * std::max(tot, 1e-300)) break;
+    if (off <= 1e-29 * std::max(tot, 1e-300)) break;  // rounding level of the off-diagonal part
     for (int p = 0; p < n - 1; ++p)
       for (int q = p + 1; q < n; ++q) {
         const double apq = A[(size_t)p * n + q];
-        if (apq == 0.0) continue;
         const double app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q];
+        if (std::fabs(apq) <= 1e-18 * (std::fabs(app) + std::fabs(aqq)) + 1e-300) continue;
         const double th = (aqq - app) / (2.0 * apq);
         const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
         const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
@@ -93,7 +94,7 @@ void eigh_complex_herm(int n, const std::vector<double>& H, std::vector<double>&
         tot += v;
         if (i != j) off += v;
       }
-    if (off <= 1e-32 * std::max(tot, 1e-300)) break;
+    if (off <= 1e-29 * std::max(tot, 1e-300)) break;  // rounding level of the off-diagonal part
     for (int p = 0; p < n - 1; ++p)
       for (int q = p + 1; q < n; ++q) {
         const double ar = re(A, p, q), ai = im(A, p, q);
@@ -330,6 +331,8 @@ __global__ void k_residual(int64_t n, const double2* __restrict__ a, const doubl
   }
 }
 
+// Davidson correction: w_o <- w_o / (diag_o - theta), the denominator kept
+// at least delta away from zero (diag = density-density diagonal of H).
 // ------------------------------------------------------------- host driver
 namespace {
 
@@ -373,7 +376,7 @@ struct VecOps {
 
 }  // namespace
 
-SolveResult solve(OpImpl& op, int nev, double tol, int maxiter, int krylovdim, uint64_t seed, double* evals,
+SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdim, uint64_t seed, double* evals_out,
                   double* evecs) {
   auto t0 = std::chrono::steady_clock::now();
   SolveResult res;
@@ -381,18 +384,29 @@ SolveResult solve(OpImpl& op, int nev, double tol, int maxiter, int krylovdim, u
   const CatalogImpl& C = *S.cat;
   const int64_t n = C.n_orbits;
   const int64_t D = S.dim;
-  SED_REQUIRE(nev >= 1, 1, "nev must be positive");
+  SED_REQUIRE(nev_out >= 1, 1, "nev must be positive");
   SED_REQUIRE(maxiter >= 1, 1, "maxiter must be positive");
   if (D == 0) return res;
-  nev = (int)std::min<int64_t>(nev, D);
-  SED_REQUIRE(nev <= 32, 5, "nev must be at most 32");
+  nev_out = (int)std::min<int64_t>(nev_out, D);
+  SED_REQUIRE(nev_out <= 32, 5, "nev must be at most 32");
+  if (D <= kDenseMaxDim) {  // SRE:1004-1017: small sectors are solved densely
+    res = solve_dense(op, nev_out, evals_out, evecs);
+    res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return res;
+  }
+  const bool mixed = op.precision == 1;
+  // Mixed precision carries two spare Ritz pairs into the FP64 polish, so a
+  // level nearly degenerate with the first one not requested is still
+  // resolved; convergence is judged on the requested pairs only.
+  int nev = mixed ? (int)std::min<int64_t>(nev_out + 2, D) : nev_out;
+  std::vector<double> evals_v(nev, 0.0);
+  double* evals = evals_v.data();
   if (krylovdim <= 0) krylovdim = 30;
   const int m = (int)std::min<int64_t>(std::max(krylovdim, 2 * nev + 1), std::min<int64_t>(D, 120));
-  const bool mixed = op.precision == 1;
   cudaStream_t s = op.stream;
-  const int nslots = std::max(m + 1, 2 * nev + 2);
+  const int nslots = std::max(m + 1, 3 * nev + 1);
   const int64_t ld = n;
-  DevBuf Vb((size_t)nslots * ld * 16), Wb((size_t)ld * 16), Rb((size_t)std::max(m, 3 * nev) * ld * 16);
+  DevBuf Vb((size_t)nslots * ld * 16), Wb((size_t)ld * 16), Rb((size_t)std::max(m, 5 * nev) * ld * 16);
   DevBuf xs((size_t)ld * 16), xs64((size_t)ld * 16), Sd((size_t)130 * 130 * 16);
   double2* V = Vb.as<double2>();
   double2* W = Wb.as<double2>();
@@ -418,23 +432,40 @@ SolveResult solve(OpImpl& op, int nev, double tol, int maxiter, int krylovdim, u
   int k = 0;
   double beta = 0.0, best_prev[3] = {1e300, 1e300, 1e300};
   double scale = 1.0;
+  double tau = 1e-6;  // mixed: relative Ritz-estimate threshold of the complex64 run
   for (;;) {
     int jend = m;
     for (int j = k; j < m; ++j) {
       op_apply_orbit(op, xs.p, (double*)W, s);
-      // CGS2: two passes of w -= V (V^H w)
-      ops.multidot(V, ld, j + 1, W, 0, false);
-      ops.multiaxpy(V, ld, j + 1, W, 0, -1);
+      // local step: CGS against the two newest basis vectors (they carry the
+      // large alpha_j and beta_{j-1} components), then one full CGS pass
+      // against the whole basis; a second full pass only when the first one
+      // removed more than half of the norm (Daniel-Gragg-Kaufman-Stewart).
+      const int l0 = j > 0 ? j - 1 : 0;
+      ops.multidot(vec(l0), ld, j + 1 - l0, W, 0, false);
+      ops.multiaxpy(vec(l0), ld, j + 1 - l0, W, 0, 5);
       ops.multidot(V, ld, j + 1, W, 128, false);
       ops.multiaxpy(V, ld, j + 1, W, 128, 1);
       ops.check();
-      SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.as<double2>() + j, 16, cudaMemcpyDeviceToHost, s));
+      SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.as<double2>() + (j - l0), 16, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaMemcpyAsync(ops.host + 2, ops.coef.as<double2>() + 128 + j, 16, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaMemcpyAsync(ops.host + 4, ops.scal.as<double>() + 1, 8, cudaMemcpyDeviceToHost, s));
+      SED_CUDA(cudaMemcpyAsync(ops.host + 5, ops.scal.as<double>() + 5, 8, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaStreamSynchronize(s));
       ++res.matvecs;
-      const double alpha = ops.host[0] + ops.host[2];
-      beta = std::sqrt(ops.host[4]);
+      double alpha = ops.host[0] + ops.host[2];
+      double nrm2 = ops.host[4];
+      if (nrm2 < 0.5 * ops.host[5]) {
+        ops.multidot(V, ld, j + 1, W, 128, false);
+        ops.multiaxpy(V, ld, j + 1, W, 128, 1);
+        ops.check();
+        SED_CUDA(cudaMemcpyAsync(ops.host + 2, ops.coef.as<double2>() + 128 + j, 16, cudaMemcpyDeviceToHost, s));
+        SED_CUDA(cudaMemcpyAsync(ops.host + 4, ops.scal.as<double>() + 1, 8, cudaMemcpyDeviceToHost, s));
+        SED_CUDA(cudaStreamSynchronize(s));
+        alpha += ops.host[2];
+        nrm2 = ops.host[4];
+      }
+      beta = std::sqrt(nrm2);
       T[(size_t)j * m + j] = alpha;
       if (j + 1 < m) T[(size_t)j * m + j + 1] = T[(size_t)(j + 1) * m + j] = beta;
       if (!(beta > 1e-13 * std::max(1.0, std::fabs(alpha)))) {
@@ -451,22 +482,27 @@ SolveResult solve(OpImpl& op, int nev, double tol, int maxiter, int krylovdim, u
     const bool invariant = msz < m || msz == D;
     scale = 1.0;
     for (int i = 0; i < std::min(nev, msz); ++i) scale = std::max(scale, std::fabs(theta[i]));
-    const double tol_w = mixed ? std::max(tol, 2e-6 * scale) : tol;
+    const double tol_w = mixed ? std::max(tol, tau * scale) : tol;
     int nconv = 0;
     double maxr = 0.0;
-    for (int i = 0; i < std::min(nev, msz); ++i) {
+    for (int i = 0; i < std::min(nev_out, msz); ++i) {
       const double r = invariant ? 0.0 : std::fabs(beta * Z[(size_t)(msz - 1) * msz + i]);
       maxr = std::max(maxr, r);
       if (r <= tol_w) ++nconv;
     }
     // FP32 matvec noise floor: stop when the residual no longer improves
+    // (only once the residual is near that floor: Lanczos also plateaus for a
+    // few restarts on clustered levels long before it)
     bool stagnated = false;
-    if (mixed && res.restarts >= 6 && maxr < 1e-3 * scale && maxr > 0.7 * best_prev[2]) stagnated = true;
+    if (mixed && res.restarts >= 6 && maxr < 5e-5 * scale && maxr > 0.7 * best_prev[2]) stagnated = true;
     best_prev[2] = best_prev[1];
     best_prev[1] = best_prev[0];
     best_prev[0] = std::min(best_prev[0], maxr);
-    const bool done = (nconv >= nev) || invariant || stagnated || res.restarts >= maxiter;
-    const int keep = done ? std::min(nev, msz) : std::min(msz - 1, std::max(nev + (m - nev) / 2, nev + 1));
+    const bool done = (nconv >= nev_out) || invariant || stagnated || res.restarts >= maxiter;
+    // a mixed-precision candidate keeps the full restart basis, so the
+    // iteration can resume if the FP64 check rejects it
+    const bool final_rot = done && (!mixed || invariant);
+    const int keep = final_rot ? std::min(nev, msz) : std::min(msz - 1, std::max(nev + (m - nev) / 2, nev + 1));
     std::vector<double> Sc((size_t)msz * keep * 2, 0.0);
     for (int l = 0; l < msz; ++l)
       for (int c = 0; c < keep; ++c) Sc[((size_t)l * keep + c) * 2] = Z[(size_t)l * msz + c];
@@ -474,15 +510,104 @@ SolveResult solve(OpImpl& op, int nev, double tol, int maxiter, int krylovdim, u
     k_rotate<<<dim3(gblk, (keep + 7) / 8), kBS, 0, s>>>(n, V, ld, msz, Sd.as<double2>(), keep, R);
     SED_CUDA(cudaMemcpyAsync(V, R, (size_t)keep * ld * 16, cudaMemcpyDeviceToDevice, s));
     ops.check();
-    if (done) {
+    if (!final_rot)  // the last normalised residual direction (slot m) continues the basis
+      SED_CUDA(cudaMemcpyAsync(vec(keep), vec(m), (size_t)ld * 16, cudaMemcpyDeviceToDevice, s));
+    if (done && !mixed) {
       res.converged = nconv;
       res.max_residual = maxr;
-      res.status = (nconv >= nev || invariant || stagnated) ? 0 : 4;
+      res.status = (nconv >= nev_out || invariant || stagnated) ? 0 : 4;
       for (int i = 0; i < keep; ++i) evals[i] = theta[i];
       break;
     }
-    // the last normalised residual direction (slot m) continues the basis
-    SED_CUDA(cudaMemcpyAsync(vec(keep), vec(m), (size_t)ld * 16, cudaMemcpyDeviceToDevice, s));
+    if (done) {
+      // FP64 check of the complex64 candidate: one Rayleigh-Ritz step with
+      // FP64 matvecs over its nev + 2 Ritz vectors B = V[0..nw).  Accepted
+      // when every requested pair meets the residual tolerance or the
+      // quadratic eigenvalue bound |dE| <= |r|^2 / gap is below
+      // kMixedRelTarget |E|, the gap measured to the first Lanczos Ritz value
+      // outside the block; otherwise the Lanczos resumes with a tighter
+      // threshold, and only a stagnated complex64 run falls back to FP64.
+      const int nw = std::min(nev, msz);
+      double2* HB = R;
+      double2* Yr = R + (size_t)nw * ld;
+      double2* HYr = R + (size_t)(2 * nw) * ld;
+      for (int i = 0; i < nw; ++i) {
+        op_scale_to_xs_prec(op, (const double*)(V + (size_t)i * ld), xs64.p, false, s);
+        op_apply_orbit64(op, xs64.p, (double*)(HB + (size_t)i * ld), s);
+        ++res.matvecs64;
+      }
+      std::vector<double> M((size_t)nw * nw * 2), lam, U;
+      for (int bcol = 0; bcol < nw; ++bcol) {
+        ops.multidot(V, ld, nw, HB + (size_t)bcol * ld, 0, false);
+        ops.check();
+        SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.p, (size_t)nw * 16, cudaMemcpyDeviceToHost, s));
+        SED_CUDA(cudaStreamSynchronize(s));
+        for (int a2 = 0; a2 < nw; ++a2) {
+          M[((size_t)a2 * nw + bcol) * 2] = ops.host[2 * a2];
+          M[((size_t)a2 * nw + bcol) * 2 + 1] = ops.host[2 * a2 + 1];
+        }
+      }
+      for (int a2 = 0; a2 < nw; ++a2)  // Hermitian part
+        for (int b2 = a2; b2 < nw; ++b2) {
+          const double r = 0.5 * (M[((size_t)a2 * nw + b2) * 2] + M[((size_t)b2 * nw + a2) * 2]);
+          const double im = 0.5 * (M[((size_t)a2 * nw + b2) * 2 + 1] - M[((size_t)b2 * nw + a2) * 2 + 1]);
+          M[((size_t)a2 * nw + b2) * 2] = r;
+          M[((size_t)a2 * nw + b2) * 2 + 1] = im;
+          M[((size_t)b2 * nw + a2) * 2] = r;
+          M[((size_t)b2 * nw + a2) * 2 + 1] = -im;
+        }
+      eigh_complex_herm(nw, M, lam, U);
+      SED_CUDA(cudaMemcpyAsync(Sd.p, U.data(), U.size() * 8, cudaMemcpyHostToDevice, s));
+      k_rotate<<<dim3(gblk, (nw + 7) / 8), kBS, 0, s>>>(n, V, ld, nw, Sd.as<double2>(), nw, Yr);
+      k_rotate<<<dim3(gblk, (nw + 7) / 8), kBS, 0, s>>>(n, HB, ld, nw, Sd.as<double2>(), nw, HYr);
+      for (int i = 0; i < nev_out; ++i) {
+        k_residual<<<gblk, kBS, 0, s>>>(n, HYr + (size_t)i * ld, Yr + (size_t)i * ld, lam[i], W);
+        ops.norm2(W, 4);
+        SED_CUDA(cudaMemcpyAsync(ops.host + i, ops.scal.as<double>() + 4, 8, cudaMemcpyDeviceToHost, s));
+      }
+      ops.check();
+      SED_CUDA(cudaStreamSynchronize(s));
+      const double thL = msz > nw ? theta[nw] : HUGE_VAL;
+      bool ok = true;
+      double maxr64 = 0.0, maxd = 0.0;
+      for (int i = 0; i < nev_out; ++i) {
+        const double r = std::sqrt(ops.host[i]), gap = thL - lam[i];
+        maxr64 = std::max(maxr64, r);
+        maxd = std::max(maxd, std::fabs(lam[i] - theta[i]));
+        ok = ok && (r <= tol || (gap > 0.0 && r * r <= kMixedRelTarget * std::max(std::fabs(lam[i]), 1e-6 * scale) * gap));
+      }
+      if (ok) {
+        res.converged = nev_out;
+        res.max_residual = maxr64;
+        res.max_delta = maxd;
+        res.status = 0;
+        for (int i = 0; i < nw; ++i) evals[i] = lam[i];
+        SED_CUDA(cudaMemcpyAsync(V, Yr, (size_t)nw * ld * 16, cudaMemcpyDeviceToDevice, s));
+        break;
+      }
+      if (invariant || stagnated || res.restarts >= maxiter || tau <= 1e-9) {
+        // the complex64 run cannot resolve these levels to the target (e.g.
+        // a gap below its noise floor): answer with a full FP64 solve instead
+        // of returning an unconverged pair
+        const int mv32 = res.matvecs, mv64 = res.matvecs64, rs = res.restarts;
+        op.precision = 0;
+        SolveResult r64;
+        try {
+          r64 = solve(op, nev_out, tol, maxiter, krylovdim, seed, evals_out, evecs);
+        } catch (...) {
+          op.precision = 1;
+          throw;
+        }
+        op.precision = 1;
+        r64.matvecs64 += r64.matvecs + mv64;
+        r64.matvecs = mv32;
+        r64.restarts += rs;
+        r64.max_delta = maxd;
+        r64.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return r64;
+      }
+      tau *= 0.1;
+    }
     std::fill(T.begin(), T.end(), 0.0);
     for (int c = 0; c < keep; ++c) {
       T[(size_t)c * m + c] = theta[c];
@@ -493,92 +618,10 @@ SolveResult solve(OpImpl& op, int nev, double tol, int maxiter, int krylovdim, u
     ++res.restarts;
   }
 
-  if (mixed && res.status == 0) {
-    // FP64 Rayleigh-Ritz over B = [Y | Q], Y = Ritz vectors, Q = orthonormal
-    // FP64 residual directions; HB = [H Y | H Q] (slots of R).
-    std::vector<double> th0(evals, evals + nev);
-    double2* Y = V;
-    double2* Q = V + (size_t)nev * ld;
-    double2* HB = R;
-    for (int i = 0; i < nev; ++i) {
-      op_scale_to_xs_prec(op, (const double*)(Y + (size_t)i * ld), xs64.p, false, s);
-      op_apply_orbit64(op, xs64.p, (double*)(HB + (size_t)i * ld), s);
-      ++res.matvecs64;
-    }
-    int q = 0;
-    for (int i = 0; i < nev; ++i) {
-      double2* qv = Q + (size_t)q * ld;
-      k_residual<<<gblk, kBS, 0, s>>>(n, HB + (size_t)i * ld, Y + (size_t)i * ld, th0[i], W);
-      ops.norm2(W, 3);
-      ops.multidot(V, ld, nev + q, W, 0, false);
-      ops.multiaxpy(V, ld, nev + q, W, 0, -1);
-      ops.multidot(V, ld, nev + q, W, 128, false);
-      ops.multiaxpy(V, ld, nev + q, W, 128, 2);
-      ops.check();
-      SED_CUDA(cudaMemcpyAsync(ops.host, ops.scal.as<double>(), 32, cudaMemcpyDeviceToHost, s));
-      SED_CUDA(cudaStreamSynchronize(s));
-      const double r0 = std::sqrt(ops.host[3]), r1 = std::sqrt(ops.host[2]);
-      if (!(r1 > 1e-14 * scale) || !(r1 > 1e-3 * r0)) continue;  // nothing left to add
-      normalize(W, 2, qv, false);
-      op_scale_to_xs_prec(op, (const double*)qv, xs64.p, false, s);
-      op_apply_orbit64(op, xs64.p, (double*)(HB + (size_t)(nev + q) * ld), s);
-      ++res.matvecs64;
-      ++q;
-    }
-    const int nb = nev + q;
-    std::vector<double> M((size_t)nb * nb * 2);
-    for (int b = 0; b < nb; ++b) {
-      ops.multidot(V, ld, nb, HB + (size_t)b * ld, 0, false);
-      ops.check();
-      SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.p, (size_t)nb * 16, cudaMemcpyDeviceToHost, s));
-      SED_CUDA(cudaStreamSynchronize(s));
-      for (int a = 0; a < nb; ++a) {
-        M[((size_t)a * nb + b) * 2] = ops.host[2 * a];
-        M[((size_t)a * nb + b) * 2 + 1] = ops.host[2 * a + 1];
-      }
-    }
-    for (int a = 0; a < nb; ++a)  // Hermitian part
-      for (int b = a; b < nb; ++b) {
-        const double r = 0.5 * (M[((size_t)a * nb + b) * 2] + M[((size_t)b * nb + a) * 2]);
-        const double i = 0.5 * (M[((size_t)a * nb + b) * 2 + 1] - M[((size_t)b * nb + a) * 2 + 1]);
-        M[((size_t)a * nb + b) * 2] = r;
-        M[((size_t)a * nb + b) * 2 + 1] = i;
-        M[((size_t)b * nb + a) * 2] = r;
-        M[((size_t)b * nb + a) * 2 + 1] = -i;
-      }
-    std::vector<double> lam, U;
-    eigh_complex_herm(nb, M, lam, U);
-    std::vector<double> Sc((size_t)nb * nev * 2);
-    for (int l = 0; l < nb; ++l)
-      for (int c = 0; c < nev; ++c) {
-        Sc[((size_t)l * nev + c) * 2] = U[((size_t)l * nb + c) * 2];
-        Sc[((size_t)l * nev + c) * 2 + 1] = U[((size_t)l * nb + c) * 2 + 1];
-      }
-    SED_CUDA(cudaMemcpyAsync(Sd.p, Sc.data(), Sc.size() * 8, cudaMemcpyHostToDevice, s));
-    // refined vectors into R[nb ..) then back into V[0..nev)
-    double2* out = R + (size_t)nb * ld;
-    k_rotate<<<dim3(gblk, (nev + 7) / 8), kBS, 0, s>>>(n, V, ld, nb, Sd.as<double2>(), nev, out);
-    SED_CUDA(cudaMemcpyAsync(V, out, (size_t)nev * ld * 16, cudaMemcpyDeviceToDevice, s));
-    double maxd = 0.0, maxr = 0.0;
-    for (int i = 0; i < nev; ++i) {
-      maxd = std::max(maxd, std::fabs(lam[i] - th0[i]));
-      evals[i] = lam[i];
-      // true FP64 residual of the refined pair
-      op_scale_to_xs_prec(op, (const double*)(V + (size_t)i * ld), xs64.p, false, s);
-      op_apply_orbit64(op, xs64.p, (double*)W, s);
-      ++res.matvecs64;
-      k_residual<<<gblk, kBS, 0, s>>>(n, W, V + (size_t)i * ld, lam[i], W);
-      ops.norm2(W, 4);
-      SED_CUDA(cudaMemcpyAsync(ops.host, ops.scal.as<double>() + 4, 8, cudaMemcpyDeviceToHost, s));
-      SED_CUDA(cudaStreamSynchronize(s));
-      maxr = std::max(maxr, std::sqrt(ops.host[0]));
-    }
-    res.max_delta = maxd;
-    res.max_residual = maxr;
-  }
+  for (int i = 0; i < nev_out; ++i) evals_out[i] = evals[i];
   if (evecs) {
     DevBuf ys((size_t)std::max<int64_t>(D, 1) * 16);
-    for (int i = 0; i < nev; ++i) {
+    for (int i = 0; i < nev_out; ++i) {
       compress_vec(S, (const double*)(V + (size_t)i * ld), ys.as<double>(), s);
       SED_CUDA(cudaMemcpyAsync(evecs + (size_t)i * D * 2, ys.p, (size_t)D * 16, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaStreamSynchronize(s));

@@ -57,6 +57,21 @@ struct HopIter {
   }
 };
 
+// Phase classes of a twisted group element h: its per-site phases take at
+// most kMaxCls + 1 distinct values.  With the most frequent one as base,
+// P_h(new) = base^k * prod_c r_c^popcount(new & mask_c); base^k is folded
+// into tchi, and r_c^n (n = 0..k) is tabulated, so a hop costs kMaxCls
+// popcounts and table reads instead of k complex products.  Unused classes
+// have an empty mask and r^0 = 1.
+static constexpr int kMaxCls = 3;
+template <class V>
+struct PhaseClasses {
+  int mode;             // 0: no phases, 1: class tables, 2: per-site product (eta)
+  int kp1;              // k + 1
+  const uint64_t* mask; // [G][kMaxCls]
+  const V* pw;          // [G][kMaxCls][k+1]
+};
+
 template <class P, bool FERMI, bool PHASES, bool TABLE>
 __device__ __forceinline__ void row_gather(uint64_t m, const typename P::V* __restrict__ xs,
                                            const typename P::V* tab,  // TABLE ? tchi[u][G] : conj(t_u)
@@ -64,7 +79,8 @@ __device__ __forceinline__ void row_gather(uint64_t m, const typename P::V* __re
                                            int N, const uint32_t* s_rank, const RankParams& rp,
                                            const uint32_t* s_rec, const uint16_t* s_off, const uint8_t* s_inv,
                                            const uint64_t* __restrict__ state, typename P::S& ar,
-                                           typename P::S& ai) {
+                                           typename P::S& ai,
+                                           const PhaseClasses<typename P::V>& pc = PhaseClasses<typename P::V>{}) {
   using V = typename P::V;
   using S = typename P::S;
   HopIter it;
@@ -106,15 +122,27 @@ __device__ __forceinline__ void row_gather(uint64_t m, const typename P::V* __re
     if (FERMI) neg ^= __popcll(m & dev::bits_between(i, j)) & 1;
     if (PHASES) {
       S pr = 1, pi = 0;
-      uint64_t b = nw;
-      const V* eh = eta + (size_t)h * N;
-      while (b) {
-        const int q = __ffsll((long long)b) - 1;
-        b &= b - 1;
-        const V e = eh[q];
-        const S nr = pr * e.x - pi * e.y;
-        pi = pr * e.y + pi * e.x;
-        pr = nr;
+      if (pc.mode == 1) {
+        const uint64_t* mk = pc.mask + h * kMaxCls;
+        const V* pw = pc.pw + (size_t)h * kMaxCls * pc.kp1;
+#pragma unroll
+        for (int cl = 0; cl < kMaxCls; ++cl) {
+          const V e = pw[cl * pc.kp1 + __popcll(nw & mk[cl])];
+          const S nr = pr * e.x - pi * e.y;
+          pi = pr * e.y + pi * e.x;
+          pr = nr;
+        }
+      } else if (pc.mode == 2) {
+        uint64_t b = nw;
+        const V* eh = eta + (size_t)h * N;
+        while (b) {
+          const int q = __ffsll((long long)b) - 1;
+          b &= b - 1;
+          const V e = eh[q];
+          const S nr = pr * e.x - pi * e.y;
+          pi = pr * e.y + pi * e.x;
+          pr = nr;
+        }
       }
       cf = P::make(cf.x * pr + cf.y * pi, cf.y * pr - cf.x * pi);  // * conj(P)
     }

@@ -1,0 +1,279 @@
+"""Served ground-state requests with continuous batching.
+
+A request is one sector solve: (model family, momentum, flux twist, nev).  The
+reference answers such streams one sector at a time
+(``ed_scan_at_irrep_matrixfree!``, src/symmetry_resolved_ed.jl:1092-1128, inside
+the loops of ``_ed_scan_sectors!`` :1199-1256 and ``ed_scan!`` :1320-1355).
+Here a scheduler keeps the GPU busy with many requests at once:
+
+* every model family has one device catalog, built once and kept resident;
+  a request only brings its momentum, its twisted group phases and its hop
+  amplitudes;
+* small sectors go to the persistent batched kernel (``sed_batch_run``); two
+  lanes alternate, so requests that arrive while one batch runs start in the
+  next launch as soon as a lane frees, overlapping the batch in flight;
+* large sectors go to device-wide solves (``sed_solve``), several at once on
+  their own streams, each admitted only while the reserved device memory of
+  the solves in flight plus its own footprint stays within the budget;
+* every library call releases the Python GIL, so the lanes and workers drive
+  the GPU concurrently from one process.
+A request's result depends only on its own inputs and seed: the same request
+gives the same eigenvalues alone and in any mix.
+"""
+from __future__ import annotations
+
+import math
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import api as A
+from . import lattice as L
+from .batched import BatchedSectorSolver
+from .groups import statistics_from_name
+
+# sectors whose catalog has at most this many orbits fit the batched kernel's
+# shared-memory vector (complex64, plus the tables)
+SMALL_MAX_ORBITS = 16384
+
+
+@dataclass
+class Family:
+    name: str
+    spec: L.ModelSpec
+    catalog: A.Symmetry_Orbit_Catalog
+    pairs: List[tuple]
+    route: str  # "batch" | "large"
+    solvers: List[BatchedSectorSolver] = field(default_factory=list)
+
+    @property
+    def n_orbits(self) -> int:
+        return self.catalog.n_orbits
+
+
+@dataclass
+class Request:
+    rid: int
+    family: str
+    k_index: int
+    twist: tuple
+    nev: int = 1
+    seed: int = 0
+    arrival: float = 0.0
+    # results
+    evals: Optional[np.ndarray] = None
+    status: int = -1
+    dim: int = -1
+    t_start: float = 0.0
+    t_end: float = 0.0
+    delta_polish: float = 0.0
+    route: str = ""
+
+
+def config5_families() -> Dict[str, L.ModelSpec]:
+    """The served mix: hard-core boson rings (t=1, V=2) at half filling, checkerboard
+    fermions at 1/3 lower-band filling (4x4: Np=5, since 16/3 is not an integer),
+    and spinful Hubbard (t=1, U=8) with N_up = N_down = 5 or 6 as the reference
+    encodes it: a fixed total particle number over 2 L1 L2 modes."""
+    fam = {}
+    for n in (20, 24, 28):
+        fam[f"ring{n}"] = L.ring_xxz(n, 1.0, 2.0)
+    fam["checkerboard3x4"] = L.checkerboard(3, 4, n_filled=4)
+    fam["checkerboard4x4"] = L.checkerboard(4, 4, n_filled=5)
+    for (l1, l2) in ((3, 4), (4, 4)):
+        for nh in (5, 6):
+            fam[f"hubbard{l1}x{l2}_{nh}+{nh}"] = L.hubbard_square(l1, l2, n_filled=2 * nh)
+    return fam
+
+
+def random_requests(families: Dict[str, L.ModelSpec], n: int, rate: float, seed: int = 20261203,
+                    nev: int = 1) -> List[Request]:
+    """A seeded Poisson stream: uniformly drawn (family, momentum, twist),
+    exponential inter-arrival times with the given rate (requests/s)."""
+    rng = np.random.default_rng(seed)
+    names = sorted(families)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate) if rate > 0 else 0.0
+        name = names[rng.integers(len(names))]
+        spec = families[name]
+        nk = spec.lattice.sample_size[0] * spec.lattice.sample_size[1]
+        tw = (float(rng.random()), float(rng.random()) if spec.lattice.sample_size[1] > 1 else 0.0)
+        out.append(Request(i, name, int(rng.integers(nk)), tw, nev, 0x5EED0000 + i, t))
+    return out
+
+
+def solver_footprint(n_orbits: int, nev: int, krylovdim: int = 30) -> int:
+    """Device bytes one device-wide mixed solve holds (Lanczos basis, work
+    vectors, polish basis and operator tables)."""
+    nw = nev + 2
+    m = max(krylovdim, 2 * nw + 1)
+    slots = max(m + 1, 3 * nw + 1) + max(m, 5 * nw) + 4
+    return int(slots * n_orbits * 16 + n_orbits * 17 + (64 << 20))
+
+
+class SectorServer:
+    def __init__(self, families: Dict[str, L.ModelSpec], budget_bytes: float = 160e9, batch_lanes: int = 2,
+                 large_workers: int = 3, max_batch: int = 512, small_max_orbits: int = SMALL_MAX_ORBITS,
+                 precision: str = "mixed", tol: float = 1e-10, nev: int = 1):
+        self.budget = float(budget_bytes)
+        self.precision = precision
+        self.tol = tol
+        self.max_batch = max_batch
+        self.families: Dict[str, Family] = {}
+        self.resident = 0
+        for name, spec in families.items():
+            G = L.build_translation_group(spec.lattice)
+            cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G,
+                                                 particle_statistics=statistics_from_name(spec.statistics))
+            pairs = [(i, j) for (i, j, _) in spec.bilinear_terms()]
+            route = "batch" if cat.n_orbits <= small_max_orbits else "large"
+            fam = Family(name, spec, cat, pairs, route)
+            self.resident += cat.n_states * 8 + cat.n_orbits * 9
+            if route == "batch":
+                for _ in range(batch_lanes):
+                    s = BatchedSectorSolver(cat, pairs, spec.density_terms, precision=precision, nev=nev,
+                                            max_requests=max_batch)
+                    fam.solvers.append(s)
+                    self.resident += s.info()["footprint_bytes"]
+            self.families[name] = fam
+        if self.resident > self.budget:
+            raise MemoryError(f"resident catalogs and batch workspaces ({self.resident / 1e9:.1f} GB) exceed the budget")
+        self.n_lanes = batch_lanes
+        self.n_large = large_workers
+        self._lock = threading.Condition()
+        self._pending_batch: List[Request] = []
+        self._pending_large: List[Request] = []
+        self._reserved = 0.0
+        self._done: List[Request] = []
+        self._closed = False
+        self._t0 = 0.0
+        self._threads: List[threading.Thread] = []
+        self.peak_reserved = 0.0
+
+    # ------------------------------------------------------------ workers
+    def _now(self) -> float:
+        return time.perf_counter() - self._t0
+
+    def _request_arrays(self, fam: Family, reqs: Sequence[Request]):
+        from .batched import SectorRequest
+
+        srs = []
+        for r in reqs:
+            G = L.build_translation_group(fam.spec.lattice, r.twist)
+            irr = L.build_translation_irrep_list(G, fam.spec.lattice)[r.k_index]
+            amps = [t for (_, _, t) in fam.spec.bilinear_terms(r.twist)]
+            srs.append(SectorRequest(irr, G, amps, r.seed))
+        return srs
+
+    def _batch_lane(self, lane: int):
+        while True:
+            with self._lock:
+                while not self._pending_batch and not self._closed:
+                    self._lock.wait()
+                if not self._pending_batch and self._closed:
+                    return
+                fam_name = self._pending_batch[0].family  # oldest request decides the family
+                take = [r for r in self._pending_batch if r.family == fam_name][: self.max_batch]
+                for r in take:
+                    self._pending_batch.remove(r)
+            fam = self.families[fam_name]
+            t_start = self._now()
+            solver = fam.solvers[lane % len(fam.solvers)]
+            out = solver.run(self._request_arrays(fam, take), tol=self.tol)
+            t_end = self._now()
+            with self._lock:
+                for i, r in enumerate(take):
+                    r.evals = out["evals"][i, : r.nev].copy()
+                    r.status = int(out["status"][i])
+                    r.dim = int(out["dims"][i])
+                    r.delta_polish = float(out["delta_polish"][i])
+                    r.t_start, r.t_end, r.route = t_start, t_end, "batch"
+                    self._done.append(r)
+                self._lock.notify_all()
+
+    def _large_worker(self):
+        while True:
+            with self._lock:
+                while True:
+                    if self._pending_large:
+                        r = self._pending_large[0]
+                        need = solver_footprint(self.families[r.family].n_orbits, r.nev)
+                        if self._reserved + need <= self.budget - self.resident or self._reserved == 0:
+                            self._pending_large.pop(0)
+                            self._reserved += need
+                            self.peak_reserved = max(self.peak_reserved, self._reserved)
+                            break
+                    elif self._closed:
+                        return
+                    self._lock.wait()
+            fam = self.families[r.family]
+            t_start = self._now()
+            try:
+                G = L.build_translation_group(fam.spec.lattice, r.twist)
+                irr = L.build_translation_irrep_list(G, fam.spec.lattice)[r.k_index]
+                basis = A.build_symmetry_sector_basis(fam.catalog, irr, group=G)
+                if basis.dim == 0:
+                    vals, status, delta = np.full(r.nev, np.nan), 0, 0.0
+                else:
+                    H = A.MatrixFreeHamiltonian(basis, fam.spec.bilinear_terms(r.twist), fam.spec.density_terms,
+                                                precision=self.precision)
+                    vals, _, info = H.solve(r.nev, tol=self.tol, seed=r.seed, want_vectors=False)
+                    status, delta = 0, info.max_delta_polish
+                    del H
+                r.evals, r.status, r.dim, r.delta_polish = np.asarray(vals), status, basis.dim, delta
+            except A._lib.SEDError as e:  # reported per request, never silently dropped
+                r.status, r.evals = e.code, np.full(r.nev, np.nan)
+            r.t_start, r.t_end, r.route = t_start, self._now(), "large"
+            with self._lock:
+                self._reserved -= need
+                self._done.append(r)
+                self._lock.notify_all()
+
+    # --------------------------------------------------------------- API
+    def start(self):
+        self._t0 = time.perf_counter()
+        self._closed = False
+        self._threads = [threading.Thread(target=self._batch_lane, args=(i,), daemon=True) for i in range(self.n_lanes)]
+        self._threads += [threading.Thread(target=self._large_worker, daemon=True) for _ in range(self.n_large)]
+        for t in self._threads:
+            t.start()
+
+    def submit(self, r: Request) -> None:
+        fam = self.families[r.family]
+        with self._lock:
+            r.arrival = self._now()
+            (self._pending_batch if fam.route == "batch" else self._pending_large).append(r)
+            self._lock.notify_all()
+
+    def close(self) -> List[Request]:
+        with self._lock:
+            self._closed = True
+            self._lock.notify_all()
+        for t in self._threads:
+            t.join()
+        return list(self._done)
+
+    def serve(self, requests: Sequence[Request], time_scale: float = 1.0) -> List[Request]:
+        """Replay a request stream: each request is submitted at its arrival
+        time (scaled), and the call returns when every request is answered."""
+        self.start()
+        for r in sorted(requests, key=lambda q: q.arrival):
+            delay = r.arrival * time_scale - self._now()
+            if delay > 0:
+                time.sleep(delay)
+            self.submit(r)
+        return self.close()
+
+
+def latency_stats(done: Sequence[Request]) -> dict:
+    lat = np.array([r.t_end - r.arrival for r in done])
+    span = max(r.t_end for r in done) - min(r.arrival for r in done)
+    return {"n": len(done), "solves_per_s": len(done) / span if span > 0 else float("nan"),
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "span_s": span}

@@ -24,16 +24,20 @@ def _solver(spec, precision, nev=4, max_requests=256):
                                max_requests=max_requests)
 
 
+@pytest.mark.parametrize("hop_table", [True, False], ids=["table", "on_the_fly"])
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 @pytest.mark.parametrize("model", ["checkerboard3x2_f", "checkerboard3x2_b", "haldane2x4"])
-def test_batch_matches_dense(oracle, model, precision):
+def test_batch_matches_dense(oracle, model, precision, hop_table):
     from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
 
     spec = {"checkerboard3x2_f": lambda: L.checkerboard(3, 2, n_filled=4),
             "checkerboard3x2_b": lambda: L.checkerboard(3, 2, n_filled=4, statistics="bosonic"),
             "haldane2x4": lambda: L.haldane_honeycomb(2, 4)}[model]()
     reqs = flux_scan_requests(spec, TWISTS)
-    out = _solver(spec, precision).run(reqs)
+    solver = _solver(spec, precision)
+    solver.set_hop_table(hop_table)
+    out = solver.run(reqs)
+    assert solver.last_stats()["hop_table"] == hop_table
     assert (out["status"] == 0).all()
     nG = len(reqs) // len(TWISTS)
     for b, r in enumerate(reqs):
@@ -49,18 +53,26 @@ def test_batch_matches_dense(oracle, model, precision):
         np.testing.assert_allclose(out["evals"][b, :k], ref[:k], atol=tol, rtol=0, err_msg=f"{model} {b} {th}")
 
 
-def test_batch_alone_equals_in_mix():
-    """A request's result does not depend on the other requests of the launch."""
+@pytest.mark.parametrize("fresh", [False, True], ids=["same_solver", "fresh_solver"])
+def test_batch_alone_equals_in_mix(fresh):
+    """A request's result is the same alone and in the mix, within the mixed
+    path's 1e-9 relative tolerance: the other requests of a launch change only
+    the hop table's phase-class partition (fresh solver), never the sector or
+    its matrix.  Repeating a launch reproduces it bit for bit."""
     from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
 
     spec = L.haldane_honeycomb(2, 4)
     reqs = flux_scan_requests(spec, TWISTS)
     solver = _solver(spec, "mixed")
     mix = solver.run(reqs)
-    for b in (0, 5, len(reqs) - 1):
-        alone = solver.run([reqs[b]])
-        assert np.array_equal(alone["evals"][0], mix["evals"][b])
+    again = solver.run(reqs)
+    assert np.array_equal(again["evals"], mix["evals"])
+    for b in (0, 5, 9, len(reqs) - 1):
+        alone = (_solver(spec, "mixed") if fresh else solver).run([reqs[b]])
         assert alone["dims"][0] == mix["dims"][b]
+        e0, e1 = alone["evals"][0], mix["evals"][b]
+        ok = ~np.isnan(e1)
+        np.testing.assert_allclose(e0[ok], e1[ok], rtol=1e-9, atol=1e-12)
 
 
 def test_batch_config4_sample_golden():
@@ -75,3 +87,25 @@ def test_batch_config4_sample_golden():
     assert (out["status"] == 0).all()
     assert out["dims"][0] == 11240
     assert abs(out["evals"][0, 0] - (-14.301456146831118)) <= 14.3 * 1e-9
+
+
+def test_hop_table_fermion_flux_matches_on_the_fly():
+    """The hop table carries the Jordan-Wigner / permutation signs and the
+    twist-phase class counts of every hop: spinless fermions under a flux grid
+    give the same spectra through the table as through the on-the-fly
+    matvec (FP64 batch, so both agree to the Lanczos tolerance)."""
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.checkerboard(3, 2, n_filled=4)
+    twists = [(a / 4, b / 4) for a in range(4) for b in range(4)]
+    reqs = flux_scan_requests(spec, twists)
+    s_tab = _solver(spec, "fp64")
+    s_fly = _solver(spec, "fp64")
+    s_fly.set_hop_table(False)
+    a = s_tab.run(reqs)
+    st = s_tab.last_stats()
+    assert st["hop_table"] and st["hop_records"] > 0
+    b = s_fly.run(reqs)
+    assert not s_fly.last_stats()["hop_table"]
+    assert np.array_equal(a["dims"], b["dims"])
+    np.testing.assert_allclose(a["evals"], b["evals"], rtol=0, atol=1e-9)

@@ -89,8 +89,35 @@ def test_matvec_matches_oracle(oracle, name, precision):
             assert np.abs(y - y_tab).max() <= tol * scale, (name, k, precision)
 
 
+def assert_lanczos_spectrum(vals, ref, tol, msg=""):
+    """Lanczos semantics (the reference's KrylovKit branch, n > 500): every
+    returned value is an eigenvalue; the distinct returned values are exactly
+    the lowest distinct eigenvalues (none skipped), each copy at most as often
+    as its multiplicity.  A single-vector Krylov method may return an exactly
+    degenerate level fewer times than its multiplicity."""
+    distinct, mult = [], []
+    for e in ref:
+        if distinct and abs(e - distinct[-1]) <= 1e-8 * max(1.0, abs(e)):
+            mult[-1] += 1
+        else:
+            distinct.append(e)
+            mult.append(1)
+    got = []
+    for v in vals:
+        i = int(np.argmin([abs(v - d) for d in distinct]))
+        assert abs(v - distinct[i]) <= tol, (msg, v, distinct[:6])
+        got.append(i)
+    assert got == sorted(got), msg
+    assert sorted(set(got)) == list(range(len(set(got)))), (msg, got)
+    for i in set(got):
+        assert got.count(i) <= mult[i], (msg, got, mult[:6])
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_eigenvalues_match_dense(oracle, name):
+    """Sectors up to 500 take the reference's dense branch (SRE:1004-1017):
+    exactly the lowest nev eigenvalues with multiplicity.  Larger sectors take
+    Lanczos: see assert_lanczos_spectrum."""
     case = case_by_name(name)
     for k in range(len(case.irreps())):
         _, _, op = oracle_objects(oracle, case, k)
@@ -103,11 +130,15 @@ def test_eigenvalues_match_dense(oracle, name):
         for precision in ("fp64", "mixed"):
             _, _, H = _device(case, k, precision)
             vals, vecs, info = H.solve(nev, tol=1e-10)
-            np.testing.assert_allclose(vals, ref[:nev], atol=1e-9, rtol=0, err_msg=f"{name} k={k} {precision}")
-            # eigenvectors: residual in the sector basis
-            for i in range(nev):
+            tol = 1e-9 * max(1.0, abs(ref[0]))
+            if op.dim <= 500:
+                np.testing.assert_allclose(vals, ref[:nev], atol=tol, rtol=0, err_msg=f"{name} k={k} {precision}")
+            else:
+                assert_lanczos_spectrum(vals, ref, tol, f"{name} k={k} {precision}")
+            for i in range(len(vals)):
                 r = Hd @ vecs[:, i] - vals[i] * vecs[:, i]
-                assert np.linalg.norm(r) < 1e-6, (name, k, precision, i)
+                bound = 1e-7 if (precision == "fp64" or op.dim <= 500) else 1e-4
+                assert np.linalg.norm(r) < bound * max(1.0, abs(vals[i])), (name, k, precision, i)
 
 
 def test_sector_union_equals_full_spectrum(oracle):
