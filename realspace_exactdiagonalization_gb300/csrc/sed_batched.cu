@@ -80,7 +80,7 @@ struct BatchArgs {
 
 struct BatchSmem {
   size_t x, tchi, eta, chi64, T, Z, theta, coef, red, isr, rank, rec, off, inv, perm, misc, pw32, pw64, mask, basek,
-      pwc, total;
+      pwc, zdf, cdf, total;
 };
 
 template <class VT>
@@ -107,7 +107,11 @@ static BatchSmem batch_layout(const BatchArgs& a, bool x_in_smem) {
   L.red = o;
   o = al(o + kNW * 16 * 8);
   L.isr = o;
-  o = al(o + 130 * 8);
+  o = al(o + 130 * 8 + 130 * 4);
+  L.zdf = o;
+  o = al(o + kMaxM * kMaxM * 8);
+  L.cdf = o;
+  o = al(o + (kMaxM + 8) * 16);
   L.misc = o;
   o = al(o + 64 * 8);
   L.rank = o;
@@ -164,6 +168,101 @@ __device__ __forceinline__ double block_sum1(double v, double* red, double* out)
   block_sum<1>(a, red, out);
   return out[0];
 }
+
+// ------------------------------------------------------- double-float vectors
+// GB300 executes FP64 at 1/64 of its FP32 rate, so the batched solver keeps its
+// Lanczos vectors as double-float numbers: a value is the unevaluated sum
+// hi + lo of two floats (48-bit significand, unit roundoff 2^-48 ~ 3.6e-15),
+// and products and sums go through the error-free transformations TwoProd
+// (via FMA) and TwoSum (Knuth 1969; Dekker 1971; Ogita, Rump & Oishi 2005).
+// The recurrence, the reorthogonalisation and the restart rotations thus keep
+// FP64-class accuracy (basis orthogonal to ~1e-14) while running on the FP32
+// pipe.  A complex element is a float4 (re_hi, im_hi, re_lo, im_lo).  The
+// rounding intrinsics keep the compiler from contracting the operations the
+// transformations depend on.
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (h, l) += (xh + xl) (yh + yl), dropping xl yl
+__device__ __forceinline__ void df_mac(float& h, float& l, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  const float pe = __fmaf_rn(xh, yh, -p);
+  float sh, e;
+  df_two_sum(h, p, sh, e);
+  h = sh;
+  l = __fadd_rn(l, __fadd_rn(e, __fmaf_rn(xh, yl, __fmaf_rn(xl, yh, pe))));
+}
+// (h, l) += (h2, l2)
+__device__ __forceinline__ void df_add(float& h, float& l, float h2, float l2) {
+  float sh, e;
+  df_two_sum(h, h2, sh, e);
+  h = sh;
+  l = __fadd_rn(l, __fadd_rn(l2, e));
+}
+__device__ __forceinline__ void df_renorm(float& h, float& l) {
+  const float sh = __fadd_rn(h, l);
+  l = __fsub_rn(l, __fsub_rn(sh, h));
+  h = sh;
+}
+__device__ __forceinline__ double df_to_d(float h, float l) { return (double)h + (double)l; }
+__device__ __forceinline__ void d_to_df(double v, float& h, float& l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
+// Sum 16 double-float values per thread over the block; FP64 results in
+// out[0..16).  Within a warp a reduce-scatter butterfly leaves lane pairs
+// holding one total each (16 adds per lane instead of 80); the 16 warp totals
+// are summed in FP64 in fixed order.
+__device__ __forceinline__ void block_sum_df16(float (&h)[16], float (&l)[16], double* red, double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int st = 16, half = 8; st >= 2; st >>= 1, half >>= 1) {
+    const bool up = (lane & st) != 0;
+#pragma unroll
+    for (int i = 0; i < half; ++i) {
+      const float sh = up ? h[i] : h[i + half], sl = up ? l[i] : l[i + half];
+      const float rh = __shfl_xor_sync(0xFFFFFFFFu, sh, st), rl = __shfl_xor_sync(0xFFFFFFFFu, sl, st);
+      if (up) {
+        h[i] = h[i + half];
+        l[i] = l[i + half];
+      }
+      df_add(h[i], l[i], rh, rl);
+    }
+  }
+  {
+    const float rh = __shfl_xor_sync(0xFFFFFFFFu, h[0], 1), rl = __shfl_xor_sync(0xFFFFFFFFu, l[0], 1);
+    df_add(h[0], l[0], rh, rl);
+  }
+  const int idx = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+  if (!(lane & 1)) red[wid * 16 + idx] = df_to_d(h[0], l[0]);
+  __syncthreads();
+  if (threadIdx.x < 16) {
+    double sum = 0.0;
+    for (int w = 0; w < kNW; ++w) sum += red[w * 16 + threadIdx.x];
+    out[threadIdx.x] = sum;
+  }
+  __syncthreads();
+}
+
+// store one matvec output row: double-float from an FP32 or FP64 accumulator
+__device__ __forceinline__ void store_row(float4* w, int64_t o, float yr, float yi) {
+  w[o] = make_float4(yr, yi, 0.f, 0.f);
+}
+__device__ __forceinline__ void store_row(float4* w, int64_t o, double yr, double yi) {
+  float4 r;
+  d_to_df(yr, r.x, r.z);
+  d_to_df(yi, r.y, r.w);
+  w[o] = r;
+}
+__device__ __forceinline__ void store_row(double2* w, int64_t o, double yr, double yi) { w[o] = make_double2(yr, yi); }
+__device__ __forceinline__ void store_row(double2* w, int64_t o, float yr, float yi) {
+  w[o] = make_double2((double)yr, (double)yi);
+}
+__device__ __forceinline__ void zero_row(float4* w, int64_t o) { w[o] = make_float4(0.f, 0.f, 0.f, 0.f); }
+__device__ __forceinline__ void zero_row(double2* w, int64_t o) { w[o] = make_double2(0.0, 0.0); }
 
 // Jacobi rotation (c, s) for the 2x2 block [[app, apq], [apq, aqq]].  The
 // angle only has to shrink apq, not zero it exactly, so it is computed in
@@ -360,19 +459,17 @@ __device__ __forceinline__ int64_t count_row_hops(uint64_t m, const uint16_t* s_
   return c;
 }
 
-template <class P, bool FERMI, bool PHASES>
-__device__ __forceinline__ double block_matvec(const BatchArgs& a, const typename P::V* x,
-                                               const typename P::V* tchi, const typename P::V* eta,
-                                               const double* s_isr, const uint32_t* s_rank, const uint32_t* s_rec,
-                                               const uint16_t* s_off, const uint8_t* s_inv,
-                                               const uint8_t* __restrict__ rowflag, double2* __restrict__ w,
-                                               const PhaseClasses<typename P::V>& pcl) {
+template <class P, bool FERMI, bool PHASES, class WT>
+__device__ __forceinline__ void block_matvec(const BatchArgs& a, const typename P::V* x, const typename P::V* tchi,
+                                             const typename P::V* eta, const double* s_isr, const float* s_isrf,
+                                             const uint32_t* s_rank, const uint32_t* s_rec, const uint16_t* s_off,
+                                             const uint8_t* s_inv, const uint8_t* __restrict__ rowflag,
+                                             WT* __restrict__ w, const PhaseClasses<typename P::V>& pcl) {
   using V = typename P::V;
   using S = typename P::S;
-  double nrm = 0.0;
   for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
     if (!rowflag[o]) {
-      w[o] = make_double2(0.0, 0.0);
+      zero_row(w, o);
       continue;
     }
     const double2 dg = a.diag[o];
@@ -381,12 +478,9 @@ __device__ __forceinline__ double block_matvec(const BatchArgs& a, const typenam
     S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
     row_gather<P, FERMI, PHASES, true>(a.reps[o], x, tchi, nullptr, a.G, eta, a.N, s_rank, a.rp, s_rec, s_off, s_inv,
                                        a.state, ar, ai, pcl);
-    const double is = s_isr[a.stab[o]];
-    const double2 y = make_double2((double)ar * is, (double)ai * is);
-    w[o] = y;
-    nrm += y.x * y.x + y.y * y.y;
+    const S is = sizeof(S) == 4 ? (S)s_isrf[a.stab[o]] : (S)s_isr[a.stab[o]];
+    store_row(w, o, ar * is, ai * is);
   }
-  return nrm;
 }
 
 // The same matvec through the hop table: one coalesced 8-byte record per hop
@@ -394,11 +488,11 @@ __device__ __forceinline__ double block_matvec(const BatchArgs& a, const typenam
 // the term-group coefficient and the phase-id coefficient from shared memory
 // or L1; the records carry the signs and phase-class counts, so a hop costs
 // no rank lookup, state word or popcount.
-template <class P>
+template <class P, class WT>
 __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typename P::V* x,
                                                  const typename P::V* tchi, const typename P::V* pwc,
-                                                 const double* s_isr, const uint8_t* __restrict__ rowflag,
-                                                 double2* __restrict__ w) {
+                                                 const double* s_isr, const float* s_isrf,
+                                                 const uint8_t* __restrict__ rowflag, WT* __restrict__ w) {
   using V = typename P::V;
   using S = typename P::S;
   const int lane = threadIdx.x & 31;
@@ -421,11 +515,11 @@ __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typen
       ai += cr * xc.y + ci * xc.x;
     }
     if (!rowflag[o]) {
-      w[o] = make_double2(0.0, 0.0);
+      zero_row(w, o);
       continue;
     }
-    const double is = s_isr[a.stab[o]];
-    w[o] = make_double2((double)ar * is, (double)ai * is);
+    const S is = sizeof(S) == 4 ? (S)s_isrf[a.stab[o]] : (S)s_isr[a.stab[o]];
+    store_row(w, o, ar * is, ai * is);
   }
 }
 
@@ -494,6 +588,124 @@ __device__ void block_rotate(const BatchArgs& a, const double2* V, int msz, cons
   }
 }
 
+// coef[l0..l0+nv) = V[0..nv)^H w for double-float vectors, in chunks of 8
+__device__ void df_dots(const BatchArgs& a, const float4* V, int nv, const float4* w, double* red, double2* coef) {
+  for (int l0 = 0; l0 < nv; l0 += 8) {
+    float h[16], l[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) h[c] = l[c] = 0.f;
+    const int cn = min(8, nv - l0);
+    for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+      const float4 x = w[o];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn) {
+          const float4 v = V[(size_t)(l0 + c) * a.ld + o];
+          // conj(v) x = (vr xr + vi xi) + i (vr xi - vi xr)
+          df_mac(h[2 * c], l[2 * c], v.x, v.z, x.x, x.z);
+          df_mac(h[2 * c], l[2 * c], v.y, v.w, x.y, x.w);
+          df_mac(h[2 * c + 1], l[2 * c + 1], v.x, v.z, x.y, x.w);
+          df_mac(h[2 * c + 1], l[2 * c + 1], -v.y, -v.w, x.x, x.z);
+        }
+    }
+    block_sum_df16(h, l, red, reinterpret_cast<double*>(coef + l0));
+  }
+}
+
+// split FP64 coefficients into double-float (one thread each)
+__device__ __forceinline__ void df_coefs(const double2* coef, int nv, float4* cdf) {
+  if (threadIdx.x < nv) {
+    float4 c;
+    d_to_df(coef[threadIdx.x].x, c.x, c.z);
+    d_to_df(coef[threadIdx.x].y, c.y, c.w);
+    cdf[threadIdx.x] = c;
+  }
+  __syncthreads();
+}
+
+// w -= V[0..nv) c (c double-float in shared memory); returns this thread's
+// partial |w|^2 in FP64
+__device__ __forceinline__ double df_axpy(const BatchArgs& a, const float4* V, int nv, const float4* cdf,
+                                          float4* w) {
+  float nh = 0.f, nl = 0.f;
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    float4 x = w[o];
+    for (int q = 0; q < nv; ++q) {
+      const float4 v = V[(size_t)q * a.ld + o];
+      const float4 c = cdf[q];
+      // x -= c v: re -= cr vr - ci vi, im -= cr vi + ci vr
+      df_mac(x.x, x.z, -c.x, -c.z, v.x, v.z);
+      df_mac(x.x, x.z, c.y, c.w, v.y, v.w);
+      df_mac(x.y, x.w, -c.x, -c.z, v.y, v.w);
+      df_mac(x.y, x.w, -c.y, -c.w, v.x, v.z);
+    }
+    df_renorm(x.x, x.z);
+    df_renorm(x.y, x.w);
+    w[o] = x;
+    df_mac(nh, nl, x.x, x.z, x.x, x.z);
+    df_mac(nh, nl, x.y, x.w, x.y, x.w);
+  }
+  return df_to_d(nh, nl);
+}
+
+// v = w * inv (double-float), and the scaled matvec input x = sqrt(stab) v:
+// complex64 from the high parts, or FP64 for the FP64 matvec
+template <class VT>
+__device__ __forceinline__ void df_normalize(const BatchArgs& a, const float4* w, double inv, float4* v, VT* x,
+                                             const float* s_sqrtf, const double* s_sqrt) {
+  float ih, il;
+  d_to_df(inv, ih, il);
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    const float4 y = w[o];
+    float4 r;
+    r.x = __fmul_rn(y.x, ih);
+    r.z = __fmaf_rn(y.x, il, __fmaf_rn(y.z, ih, __fmaf_rn(y.x, ih, -r.x)));
+    r.y = __fmul_rn(y.y, ih);
+    r.w = __fmaf_rn(y.y, il, __fmaf_rn(y.w, ih, __fmaf_rn(y.y, ih, -r.y)));
+    df_renorm(r.x, r.z);
+    df_renorm(r.y, r.w);
+    if (v) v[o] = r;
+    if (x) {
+      if (sizeof(VT) == 8) {
+        const float sq = s_sqrtf[a.stab[o]];
+        reinterpret_cast<float2*>(x)[o] = make_float2(r.x * sq, r.y * sq);
+      } else {
+        const double sq = s_sqrt[a.stab[o]];
+        reinterpret_cast<double2*>(x)[o] = make_double2(df_to_d(r.x, r.z) * sq, df_to_d(r.y, r.w) * sq);
+      }
+    }
+  }
+}
+
+// out[c] = sum_l V[l] Z[l][c] for c < keep, Z real double-float (row stride kMaxM)
+__device__ void df_rotate(const BatchArgs& a, const float4* V, int msz, const float2* Z, int keep, float4* out) {
+  for (int c0 = 0; c0 < keep; c0 += 8) {
+    const int cn = min(8, keep - c0);
+    for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+      float4 acc[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int q = 0; q < msz; ++q) {
+        const float4 v = V[(size_t)q * a.ld + o];
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          if (c < cn) {
+            const float2 z = Z[q * kMaxM + c0 + c];
+            df_mac(acc[c].x, acc[c].z, v.x, v.z, z.x, z.y);
+            df_mac(acc[c].y, acc[c].w, v.y, v.w, z.x, z.y);
+          }
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn) {
+          df_renorm(acc[c].x, acc[c].z);
+          df_renorm(acc[c].y, acc[c].w);
+          out[(size_t)(c0 + c) * a.ld + o] = acc[c];
+        }
+    }
+  }
+}
+
 // out_c = sum_l V[l] S[l][c], complex coefficients (row stride kPolCap)
 __device__ void block_rotate_c(const BatchArgs& a, const double2* V, int nb, const double2* S, int nw, double2* out) {
   for (int c0 = 0; c0 < nw; c0 += 8) {
@@ -552,6 +764,10 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
   double* s_red = reinterpret_cast<double*>(smem + L.red);
   double* s_isr = reinterpret_cast<double*>(smem + L.isr);
   double* s_sqrt = s_isr + 65;
+  float* s_isrf = reinterpret_cast<float*>(s_isr + 130);
+  float* s_sqrtf = s_isrf + 65;
+  float2* s_zdf = reinterpret_cast<float2*>(smem + L.zdf);
+  float4* s_cdf = reinterpret_cast<float4*>(smem + L.cdf);
   double* s_misc = reinterpret_cast<double*>(smem + L.misc);
   uint32_t* s_rank = reinterpret_cast<uint32_t*>(smem + L.rank);
   uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem + L.rec);
@@ -573,13 +789,17 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
   for (int i = threadIdx.x; i < 65; i += blockDim.x) {
     s_isr[i] = i ? 1.0 / sqrt((double)i) : 0.0;
     s_sqrt[i] = sqrt((double)i);
+    s_isrf[i] = (float)s_isr[i];
+    s_sqrtf[i] = (float)s_sqrt[i];
   }
 
   const size_t slots = (size_t)a.m + 1;
   const size_t rslots = (size_t)max(a.m, 5 * (a.nev + 2));
-  double2* Vb = a.V + (size_t)blockIdx.x * slots * a.ld;
-  double2* Rb = a.R + (size_t)blockIdx.x * rslots * a.ld;
-  double2* W = a.W + (size_t)blockIdx.x * a.ld;
+  // Lanczos basis, restart buffer and work vector: double-float complex
+  float4* Vb = reinterpret_cast<float4*>(a.V + (size_t)blockIdx.x * slots * a.ld);
+  float4* Rb = reinterpret_cast<float4*>(a.R + (size_t)blockIdx.x * rslots * a.ld);
+  double2* Rb64 = reinterpret_cast<double2*>(Rb);  // the FP64 polish reuses the restart buffer
+  float4* W = reinterpret_cast<float4*>(a.W + (size_t)blockIdx.x * a.ld);
   double2* X64 = a.X64 + (size_t)blockIdx.x * a.ld;
   double2* tchi64 = a.tchi64 + (size_t)blockIdx.x * a.n_bil * a.G;
   uint8_t* rowflag = a.rowflag + (size_t)blockIdx.x * a.ld;
@@ -775,11 +995,11 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         sincospi(2.0 * u2, &sn, &cs);
         v = make_double2(rr * cs, rr * sn);
       }
-      W[o] = v;
+      store_row(W, o, v.x, v.y);
       nrm += v.x * v.x + v.y * v.y;
     }
     nrm = block_sum1(nrm, s_red, s_misc);
-    block_normalize<V>(a, W, 1.0 / sqrt(nrm), Vb, x, s_sqrt);
+    df_normalize<V>(a, W, 1.0 / sqrt(nrm), Vb, x, s_sqrtf, s_sqrt);
     for (int i = threadIdx.x; i < kMaxM * kMaxM; i += blockDim.x) s_T[i] = 0.0;
     __syncthreads();
 
@@ -790,11 +1010,12 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
     for (;;) {
       int jend = m;
       for (int j = k; j < m; ++j) {
-        double2* vj = Vb + (size_t)j * a.ld;
+        float4* vj = Vb + (size_t)j * a.ld;
         if (a.use_tab)
-          block_matvec_tab<P>(a, x, s_tchi, s_pwc, s_isr, rowflag, W);
+          block_matvec_tab<P>(a, x, s_tchi, s_pwc, s_isr, s_isrf, rowflag, W);
         else
-          block_matvec<P, FERMI, PHASES>(a, x, s_tchi, s_eta, s_isr, s_rank, s_rec, s_off, s_inv, rowflag, W, pcl);
+          block_matvec<P, FERMI, PHASES>(a, x, s_tchi, s_eta, s_isr, s_isrf, s_rank, s_rec, s_off, s_inv, rowflag, W,
+                                         pcl);
         __syncthreads();
         ++nmv;
         // local step: CGS against the two newest basis vectors (they carry
@@ -802,20 +1023,23 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         // a second full pass only when the first removed more than half of
         // the norm (Daniel-Gragg-Kaufman-Stewart).
         const int l0 = j > 0 ? j - 1 : 0;
-        block_dots(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, W, s_red, s_coef);
-        double n0 = block_axpy(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, s_coef, W);
+        df_dots(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, W, s_red, s_coef);
+        df_coefs(s_coef, j + 1 - l0, s_cdf);
+        double n0 = df_axpy(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, s_cdf, W);
         double alpha = s_coef[j - l0].x;
         __syncthreads();
         n0 = block_sum1(n0, s_red, s_misc);
-        block_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
-        double n1 = block_axpy(a, Vb, j + 1, s_coef + kMaxM + 8, W);
+        df_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
+        df_coefs(s_coef + kMaxM + 8, j + 1, s_cdf);
+        double n1 = df_axpy(a, Vb, j + 1, s_cdf, W);
         alpha += s_coef[kMaxM + 8 + j].x;
         __syncthreads();
         n1 = block_sum1(n1, s_red, s_misc + 1);
         double nf = n1;
         if (n1 < 0.5 * n0) {
-          block_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
-          double n2 = block_axpy(a, Vb, j + 1, s_coef + kMaxM + 8, W);
+          df_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
+          df_coefs(s_coef + kMaxM + 8, j + 1, s_cdf);
+          double n2 = df_axpy(a, Vb, j + 1, s_cdf, W);
           alpha += s_coef[kMaxM + 8 + j].x;
           __syncthreads();
           nf = block_sum1(n2, s_red, s_misc + 2);
@@ -829,7 +1053,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           jend = j + 1;
           break;
         }
-        block_normalize<V>(a, W, 1.0 / beta, vj + a.ld, x, s_sqrt);
+        df_normalize<V>(a, W, 1.0 / beta, vj + a.ld, x, s_sqrtf, s_sqrt);
         __syncthreads();
         (void)vj;
       }
@@ -863,7 +1087,14 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       const bool final_rot = done && (!mixed || invariant);
       const int keep = final_rot ? min(nev, msz) : min(msz - 1, max(nev + (m - nev) / 2, nev + 1));
       if (threadIdx.x < keep) s_arrow[threadIdx.x] = beta * s_T[(msz - 1) * kMaxM + threadIdx.x];
-      block_rotate(a, Vb, msz, s_T, keep, Rb);
+      for (int i = threadIdx.x; i < msz * keep; i += blockDim.x) {
+        const int q = i / keep, c = i % keep;
+        float2 z;
+        d_to_df(s_T[q * kMaxM + c], z.x, z.y);
+        s_zdf[q * kMaxM + c] = z;
+      }
+      __syncthreads();
+      df_rotate(a, Vb, msz, s_zdf, keep, Rb);
       __syncthreads();
       for (int c = 0; c < keep; ++c)
         for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
@@ -885,24 +1116,31 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         // the Lanczos resumes with a tighter threshold; a stagnated run is
         // re-solved by the FP64 kernel (status kPolishFailed).
         const int nw = min(nev, msz);
-        double2* HB = Rb;
-        double2* Yr = Rb + (size_t)nw * a.ld;
-        double2* HYr = Rb + (size_t)(2 * nw) * a.ld;
+        double2* HB = Rb64;
+        double2* Yr = Rb64 + (size_t)nw * a.ld;
+        double2* HYr = Rb64 + (size_t)(2 * nw) * a.ld;
+        double2* B64 = Rb64 + (size_t)(3 * nw) * a.ld;  // the Ritz vectors in FP64
+        for (int i = 0; i < nw; ++i)
+          for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+            const float4 v = Vb[(size_t)i * a.ld + o];
+            B64[(size_t)i * a.ld + o] = make_double2(df_to_d(v.x, v.z), df_to_d(v.y, v.w));
+          }
+        __syncthreads();
         double2* M = reinterpret_cast<double2*>(s_Z);  // kPolCap^2 complex fit in kMaxM^2 doubles
         double2* Zc = reinterpret_cast<double2*>(s_T);
         for (int i = 0; i < nw; ++i) {
-          block_normalize<double2>(a, Vb + (size_t)i * a.ld, 1.0, nullptr, X64, s_sqrt);
+          block_normalize<double2>(a, B64 + (size_t)i * a.ld, 1.0, nullptr, X64, s_sqrt);
           __syncthreads();
           if (a.use_tab)
-            block_matvec_tab<P64>(a, X64, tchi64, pwc64, s_isr, rowflag, HB + (size_t)i * a.ld);
+            block_matvec_tab<P64>(a, X64, tchi64, pwc64, s_isr, s_isrf, rowflag, HB + (size_t)i * a.ld);
           else
-            block_matvec<P64, FERMI, PHASES>(a, X64, tchi64, phase, s_isr, s_rank, s_rec, s_off, s_inv, rowflag,
-                                             HB + (size_t)i * a.ld, pcl64);
+            block_matvec<P64, FERMI, PHASES>(a, X64, tchi64, phase, s_isr, s_isrf, s_rank, s_rec, s_off, s_inv,
+                                             rowflag, HB + (size_t)i * a.ld, pcl64);
           __syncthreads();
         }
         n64 += nw;
         for (int bcol = 0; bcol < nw; ++bcol) {
-          block_dots(a, Vb, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
+          block_dots(a, B64, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
           if (threadIdx.x < nw) M[threadIdx.x * kPolCap + bcol] = s_coef[threadIdx.x];
           __syncthreads();
         }
@@ -917,7 +1155,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         __syncthreads();
         if (threadIdx.x < 32) warp_jacobi_herm(nw, M, Zc, s_lam);
         __syncthreads();
-        block_rotate_c(a, Vb, nw, Zc, nw, Yr);
+        block_rotate_c(a, B64, nw, Zc, nw, Yr);
         block_rotate_c(a, HB, nw, Zc, nw, HYr);
         double rr[kMaxNev];
 #pragma unroll
