@@ -295,70 +295,115 @@ __device__ __forceinline__ void unit_phase(double2 a, double* er, double* ei, do
   *r = n2 * inv;
 }
 
-// Warp-parallel cyclic Jacobi for a real symmetric n x n matrix (row stride
-// ld) in shared memory; eigenvalues ascending in w, eigenvectors in Z columns.
-__device__ void warp_jacobi(int n, double* A, double* Z, double* w) {
-  const int lane = threadIdx.x & 31;
-  for (int i = lane; i < n * kMaxM; i += 32) Z[i] = 0.0;
-  __syncwarp();
-  for (int i = lane; i < n; i += 32) Z[i * kMaxM + i] = 1.0;
-  __syncwarp();
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    double off = 0.0, tot = 0.0;
-    for (int e = lane; e < n * n; e += 32) {
+
+// Pair k of step t of the round-robin (circle-method) ordering of np players
+// (np even): over np - 1 steps every pair meets exactly once, and the pairs
+// of one step are disjoint.
+__device__ __forceinline__ void rr_pair(int t, int k, int np, int& p, int& q) {
+  const int m = np - 1;
+  if (k == 0) {
+    p = t;
+    q = m;
+  } else {
+    p = (t + k) % m;
+    q = (t - k + m) % m;
+  }
+  if (p > q) {
+    const int x = p;
+    p = q;
+    q = x;
+  }
+}
+
+// Parallel cyclic Jacobi for a real symmetric n x n matrix A (row stride
+// kMaxM) in shared memory, by the whole block: each step rotates the n/2
+// disjoint pairs of the round-robin ordering at once, so the FP64 row, column
+// and eigenvector updates of a step spread over every warp (and all four SM
+// sub-partitions) instead of one warp.  Eigenvalues ascending in w,
+// eigenvectors in the columns of Z; A is destroyed.  cs holds kMaxM doubles
+// of scratch, out2 two.
+__device__ void block_jacobi(int n, double* A, double* Z, double* w, double* cs, double* red, double* out2) {
+  const int t = threadIdx.x, bd = blockDim.x;
+  const int np = (n + 1) & ~1;  // an odd size gets a dummy player n
+  const int half = np / 2;
+  for (int i = t; i < n * kMaxM; i += bd) Z[i] = 0.0;
+  __syncthreads();
+  for (int i = t; i < n; i += bd) Z[i * kMaxM + i] = 1.0;
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    double sums[2] = {0.0, 0.0};  // off-diagonal and total squared norm
+    for (int e = t; e < n * n; e += bd) {
       const int i = e / n, j = e % n;
       const double v = A[i * kMaxM + j] * A[i * kMaxM + j];
-      tot += v;
-      if (i != j) off += v;
+      sums[1] += v;
+      if (i != j) sums[0] += v;
     }
-    off = warp_allsum(off);
-    tot = warp_allsum(tot);
-    if (off <= 1e-29 * fmax(tot, 1e-300)) break;  // rounding level of the off-diagonal part
-    for (int p = 0; p < n - 1; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double apq = A[p * kMaxM + q];
-        const double app = A[p * kMaxM + p], aqq = A[q * kMaxM + q];
-        if (fabs(apq) <= 1e-18 * (fabs(app) + fabs(aqq)) + 1e-300) continue;
-        double c, s;
-        jacobi_cs(app, aqq, apq, &c, &s);
-        __syncwarp();
-        if (lane < n) {
-          const double akp = A[lane * kMaxM + p], akq = A[lane * kMaxM + q];
-          A[lane * kMaxM + p] = c * akp - s * akq;
-          A[lane * kMaxM + q] = s * akp + c * akq;
+    block_sum<2>(sums, red, out2);
+    if (out2[0] <= 1e-29 * fmax(out2[1], 1e-300)) break;  // rounding level of the off-diagonal part
+    for (int step = 0; step < np - 1; ++step) {
+      if (t < half) {
+        int p, q;
+        rr_pair(step, t, np, p, q);
+        double c = 1.0, sn = 0.0;
+        if (q < n) {
+          const double apq = A[p * kMaxM + q];
+          const double app = A[p * kMaxM + p], aqq = A[q * kMaxM + q];
+          if (!(fabs(apq) <= 1e-18 * (fabs(app) + fabs(aqq)) + 1e-300)) jacobi_cs(app, aqq, apq, &c, &sn);
         }
-        __syncwarp();
-        if (lane < n) {
-          const double apk = A[p * kMaxM + lane], aqk = A[q * kMaxM + lane];
-          A[p * kMaxM + lane] = c * apk - s * aqk;
-          A[q * kMaxM + lane] = s * apk + c * aqk;
-          const double zkp = Z[lane * kMaxM + p], zkq = Z[lane * kMaxM + q];
-          Z[lane * kMaxM + p] = c * zkp - s * zkq;
-          Z[lane * kMaxM + q] = s * zkp + c * zkq;
-        }
-        __syncwarp();
+        cs[2 * t] = c;
+        cs[2 * t + 1] = sn;
       }
-  }
-  __syncwarp();
-  if (lane == 0) {
-    for (int i = 0; i < n; ++i) w[i] = A[i * kMaxM + i];
-    for (int i = 0; i < n; ++i) {  // selection sort with column swaps
-      int b = i;
-      for (int j = i + 1; j < n; ++j)
-        if (w[j] < w[b]) b = j;
-      if (b != i) {
-        const double t = w[i];
-        w[i] = w[b];
-        w[b] = t;
-        for (int r = 0; r < n; ++r) {
-          const double z = Z[r * kMaxM + i];
-          Z[r * kMaxM + i] = Z[r * kMaxM + b];
-          Z[r * kMaxM + b] = z;
-        }
+      __syncthreads();
+      for (int e = t; e < half * n; e += bd) {  // rows p, q of A
+        const int k = e / n, i = e % n;
+        const double c = cs[2 * k], sn = cs[2 * k + 1];
+        if (sn == 0.0) continue;
+        int p, q;
+        rr_pair(step, k, np, p, q);
+        const double apk = A[p * kMaxM + i], aqk = A[q * kMaxM + i];
+        A[p * kMaxM + i] = c * apk - sn * aqk;
+        A[q * kMaxM + i] = sn * apk + c * aqk;
       }
+      __syncthreads();
+      for (int e = t; e < 2 * half * n; e += bd) {  // columns p, q of A and of Z
+        const int which = e >= half * n;
+        const int e2 = which ? e - half * n : e;
+        const int k = e2 / n, i = e2 % n;
+        const double c = cs[2 * k], sn = cs[2 * k + 1];
+        if (sn == 0.0) continue;
+        int p, q;
+        rr_pair(step, k, np, p, q);
+        double* M = which ? Z : A;
+        const double akp = M[i * kMaxM + p], akq = M[i * kMaxM + q];
+        M[i * kMaxM + p] = c * akp - sn * akq;
+        M[i * kMaxM + q] = sn * akp + c * akq;
+      }
+      __syncthreads();
     }
   }
-  __syncwarp();
+  // ascending order: rank every eigenvalue (ties by index), then permute the
+  // eigenvector columns through A
+  int* rank = reinterpret_cast<int*>(cs);
+  if (t < n) {
+    const double wi = A[t * kMaxM + t];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      const double wj = A[j * kMaxM + j];
+      r += (wj < wi) || (wj == wi && j < t);
+    }
+    rank[t] = r;
+    w[r] = wi;
+  }
+  __syncthreads();
+  for (int e = t; e < n * n; e += bd) {
+    const int i = e / n, j = e % n;
+    A[i * kMaxM + rank[j]] = Z[i * kMaxM + j];
+  }
+  __syncthreads();
+  for (int e = t; e < n * n; e += bd) {
+    const int i = e / n, j = e % n;
+    Z[i * kMaxM + j] = A[i * kMaxM + j];
+  }
+  __syncthreads();
 }
 
 __device__ __forceinline__ int64_t global_ns() {
@@ -1063,8 +1108,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       // copy of T in s_Z and leaves the eigenvectors in s_T
       for (int i = threadIdx.x; i < kMaxM * kMaxM; i += blockDim.x) s_Z[i] = s_T[i];
       __syncthreads();
-      if (threadIdx.x < 32) warp_jacobi(msz, s_Z, s_T, s_theta);
-      __syncthreads();
+      block_jacobi(msz, s_Z, s_T, s_theta, reinterpret_cast<double*>(s_coef), s_red, s_misc + 40);
       // now s_T holds eigenvectors (columns), s_Z the diagonalised matrix
       const bool invariant = msz < m || (int64_t)msz == dim;
       double scale = 1.0;
