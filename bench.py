@@ -47,13 +47,26 @@ def workload_requests(grid: int = 8):
     return spec, twists, flux_scan_requests(spec, twists)
 
 
-def config(n_req, extra=None):
+def config(n_req, extra=None, grid=8):
     c = {"workload": WORKLOAD, "model": "haldane_honeycomb_3x4_hardcore_bosons", "n_site": 24, "n_particles": 6,
-         "sectors_per_step": n_req, "momenta": 12, "twist_grid": "8x8", "nev": 4, "tol": 1e-10,
+         "sectors_per_step": n_req, "momenta": 12, "twist_grid": f"{grid}x{grid}", "nev": 4, "tol": 1e-10,
          "l2": "flushed between timed steps (256 MiB write)"}
     if extra:
         c.update(extra)
     return c
+
+
+def profiled_traffic_per_sector():
+    """DRAM bytes (read + write) per sector of one k_batch launch, from the ncu
+    capture summarised in profiles/ (the capture scales with the sector count)."""
+    path = os.path.join(ROOT, "profiles", "k_batch_flux_scan_haldane3x4.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_sector:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
 
 
 # ------------------------------------------------------------------ clocks
@@ -206,7 +219,7 @@ def run_ours(args, rank, world):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    spec, twists, reqs = workload_requests()
+    spec, twists, reqs = workload_requests(args.twist_grid)
     n = len(reqs)
     G0 = reqs[0].group
     cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G0,
@@ -306,9 +319,13 @@ def run_ours(args, rank, world):
                                     spec.density_terms)
         vals, _, info = H.solve(4, tol=1e-10, seed=rq.seed, want_vectors=False)
         plain_ev[b] = vals
-    plain_s = (time.perf_counter() - t0) / n_plain
-    plain_rate = 1.0 / plain_s
-    max_rel_plain = max(float(np.max(np.abs(ev_mixed[b] - plain_ev[b]) / np.abs(plain_ev[b]))) for b in idx)
+    plain = None
+    if n_plain:
+        plain_s = (time.perf_counter() - t0) / n_plain
+        max_rel_plain = max(float(np.max(np.abs(ev_mixed[b] - plain_ev[b]) / np.abs(plain_ev[b]))) for b in idx)
+        plain = {"solves_per_s": 1.0 / plain_s, "sample": n_plain,
+                 "p50_ms": 1e3 * plain_s * (n / 2 + 0.5), "p99_ms": 1e3 * plain_s * (0.99 * n + 1),
+                 "max_rel_dE_mixed_vs_plain": max_rel_plain}
 
     cpu = None
     if not args.no_cpu:
@@ -321,10 +338,12 @@ def run_ours(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64 matvec / f64 Lanczos", "data": "synthetic (generated lattice model, seeded start vectors)",
-        "config": config(n, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
+        "config": config(n, {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"}, args.twist_grid),
         "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_batch (persistent batched Lanczos)",
+                     "traffic": (lambda t: t * n if t else None)(profiled_traffic_per_sector()),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_batch launch "
+                                       "(192-sector capture, scaled by sectors)", "peak_kind": peak_kind, "kernel": "k_batch (persistent batched Lanczos)",
                      "bytes_per_launch": bytes_launch,
                      "note": "algorithmic matvec bytes (D*(8+4+2s)+hops*(4+1+4+s), s=8) of all matvecs of one launch"},
         "cpu_baseline": cpu,
@@ -333,11 +352,9 @@ def run_ours(args, rank, world):
         "gpu_launches": args.steps * (1 + (stats["fp64_fallbacks"] > 0)),
         "fp64_fallbacks_per_step": stats["fp64_fallbacks"],
         "clocks": clocks,
-        "plain_fp64_dropin": {"solves_per_s": plain_rate, "sample": n_plain,
-                              "p50_ms": 1e3 * plain_s * (n / 2 + 0.5), "p99_ms": 1e3 * plain_s * (0.99 * n + 1),
-                              "max_rel_dE_mixed_vs_plain": max_rel_plain},
+        "plain_fp64_dropin": plain,
         "fp64_batched": {"solves_per_s": n / fp64_batch_s},
-        "speedup_vs_plain_fp64": value / plain_rate,
+        "speedup_vs_plain_fp64": value / plain["solves_per_s"] if plain else None,
         "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99))},
         "max_rel_dE_mixed_vs_fp64": max_rel,
         "dims": {"min": int(dims.min()), "max": int(dims.max())},
@@ -488,6 +505,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=6)
     ap.add_argument("--ref-sample", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--twist-grid", type=int, default=8,
+                    help="flux-scan batch: twist grid G (12 G^2 sectors per step; 8 = the 768-sector batch)")
     ap.add_argument("--workload", default="flux_scan", choices=["flux_scan", "large", "served"])
     ap.add_argument("--served-n", type=int, default=300)
     ap.add_argument("--served-rate", type=float, default=50.0)

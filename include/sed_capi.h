@@ -121,6 +121,17 @@ int sed_sector_get(const sed_sector* s, uint64_t* reps, int32_t* stab_order, int
  * orbit is not in the sector), coeff_out[i] = rep_amp * conj(chi(rep_sym)),
  * bit-exact with the reference's evaluation order. */
 int sed_sector_project(const sed_sector* s, int64_t n, const uint64_t* masks, int64_t* row_out, double* coeff_reim);
+/* _expand_sector_state_to_fock_amplitudes (observables/entanglement_spectrum.jl:46-79):
+ * the sector vector c (dim complex128 in sector row order) spread over the
+ * fixed-filling Fock states, amplitudes of one mask summed over the group
+ * elements that reach it, |amp| <= atol dropped and the rest normalised.
+ * fock_reim receives n_states (= the catalog's state count) complex128 in
+ * colex-rank order, i.e. the r-th k-subset in ascending mask order; dropped
+ * states are 0.  is_device_ptr: c and fock are device pointers.  norm2
+ * (nullable) receives the squared norm before normalisation.  Fails with the
+ * reference's "Expanded state has near-zero norm." */
+int sed_sector_expand_fock(const sed_sector* s, const double* c_reim, int64_t dim, double atol, double* fock_reim,
+                           int64_t n_states, int is_device_ptr, double* norm2);
 void sed_sector_destroy(sed_sector* s);
 
 /* --------------------------------------------------------------- operator */

@@ -69,6 +69,8 @@ def lib():
         L.or_sector_get.argtypes = [p, p, p, p]
         L.or_project.restype = i32
         L.or_project.argtypes = [p, u64, i32, p, p]
+        L.or_sector_expand_fock.restype = i32
+        L.or_sector_expand_fock.argtypes = [p, p, dbl, p, p]
         L.or_canonical.argtypes = [p, u64, p, p, p]
         L.or_op_create.restype = p
         L.or_op_create.argtypes = [p, i32, p, p, i32, p, p]
@@ -204,6 +206,16 @@ class Sector:
         orb = np.zeros(n, dtype=np.int32)
         lib().or_sector_get(self.h, _ptr(reps), _ptr(stab), _ptr(orb))
         return reps, stab, orb
+
+    def expand_fock(self, c: np.ndarray, atol: float = 1e-12) -> np.ndarray:
+        """_expand_sector_state_to_fock_amplitudes (observables/entanglement_spectrum.jl:46-79)
+        as a dense complex128 vector over the fixed-filling states in colex-rank order."""
+        c = np.ascontiguousarray(c, dtype=np.complex128)
+        out = np.zeros(self.cat.n_states, dtype=np.complex128)
+        n2 = np.zeros(1)
+        if lib().or_sector_expand_fock(self.h, _ptr(c), atol, _ptr(out), _ptr(n2)) != 0:
+            raise RuntimeError(_err())
+        return out
 
     def project(self, m: int, mode: int = 0):
         row = np.zeros(1, dtype=np.int64)

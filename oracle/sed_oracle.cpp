@@ -28,6 +28,7 @@
 #include <cstring>
 #include <random>
 #include <string>
+#include <unordered_map>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -828,6 +829,63 @@ void or_sector_get(void* s, uint64_t* reps, int32_t* stab, int32_t* orbit) {
   if (stab) std::memcpy(stab, S->stab.data(), S->stab.size() * 4);
   if (orbit) std::memcpy(orbit, S->orbit.data(), S->orbit.size() * 4);
 }
+// observables/entanglement_spectrum.jl:46-79 _expand_sector_state_to_fock_
+// amplitudes: every column's coefficient spread over the group images of its
+// representative, amplitudes of one mask summed in (column, g) order, entries
+// with |amp| <= atol dropped, the rest normalised.  Output: dense complex128
+// over the fixed-filling states in colex-rank order (dropped entries are 0).
+// Returns 1 with the reference's message when the expanded norm vanishes.
+int or_sector_expand_fock(void* s, const double* c_reim, double atol, double* fock_reim, double* norm2_out) {
+  init_binom();
+  Sector* S = (Sector*)s;
+  const Catalog& C = *S->cat;
+  const Group& G = C.G;
+  const int nG = G.n_ops;
+  std::unordered_map<uint64_t, cd> amps;
+  std::vector<uint64_t> order;  // first-insertion order of the masks
+  for (size_t col = 0; col < S->reps.size(); ++col) {
+    const cd coeff{c_reim[2 * col], c_reim[2 * col + 1]};
+    if (std::hypot(coeff.re, coeff.im) <= atol) continue;
+    const double d = std::sqrt((double)(nG * S->stab[col]));
+    const cd pre{coeff.re / d, coeff.im / d};
+    for (int g = 0; g < nG; ++g) {
+      uint64_t shifted;
+      cd phase;
+      apply_op(G, g, S->reps[col], &shifted, &phase);
+      const cd amp = cmul(cmul(pre, cconj(S->chi[g])), phase);
+      auto it = amps.find(shifted);
+      if (it == amps.end()) {
+        amps.emplace(shifted, amp);
+        order.push_back(shifted);
+      } else {
+        it->second = cadd(it->second, amp);
+      }
+    }
+  }
+  double norm2 = 0.0;
+  for (uint64_t m : order) {
+    const cd a = amps[m];
+    if (std::hypot(a.re, a.im) <= atol) {
+      amps.erase(m);
+      continue;
+    }
+    norm2 += a.re * a.re + a.im * a.im;
+  }
+  if (norm2_out) *norm2_out = norm2;
+  if (!(norm2 > atol)) {
+    g_err = "Expanded state has near-zero norm.";
+    return 1;
+  }
+  const double invnorm = 1.0 / std::sqrt(norm2);
+  for (int64_t i = 0; i < C.n_states; ++i) fock_reim[2 * i] = fock_reim[2 * i + 1] = 0.0;
+  for (const auto& kv : amps) {
+    const int64_t r = rank_combination(kv.first);
+    fock_reim[2 * r] = kv.second.re * invnorm;
+    fock_reim[2 * r + 1] = kv.second.im * invnorm;
+  }
+  return 0;
+}
+
 // project a mask: returns 1 and (row, coeff) when in sector; mode 0 = table
 // (project_to_sector), 1 = O(|G|) (project_to_unnormalized_sector).
 int or_project(void* s, uint64_t m, int mode, int64_t* row, double* coeff) {

@@ -24,6 +24,7 @@ __all__ = [
     "Bosonic", "Fermionic", "Symmetry_Operation", "Finite_Symmetry_Group", "OneDim_Irrep", "group_order",
     "build_identity_group", "build_identity_irrep_list", "Real_Space_Second_Quantized_Model",
     "Symmetry_Orbit_Catalog", "build_symmetry_orbit_catalog", "update_orbit_stabilizer_phases_",
+    "expand_sector_state_to_fock", "_expand_sector_state_to_fock_amplitudes", "colex_unrank",
     "Symmetry_Sector_Basis", "build_symmetry_sector_basis", "CanonicalMap", "populate_canonical_map_",
     "MatrixFreeHamiltonian", "apply_hamiltonian_", "hamiltonian_linear_operator", "diagonalize_block_matrixfree",
     "DeviceGroup",
@@ -259,6 +260,50 @@ def build_symmetry_sector_basis(catalog: Symmetry_Orbit_Catalog, irrep: OneDim_I
     if group is not None:
         basis.symmetry_group = group
     return basis
+
+
+def expand_sector_state_to_fock(c: np.ndarray, basis: "Symmetry_Sector_Basis", atol: float = 1e-12) -> np.ndarray:
+    """_expand_sector_state_to_fock_amplitudes (observables/entanglement_spectrum.jl:46-79)
+    on the device, as a dense complex128 vector over the fixed-filling Fock
+    states in colex-rank order (ascending masks); dropped amplitudes are 0."""
+    c = np.ascontiguousarray(c, dtype=np.complex128)
+    if c.shape != (basis.dim,):
+        raise ValueError(f"expected {basis.dim} sector coefficients")
+    out = np.zeros(basis.catalog.n_states, dtype=np.complex128)
+    n2 = C.c_double()
+    check(_lib.load().sed_sector_expand_fock(basis.handle, ptr(c), basis.dim, float(atol), ptr(out),
+                                             basis.catalog.n_states, 0, C.byref(n2)))
+    return out
+
+
+def colex_unrank(ranks: np.ndarray, n_site: int, n_filled: int) -> np.ndarray:
+    """Masks of the given colex ranks (the r-th k-subset in ascending order)."""
+    from math import comb
+
+    r = np.asarray(ranks, dtype=np.int64).copy()
+    m = np.zeros(r.shape, dtype=np.uint64)
+    b = np.full(r.shape, n_site - 1, dtype=np.int64)
+    table = np.array([[comb(n, j) for j in range(n_filled + 1)] for n in range(n_site + 1)], dtype=np.int64)
+    for j in range(n_filled, 0, -1):
+        while True:
+            big = (b >= j) & (table[np.maximum(b, 0), j] > r)
+            if not big.any():
+                break
+            b = np.where(big, b - 1, b)
+        m |= np.left_shift(np.uint64(1), b.astype(np.uint64))
+        r -= table[b, j]
+        b -= 1
+    return m
+
+
+def _expand_sector_state_to_fock_amplitudes(c: np.ndarray, basis: "Symmetry_Sector_Basis",
+                                            particle_statistics=None, atol: float = 1e-12) -> Dict[int, complex]:
+    """The reference's Dict{Mask, ComplexF64} form of expand_sector_state_to_fock."""
+    dense = expand_sector_state_to_fock(c, basis, atol)
+    nz = np.nonzero(dense)[0]
+    g = basis.catalog.symmetry_group
+    masks = colex_unrank(nz, g.n_site, basis.catalog.n_filled)
+    return {int(mk): complex(a) for mk, a in zip(masks, dense[nz])}
 
 
 @dataclass

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <unordered_map>
 
 #include "../../include/sed_capi.h"
@@ -555,9 +556,11 @@ __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typen
       const V t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
       const V ph = pwc[(uint32_t)(r >> 42)];
       const V xc = x[(uint32_t)r & 0xFFFFFFu];
-      const S cr = t.x * ph.x - t.y * ph.y, ci = t.x * ph.y + t.y * ph.x;
-      ar += cr * xc.x - ci * xc.y;
-      ai += cr * xc.y + ci * xc.x;
+      const S cr = P::mad(t.x, ph.x, -t.y * ph.y), ci = P::mad(t.x, ph.y, t.y * ph.x);
+      ar = P::mad(cr, xc.x, ar);
+      ar = P::mad(-ci, xc.y, ar);
+      ai = P::mad(cr, xc.y, ai);
+      ai = P::mad(ci, xc.x, ai);
     }
     if (!rowflag[o]) {
       zero_row(w, o);
@@ -1287,12 +1290,36 @@ struct BatchImpl {
   }
 };
 
+// The shared-memory opt-in is a property of each kernel instantiation,
+// shared by every batch object (and host thread) that launches it: it is only
+// ever raised, and raised-and-launched under one lock, so a concurrent batch
+// with a smaller footprint cannot undercut a launch in progress.
+template <class P, bool F, bool PH, bool XS>
+struct KernelSmem {
+  static std::mutex& mu() {
+    static std::mutex m;
+    return m;
+  }
+  static size_t& configured() {
+    static size_t c = 0;
+    return c;
+  }
+  static void ensure(size_t bytes) {
+    if (bytes > configured()) {
+      SED_CUDA(cudaFuncSetAttribute(k_batch<P, F, PH, XS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      configured() = bytes;
+    }
+  }
+};
+
 template <class P, bool F, bool PH, bool XS>
 static void batch_prepare(BatchImpl& B, const BatchArgs& a, BatchSmem& L, int& ncta) {
   auto kern = k_batch<P, F, PH, XS>;
   L = batch_layout<typename P::V>(a, XS);
   SED_REQUIRE(L.total <= 220 * 1024, 5, "batched solve tables exceed the shared-memory budget (sector too large)");
-  SED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
+  using KS = KernelSmem<P, F, PH, XS>;
+  std::lock_guard<std::mutex> lock(KS::mu());
+  KS::ensure(L.total);
   int per_sm = 0;
   SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBT, L.total));
   SED_REQUIRE(per_sm >= 1, 5, "batched kernel cannot be resident with this shared-memory footprint");
@@ -1301,6 +1328,9 @@ static void batch_prepare(BatchImpl& B, const BatchArgs& a, BatchSmem& L, int& n
 
 template <class P, bool F, bool PH, bool XS>
 static void batch_launch(const BatchArgs& a, const BatchSmem& L, int ncta, cudaStream_t s) {
+  using KS = KernelSmem<P, F, PH, XS>;
+  std::lock_guard<std::mutex> lock(KS::mu());
+  KS::ensure(L.total);
   k_batch<P, F, PH, XS><<<ncta, kBT, L.total, s>>>(a, L);
   SED_CUDA(cudaGetLastError());
 }
@@ -1400,7 +1430,7 @@ __global__ void k_hop_fill(int64_t n_orb, const uint64_t* __restrict__ reps, con
       const uint64_t wd = state[dev::rank_of(nw, rank_tab, rp)];
       int neg = (int)((wd >> 40) & 1);
       if (FERMI) neg ^= __popcll(m & dev::bits_between(from, j)) & 1;
-      const int h = inv[(wd >> 32) & 0xFF];
+      const int h = (int)((wd >> 48) & 0xFF);
       const uint64_t* fm = fmask + 3 * h;
       const uint32_t n1 = __popcll(nw & fm[0]), n2 = __popcll(nw & fm[1]), n3 = __popcll(nw & fm[2]);
       out[base + 32 * (int64_t)k] = (uint64_t)(uint32_t)wd | ((uint64_t)((r >> 8) * G + h) << 24);
@@ -1518,24 +1548,25 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
     k_hop_count<<<grid, 256, 0, s>>>(n, C.reps.as<uint64_t>(), B.site_off.as<uint16_t>(), B.rec.as<uint32_t>(),
                                      cnt.as<int32_t>());
     SED_CUDA(cudaGetLastError());
-    B.row_cnt.resize(n);
-    SED_CUDA(cudaMemcpyAsync(B.row_cnt.data(), cnt.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    std::vector<int32_t> row_cnt(n);
+    SED_CUDA(cudaMemcpyAsync(row_cnt.data(), cnt.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
     SED_CUDA(cudaStreamSynchronize(s));
     std::vector<uint32_t> off(n_sl);
     std::vector<int32_t> w(n_sl);
     int64_t tot = 0;
     for (int64_t sl = 0; sl < n_sl; ++sl) {
       int mx = 0;
-      for (int64_t o = sl * 32; o < std::min(n, sl * 32 + 32); ++o) mx = std::max(mx, B.row_cnt[o]);
+      for (int64_t o = sl * 32; o < std::min(n, sl * 32 + 32); ++o) mx = std::max(mx, row_cnt[o]);
       SED_REQUIRE(tot < (int64_t)UINT32_MAX, 5, "hop table too large");
       off[sl] = (uint32_t)tot;
       w[sl] = mx;
       tot += 32 * (int64_t)mx;
     }
-    B.hop_records = tot;
+    B.hop.alloc((size_t)std::max<int64_t>(tot, 1) * 8);
     upload(B.sl_off, off, s);
     upload(B.sl_w, w, s);
-    B.hop.alloc((size_t)std::max<int64_t>(tot, 1) * 8);
+    B.hop_records = tot;
+    B.row_cnt.swap(row_cnt);  // the slices exist from here on
   }
   upload(B.fmask_dev, fmask, s);
   const int64_t tot = B.hop_records;

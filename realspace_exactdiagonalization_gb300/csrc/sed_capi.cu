@@ -150,6 +150,13 @@ int sed_sector_project(const sed_sector* s, int64_t n, const uint64_t* masks, in
     sed::sector_project(*s->p, n, masks, row_out, coeff_reim);
   });
 }
+int sed_sector_expand_fock(const sed_sector* s, const double* c_reim, int64_t dim, double atol, double* fock_reim,
+                           int64_t n_states, int is_device_ptr, double* norm2) {
+  return guarded([&] {
+    REQ(s, "NULL sector");
+    sed::sector_expand_fock(*s->p, c_reim, dim, atol, fock_reim, n_states, is_device_ptr, norm2);
+  });
+}
 void sed_sector_destroy(sed_sector* s) { delete s; }
 
 int sed_op_create(const sed_sector* s, int n_bil, const int32_t* bil_ij, const double* bil_t_reim, int n_den,

@@ -12,22 +12,26 @@
 #include <cmath>
 #include <cstring>
 
+#include <mutex>
+
 #include "sed_internal.cuh"
 
 namespace sed {
 
 // ------------------------------------------------------------------ binomials
 static int64_t g_binom[65][65];
-static bool g_binom_init = false;
+static std::once_flag g_binom_once;
+// filled exactly once, whichever thread gets here first (the library is
+// called from several host threads at once)
 static void init_binom() {
-  if (g_binom_init) return;
-  for (int n = 0; n <= 64; ++n)
-    for (int k = 0; k <= 64; ++k) g_binom[n][k] = 0;
-  for (int n = 0; n <= 64; ++n) {
-    g_binom[n][0] = 1;
-    for (int k = 1; k <= n; ++k) g_binom[n][k] = g_binom[n - 1][k - 1] + (k <= n - 1 ? g_binom[n - 1][k] : 0);
-  }
-  g_binom_init = true;
+  std::call_once(g_binom_once, [] {
+    for (int n = 0; n <= 64; ++n)
+      for (int k = 0; k <= 64; ++k) g_binom[n][k] = 0;
+    for (int n = 0; n <= 64; ++n) {
+      g_binom[n][0] = 1;
+      for (int k = 1; k <= n; ++k) g_binom[n][k] = g_binom[n - 1][k - 1] + (k <= n - 1 ? g_binom[n - 1][k] : 0);
+    }
+  });
 }
 int64_t binom64(int n, int k) {
   init_binom();
@@ -283,12 +287,14 @@ __global__ void __launch_bounds__(256) k_expand(int64_t n_states, int N, int k, 
                                                 const uint32_t* __restrict__ flags,
                                                 const uint32_t* __restrict__ offs,
                                                 const uint32_t* __restrict__ rank_tab, RankParams rp,
-                                                uint64_t* __restrict__ state, uint64_t* __restrict__ reps,
-                                                uint8_t* __restrict__ stab) {
+                                                const uint8_t* __restrict__ inv, uint64_t* __restrict__ state,
+                                                uint64_t* __restrict__ reps, uint8_t* __restrict__ stab) {
   extern __shared__ uint32_t srank[];
   __shared__ uint8_t sperm[SED_MAX_OPS * 64];
+  __shared__ uint8_t sinv[SED_MAX_OPS];
   for (int i = threadIdx.x; i < rp.total; i += blockDim.x) srank[i] = rank_tab[i];
   for (int i = threadIdx.x; i < G * 64; i += blockDim.x) sperm[i] = perm_g[i];
+  for (int i = threadIdx.x; i < G; i += blockDim.x) sinv[i] = inv[i];
   __syncthreads();
   const int64_t nw = (n_states + 31) / 32;
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
@@ -310,7 +316,8 @@ __global__ void __launch_bounds__(256) k_expand(int64_t n_states, int N, int k, 
         int par = 0;
         const uint64_t img = dev::apply_perm_parity(m, sperm + g * 64, &par);
         const uint32_t idx = dev::rank_of(img, srank, rp);
-        state[idx] = (uint64_t)o | ((uint64_t)g << 32) | ((uint64_t)(fermi ? par : 0) << 40) | ((uint64_t)so << 41);
+        state[idx] = (uint64_t)o | ((uint64_t)g << 32) | ((uint64_t)(fermi ? par : 0) << 40) | ((uint64_t)so << 41) |
+                     ((uint64_t)sinv[g] << 48);
       }
       reps[o] = m;
       stab[o] = (uint8_t)so;
@@ -379,8 +386,9 @@ std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> gp, int n_
   k_expand<<<grid_for(nw, 256), 256, smem, s>>>(n_states, G.n_site, n_filled, G.n_ops, G.stats,
                                                 c->perm_u8.as<uint8_t>(), c->binom.as<uint64_t>(),
                                                 flags.as<uint32_t>(), offs.as<uint32_t>(),
-                                                c->rank.dev.as<uint32_t>(), c->rank.rp, c->state.as<uint64_t>(),
-                                                c->reps.as<uint64_t>(), c->stab.as<uint8_t>());
+                                                c->rank.dev.as<uint32_t>(), c->rank.rp, c->inv_u8.as<uint8_t>(),
+                                                c->state.as<uint64_t>(), c->reps.as<uint64_t>(),
+                                                c->stab.as<uint8_t>());
   SED_CUDA(cudaGetLastError());
   c->stab_host.resize(c->n_orbits);
   if (c->n_orbits)

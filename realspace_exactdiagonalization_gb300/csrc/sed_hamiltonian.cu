@@ -20,6 +20,8 @@
 #include <complex>
 #include <map>
 
+#include <mutex>
+
 #include "sed_internal.cuh"
 #include "sed_rowgather.cuh"
 
@@ -464,12 +466,17 @@ static void launch_apply(const ApplyArgs& a, const void* xs, double* y, cudaStre
   using V = typename P::V;
   const SmemLayout<V> L = SmemLayout<V>::make(a, T);
   auto kern = k_apply<P, F, PH, T>;
+  SED_REQUIRE(L.total <= 200 * 1024, 5, "operator tables exceed the shared-memory budget");
+  // the shared-memory opt-in is a property of the kernel, shared by every
+  // operator: raise it (never lower it) and launch under one lock, so a
+  // concurrent caller with a smaller footprint cannot undercut this launch
+  static std::mutex mu;
   static size_t configured = 0;
+  std::lock_guard<std::mutex> lock(mu);
   if (L.total > configured) {
     SED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
     configured = L.total;
   }
-  SED_REQUIRE(L.total <= 200 * 1024, 5, "operator tables exceed the shared-memory budget");
   int blocks_per_sm = 0;
   SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kApplyBS, L.total));
   blocks_per_sm = std::max(blocks_per_sm, 1);

@@ -9,6 +9,8 @@
 //                               g(rep) = state (SRE:461-466, last write wins)
 //                   bit  40     sign of the fermionic reordering of g on rep
 //                   bits 41..47 stabilizer order of the orbit
+//                   bits 48..55 g^-1 (the element the gather's coefficient
+//                               tables are indexed by)
 //   reps[orbit]   uint64 representative mask (ascending = catalog order)
 //   stab[orbit]   uint8 stabilizer order
 // Sector vectors on the device are indexed by catalog orbit (length n_orbits);
@@ -192,6 +194,8 @@ std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> c, const d
                                          std::shared_ptr<GroupImpl> g = nullptr);
 void sector_readback(const SectorImpl& s, uint64_t* reps, int32_t* stab, int32_t* orbit);
 void sector_project(const SectorImpl& s, int64_t n, const uint64_t* masks, int64_t* rows, double* coeff);
+void sector_expand_fock(const SectorImpl& S, const double* c, int64_t dim, double atol, double* out,
+                        int64_t n_states, int is_device, double* norm2_out);
 std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> s, int n_bil, const int32_t* bil_ij, const double* bil_t,
                                 int n_den, const int32_t* den_ij, const double* den_v, int precision);
 void build_term_tables(const GroupImpl& G, int n_bil, const int32_t* bil_ij, const double* bil_t, TermTables& tt);

@@ -20,11 +20,23 @@ struct P64 {
   using V = double2;
   using S = double;
   __device__ static __forceinline__ V make(S a, S b) { return make_double2(a, b); }
+  __device__ static __forceinline__ S mad(S a, S b, S c) { return fma(a, b, c); }
+  // x or -x by the sign bit alone (integer XOR on the high words, no FP64 op)
+  __device__ static __forceinline__ V flip(V x, int neg) {
+    const long long m = (long long)((unsigned long long)neg << 63);
+    return make_double2(__longlong_as_double(__double_as_longlong(x.x) ^ m),
+                        __longlong_as_double(__double_as_longlong(x.y) ^ m));
+  }
 };
 struct P32 {
   using V = float2;
   using S = float;
   __device__ static __forceinline__ V make(S a, S b) { return make_float2(a, b); }
+  __device__ static __forceinline__ S mad(S a, S b, S c) { return fmaf(a, b, c); }
+  __device__ static __forceinline__ V flip(V x, int neg) {
+    const unsigned m = (unsigned)neg << 31;
+    return make_float2(__uint_as_float(__float_as_uint(x.x) ^ m), __uint_as_float(__float_as_uint(x.y) ^ m));
+  }
 };
 
 // Iterator over the valid hops of one representative.
@@ -107,10 +119,9 @@ __device__ __forceinline__ void row_gather(uint64_t m, const typename P::V* __re
     }
     const int j = rec & 0xFF;
     const uint32_t c = (uint32_t)w;
-    const int g = (int)((w >> 32) & 0xFF);
     int neg = (int)((w >> 40) & 1);
     const V xc = xs[c];
-    const int h = s_inv[g];
+    const int h = (int)((w >> 48) & 0xFF);  // inverse of the state's group element
     const int u = (int)(rec >> 8);
     V cf;
     if (TABLE) {
@@ -146,9 +157,13 @@ __device__ __forceinline__ void row_gather(uint64_t m, const typename P::V* __re
       }
       cf = P::make(cf.x * pr + cf.y * pi, cf.y * pr - cf.x * pi);  // * conj(P)
     }
-    if (neg) cf = P::make(-cf.x, -cf.y);
-    ar += cf.x * xc.x - cf.y * xc.y;
-    ai += cf.x * xc.y + cf.y * xc.x;
+    // (ar, ai) += sign * cf * xc as four fused multiply-adds, the sign
+    // applied to xc's bits
+    const V xq = P::flip(xc, neg);
+    ar = P::mad(cf.x, xq.x, ar);
+    ar = P::mad(-cf.y, xq.y, ar);
+    ai = P::mad(cf.x, xq.y, ai);
+    ai = P::mad(cf.y, xq.x, ai);
   }
 }
 
