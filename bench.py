@@ -409,28 +409,54 @@ def run_large(args):
         xs = torch.randn(n_orb * 2, dtype=torch.float64 if prec == "fp64" else torch.float32, device="cuda")
         y = torch.empty(n_orb * 2, dtype=torch.float64, device="cuda")
         flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-        for _ in range(2):
-            _lib.check(_lib.load().sed_op_apply_orbit(H.handle, C.c_void_p(xs.data_ptr()), C.c_void_p(y.data_ptr())))
-        torch.cuda.synchronize()
-        ms = []
-        for _ in range(args.steps):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            _lib.check(_lib.load().sed_op_apply_orbit(H.handle, C.c_void_p(xs.data_ptr()), C.c_void_p(y.data_ptr())))
-            e1.record(stream)
+
+        def time_matvec():
+            for _ in range(2):
+                _lib.check(_lib.load().sed_op_apply_orbit(H.handle, C.c_void_p(xs.data_ptr()),
+                                                          C.c_void_p(y.data_ptr())))
             torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        t_mv = statistics.median(ms) / 1e3
+            ms = []
+            for _ in range(args.steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                _lib.check(_lib.load().sed_op_apply_orbit(H.handle, C.c_void_p(xs.data_ptr()),
+                                                          C.c_void_p(y.data_ptr())))
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            return statistics.median(ms) / 1e3
+
+        # the matrix-free gather (every hop re-derived from the representative)
+        H.set_hop_table(H.HOP_TABLE_OFF)
+        t_fly = time_matvec()
         b_alg = info["dim"] * (8 + 4 + 2 * s) + info["hops"] * (4 + 1 + 4 + s)
-        r = {"matvec_ms": 1e3 * t_mv, "bytes_alg": b_alg, "achieved_gbs": b_alg / t_mv / 1e9,
-             "frac": b_alg / t_mv / 1e9 / peak, "hops": info["hops"]}
+        r = {"matvec_ms": 1e3 * t_fly, "bytes_alg": b_alg, "achieved_gbs": b_alg / t_fly / 1e9,
+             "frac": b_alg / t_fly / 1e9 / peak, "hops": info["hops"]}
+        # the stored hop table (8 bytes per hop, streamed)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        try:
+            H.set_hop_table(H.HOP_TABLE_NOW)
+            t_build = time.perf_counter() - t0
+            tinfo = H.hop_table_info()
+            t_tab = time_matvec()
+            # bytes the table matvec must move: records, x gathers, row reads and writes
+            b_tab = tinfo["records"] * 8 + info["hops"] * s + info["dim"] * (16 + 4 + 1 + s + 16)
+            r["hop_table"] = {"matvec_ms": 1e3 * t_tab, "build_s": t_build, "table_gb": tinfo["bytes"] / 1e9,
+                              "records": tinfo["records"], "padding": tinfo["records"] / max(info["hops"], 1) - 1,
+                              "achieved_gbs_alg": b_alg / t_tab / 1e9, "frac_alg": b_alg / t_tab / 1e9 / peak,
+                              "table_bytes": b_tab, "achieved_gbs_table": b_tab / t_tab / 1e9,
+                              "frac_table": b_tab / t_tab / 1e9 / peak, "speedup_vs_gather": t_fly / t_tab}
+        except _lib.SEDError as e:
+            r["hop_table"] = {"unavailable": str(e)}
         if not args.no_solve:
             t0 = time.perf_counter()
             vals, _, sinfo = H.solve(3, tol=1e-10, want_vectors=False)
             r.update({"solve_s": time.perf_counter() - t0, "evals": [float(v) for v in vals],
                       "matvecs": sinfo.n_matvec, "matvecs_fp64": sinfo.n_matvec_fp64,
-                      "max_residual": sinfo.max_residual, "delta_polish": sinfo.max_delta_polish})
+                      "max_residual": sinfo.max_residual, "delta_polish": sinfo.max_delta_polish,
+                      "solve_uses_hop_table": H.hop_table_info()["built"]})
         res[prec] = r
         del H
     if "evals" in res.get("fp64", {}) and "evals" in res.get("mixed", {}):

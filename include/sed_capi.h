@@ -154,6 +154,17 @@ int sed_op_apply(sed_op* op, const double* x_reim, double* y_reim, int64_t n, in
 /* dim = sector dimension, n_orbits = length of the orbit-indexed device
  * vectors, hops = valid hops one matvec evaluates (counted on the device). */
 int sed_op_info(const sed_op* op, int64_t* dim, int64_t* n_orbits, int64_t* hops);
+/* The operator's hop table: the sector matvec stored as 8 bytes per hop
+ * (column orbit + coefficient index, SELL-32 slices), the compressed form of
+ * the reference's projection table (build_matrixfree_projection_table,
+ * SRE:680-728, streamed by _apply_table!, SRE:731-765).  mode 1 (default)
+ * builds it at the first sed_solve when it fits 35 % of the free device memory;
+ * 2 builds it now (SED_ERR_ARG when it cannot: memory budget, field widths, or
+ * a twist whose phases take more than four values per group element); 0 drops
+ * it and keeps the on-the-fly gather.  Every later sed_op_apply / sed_solve
+ * uses it; results agree with the on-the-fly gather to rounding. */
+int sed_op_set_hop_table(sed_op* op, int mode);
+int sed_op_hop_table_info(const sed_op* op, int32_t* built, int64_t* records, int64_t* bytes);
 int sed_op_set_stream(sed_op* op, void* cuda_stream);
 /* Orbit-indexed matvec for benchmarking the kernel alone: xs_dev holds
  * sqrt(stab)*x in the op's precision (complex64 or complex128, length

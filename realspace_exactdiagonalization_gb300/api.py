@@ -373,6 +373,18 @@ class MatrixFreeHamiltonian(_Handle):
         check(_lib.load().sed_op_info(self._h, C.byref(d), C.byref(no), C.byref(hops)))
         return {"dim": d.value, "n_orbits": no.value, "hops": hops.value}
 
+    HOP_TABLE_OFF, HOP_TABLE_AUTO, HOP_TABLE_NOW = 0, 1, 2
+
+    def set_hop_table(self, mode: int) -> None:
+        """The stored form of this operator's matvec (8 bytes per hop): 0 off,
+        1 built at the first solve when it fits (default), 2 built now."""
+        check(_lib.load().sed_op_set_hop_table(self._h, int(mode)))
+
+    def hop_table_info(self) -> dict:
+        built, rec, nb = C.c_int32(), C.c_int64(), C.c_int64()
+        check(_lib.load().sed_op_hop_table_info(self._h, C.byref(built), C.byref(rec), C.byref(nb)))
+        return {"built": bool(built.value), "records": rec.value, "bytes": nb.value}
+
     def solve(self, nev: int, tol: float = 1e-10, maxiter: int = 300, krylovdim: int = 30, seed: int = 0x5EED0000,
               want_vectors: bool = True):
         ev = np.zeros(max(nev, 1), dtype=np.float64)

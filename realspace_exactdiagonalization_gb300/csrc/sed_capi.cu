@@ -191,6 +191,30 @@ int sed_op_info(const sed_op* op, int64_t* dim, int64_t* n_orbits, int64_t* hops
     if (hops) *hops = sed::op_count_hops(*op->p);
   });
 }
+int sed_op_set_hop_table(sed_op* op, int mode) {
+  return guarded([&] {
+    REQ(op, "NULL operator");
+    REQ(mode >= 0 && mode <= 2, "mode must be 0 (off), 1 (at the first solve) or 2 (now)");
+    sed::OpImpl& o = *op->p;
+    o.tab_mode = mode;
+    o.tab_refused = false;
+    if (mode == 0) sed::op_drop_table(o);
+    if (mode == 2 && !o.tab_built) {
+      REQ(sed::op_build_table(o), "the hop table does not fit (memory budget, field widths or twist classes)");
+    }
+  });
+}
+int sed_op_hop_table_info(const sed_op* op, int32_t* built, int64_t* records, int64_t* bytes) {
+  return guarded([&] {
+    REQ(op, "NULL operator");
+    const sed::OpImpl& o = *op->p;
+    if (built) *built = o.tab_built ? 1 : 0;
+    if (records) *records = o.tab_records;
+    if (bytes) *bytes = o.tab_built ? (int64_t)(o.tab_hop.bytes + o.tab_off.bytes + o.tab_w.bytes + o.tab_coef64.bytes +
+                                                o.tab_coef32.bytes)
+                                    : 0;
+  });
+}
 int sed_op_set_stream(sed_op* op, void* stream) {
   return guarded([&] {
     REQ(op, "NULL operator");

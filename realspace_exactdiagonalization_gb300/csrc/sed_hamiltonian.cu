@@ -511,6 +511,10 @@ static void dispatch_apply(const ApplyArgs& a, bool fermi, bool phases, bool tab
 static void apply_impl(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s) {
   const GroupImpl& G = *op.sec->group;
   if (op.sec->cat->n_orbits == 0) return;
+  if (op.tab_built) {  // the stored form of the same matvec (sed_optable.cu)
+    apply_table(op, fp32, xs, ypad, s);
+    return;
+  }
   const ApplyArgs a = make_args(op, fp32);
   if (fp32)
     dispatch_apply<P32>(a, G.stats == 1, G.has_phases, op.tchi_in_smem, xs, ypad, s);

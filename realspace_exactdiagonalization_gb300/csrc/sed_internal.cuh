@@ -181,8 +181,17 @@ struct OpImpl {
   bool own_stream = false;
   size_t smem_bytes = 0;
   bool tchi_in_smem = true;
+  // hop table (sed_optable.cu): 0 off, 1 built at the first solve when it
+  // fits the memory budget, 2 requested now
+  int tab_mode = 1;
+  bool tab_built = false, tab_refused = false;
+  DevBuf tab_hop, tab_off, tab_w, tab_coef64, tab_coef32;
+  int64_t tab_records = 0, tab_coefs = 0;
   ~OpImpl();
 };
+bool op_build_table(OpImpl& op);
+void op_drop_table(OpImpl& op);
+void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s);
 
 // ----------------------------------------------------------- entry points
 std::shared_ptr<GroupImpl> make_group(int n_site, int n_ops, const int32_t* perm, const double* phase, int identity,

@@ -394,6 +394,9 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
     res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return res;
   }
+  // a solve applies the operator hundreds of times: stream it from the hop
+  // table when that fits (sed_optable.cu)
+  if (op.tab_mode == 1 && !op.tab_built && !op.tab_refused) op.tab_refused = !op_build_table(op);
   const bool mixed = op.precision == 1;
   // Mixed precision carries two spare Ritz pairs into the FP64 polish, so a
   // level nearly degenerate with the first one not requested is still
