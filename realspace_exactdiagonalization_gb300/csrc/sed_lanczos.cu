@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "sed_dfloat.cuh"
 #include "sed_internal.cuh"
 
 namespace sed {
@@ -283,13 +284,16 @@ __global__ void __launch_bounds__(kBS) k_multiaxpy(int64_t n, const double2* __r
 template <class V>
 __global__ void k_normalize(int64_t n, const double2* __restrict__ w, const double* __restrict__ nrm2,
                             double2* __restrict__ v, const uint8_t* __restrict__ stab, V* __restrict__ xs) {
+  __shared__ double s_sq[65];
+  for (int i = threadIdx.x; i < 65; i += blockDim.x) s_sq[i] = sqrt((double)i);
+  __syncthreads();
   const double inv = 1.0 / sqrt(*nrm2);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double2 x = w[i];
     const double2 y = make_double2(x.x * inv, x.y * inv);
     v[i] = y;
     if (xs) {
-      const double sq = sqrt((double)stab[i]);
+      const double sq = s_sq[stab[i]];
       xs[i].x = y.x * sq;
       xs[i].y = y.y * sq;
     }
@@ -333,6 +337,179 @@ __global__ void k_residual(int64_t n, const double2* __restrict__ a, const doubl
 
 // Davidson correction: w_o <- w_o / (diag_o - theta), the denominator kept
 // at least delta away from zero (diag = density-density diagonal of H).
+// ------------------------------------------------ double-float basis (mixed)
+// The mixed-precision solve keeps its Lanczos basis, work vector and restart
+// buffer as double-float complex (float4 per element, sed_dfloat.cuh): the
+// recurrence, the reorthogonalisation and the restart rotations keep
+// FP64-class accuracy on the FP32 pipe instead of GB300's 1/64-rate FP64
+// pipe, in the same 16 bytes per element.  The complex64 matvec writes FP64,
+// converted in place; the FP64 polish reads FP64 copies of the Ritz vectors.
+
+// w (FP64 complex) -> double-float, in place
+__global__ void k_df_from_d(int64_t n, double2* __restrict__ w) {
+  float4* out = reinterpret_cast<float4*>(w);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 x = w[i];
+    float4 r;
+    d_to_df(x.x, r.x, r.z);
+    d_to_df(x.y, r.y, r.w);
+    out[i] = r;
+  }
+}
+
+__global__ void k_df_to_d(int64_t n, const float4* __restrict__ v, double2* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 x = v[i];
+    out[i] = make_double2(df_to_d(x.x, x.z), df_to_d(x.y, x.w));
+  }
+}
+
+__global__ void __launch_bounds__(kBS) k_df_norm2_part(int64_t n, const float4* __restrict__ v,
+                                                       double* __restrict__ part) {
+  float h = 0.f, l = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 x = v[i];
+    df_mac(h, l, x.x, x.z, x.x, x.z);
+    df_mac(h, l, x.y, x.w, x.y, x.w);
+  }
+  const double2 r = block_sum2(df_to_d(h, l), 0.0);
+  if (threadIdx.x == 0) part[blockIdx.x] = r.x;
+}
+
+// part[l*nblk + b] = block b's share of conj(V_l) w for the 8 vectors of
+// chunk blockIdx.y: w is read once per 8 basis vectors
+__global__ void __launch_bounds__(kBS) k_df_multidot(int64_t n, const float4* __restrict__ V, int64_t ld, int nv,
+                                                     const float4* __restrict__ w, double2* __restrict__ part) {
+  const int l0 = blockIdx.y * 8;
+  const int cn = min(8, nv - l0);
+  float h[16], lo[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) h[c] = lo[c] = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 x = w[i];
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (c < cn) {
+        const float4 v = V[(size_t)(l0 + c) * ld + i];
+        df_mac(h[2 * c], lo[2 * c], v.x, v.z, x.x, x.z);
+        df_mac(h[2 * c], lo[2 * c], v.y, v.w, x.y, x.w);
+        df_mac(h[2 * c + 1], lo[2 * c + 1], v.x, v.z, x.y, x.w);
+        df_mac(h[2 * c + 1], lo[2 * c + 1], -v.y, -v.w, x.x, x.z);
+      }
+  }
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    if (c < cn) {
+      const double2 r = block_sum2(df_to_d(h[2 * c], lo[2 * c]), df_to_d(h[2 * c + 1], lo[2 * c + 1]));
+      if (threadIdx.x == 0) part[(size_t)(l0 + c) * gridDim.x + blockIdx.x] = r;
+    }
+}
+
+// w -= sum_l c_l V_l (double-float), optionally the block partial of |w|^2
+__global__ void __launch_bounds__(kBS) k_df_multiaxpy(int64_t n, const float4* __restrict__ V, int64_t ld, int nv,
+                                                      const double2* __restrict__ c, float4* __restrict__ w,
+                                                      double* __restrict__ norm_part) {
+  __shared__ float4 sc[128];
+  for (int l = threadIdx.x; l < nv; l += blockDim.x) {
+    float4 t;
+    d_to_df(c[l].x, t.x, t.z);
+    d_to_df(c[l].y, t.y, t.w);
+    sc[l] = t;
+  }
+  __syncthreads();
+  float nh = 0.f, nl = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float4 x = w[i];
+    for (int l = 0; l < nv; ++l) {
+      const float4 v = V[(size_t)l * ld + i];
+      const float4 cc = sc[l];
+      df_mac(x.x, x.z, -cc.x, -cc.z, v.x, v.z);
+      df_mac(x.x, x.z, cc.y, cc.w, v.y, v.w);
+      df_mac(x.y, x.w, -cc.x, -cc.z, v.y, v.w);
+      df_mac(x.y, x.w, -cc.y, -cc.w, v.x, v.z);
+    }
+    df_renorm(x.x, x.z);
+    df_renorm(x.y, x.w);
+    w[i] = x;
+    df_mac(nh, nl, x.x, x.z, x.x, x.z);
+    df_mac(nh, nl, x.y, x.w, x.y, x.w);
+  }
+  if (norm_part) {
+    const double2 r = block_sum2(df_to_d(nh, nl), 0.0);
+    if (threadIdx.x == 0) norm_part[blockIdx.x] = r.x;
+  }
+}
+
+// v = w / sqrt(nrm2) (double-float); xs = sqrt(stab) v in complex64
+__global__ void k_df_normalize(int64_t n, const float4* __restrict__ w, const double* __restrict__ nrm2,
+                               float4* __restrict__ v, const uint8_t* __restrict__ stab, float2* __restrict__ xs) {
+  __shared__ float s_sq[65];
+  __shared__ float s_inv[2];
+  for (int i = threadIdx.x; i < 65; i += blockDim.x) s_sq[i] = (float)sqrt((double)i);
+  if (threadIdx.x == 0) d_to_df(1.0 / sqrt(*nrm2), s_inv[0], s_inv[1]);
+  __syncthreads();
+  const float ih = s_inv[0], il = s_inv[1];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 y = w[i];
+    float4 r;
+    r.x = __fmul_rn(y.x, ih);
+    r.z = __fmaf_rn(y.x, il, __fmaf_rn(y.z, ih, __fmaf_rn(y.x, ih, -r.x)));
+    r.y = __fmul_rn(y.y, ih);
+    r.w = __fmaf_rn(y.y, il, __fmaf_rn(y.w, ih, __fmaf_rn(y.y, ih, -r.y)));
+    df_renorm(r.x, r.z);
+    df_renorm(r.y, r.w);
+    if (v) v[i] = r;
+    if (xs) {
+      const float sq = s_sq[stab[i]];
+      xs[i] = make_float2(r.x * sq, r.y * sq);
+    }
+  }
+}
+
+// out_c = sum_l V_l S[l][c] for c in [c0, c0+8): complex FP64 coefficients
+// (row stride keep) split to double-float in shared memory
+__global__ void __launch_bounds__(kBS) k_df_rotate(int64_t n, const float4* __restrict__ V, int64_t ld, int msz,
+                                                   const double2* __restrict__ S, int keep, float4* __restrict__ out) {
+  __shared__ float4 sS[121 * 8];
+  const int c0 = blockIdx.y * 8;
+  const int cn = min(8, keep - c0);
+  for (int idx = threadIdx.x; idx < msz * 8; idx += blockDim.x) {
+    const int l = idx >> 3, c = idx & 7;
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (c < cn) {
+      const double2 v = S[(size_t)l * keep + c0 + c];
+      d_to_df(v.x, t.x, t.z);
+      d_to_df(v.y, t.y, t.w);
+    }
+    sS[idx] = t;
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float4 acc[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int l = 0; l < msz; ++l) {
+      const float4 v = V[(size_t)l * ld + i];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn) {
+          const float4 t = sS[l * 8 + c];
+          df_mac(acc[c].x, acc[c].z, v.x, v.z, t.x, t.z);
+          df_mac(acc[c].x, acc[c].z, -v.y, -v.w, t.y, t.w);
+          df_mac(acc[c].y, acc[c].w, v.x, v.z, t.y, t.w);
+          df_mac(acc[c].y, acc[c].w, v.y, v.w, t.x, t.z);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (c < cn) {
+        df_renorm(acc[c].x, acc[c].z);
+        df_renorm(acc[c].y, acc[c].w);
+        out[(size_t)(c0 + c) * ld + i] = acc[c];
+      }
+  }
+}
+
 // ------------------------------------------------------------- host driver
 namespace {
 
@@ -342,7 +519,8 @@ struct VecOps {
   cudaStream_t s;
   DevBuf part, part1, coef, scal;  // partial sums, coefficients, scalars
   double* host = nullptr;          // pinned scratch
-  explicit VecOps(int64_t n_, cudaStream_t s_) : n(n_), s(s_) {
+  bool df = false;                 // vectors are double-float (mixed precision)
+  VecOps(int64_t n_, cudaStream_t s_, bool df_) : n(n_), s(s_), df(df_) {
     const int64_t sms = device_sm_count();
     nblk = (int)std::max<int64_t>(1, std::min<int64_t>((n + kBS * 4 - 1) / (kBS * 4), sms * 4));
     part.alloc((size_t)nblk * 130 * 16);
@@ -354,21 +532,35 @@ struct VecOps {
   ~VecOps() {
     if (host) cudaFreeHost(host);
   }
-  // scal[slot] = |v|^2
-  void norm2(const double2* v, int slot) {
-    k_norm2_part<<<nblk, kBS, 0, s>>>(n, v, part1.as<double>());
+  // scal[slot] = |v|^2 (fp64: the vector is FP64 whatever the basis format)
+  void norm2(const double2* v, int slot, bool fp64 = false) {
+    if (df && !fp64)
+      k_df_norm2_part<<<nblk, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(v), part1.as<double>());
+    else
+      k_norm2_part<<<nblk, kBS, 0, s>>>(n, v, part1.as<double>());
     k_reduce_part1<<<1, kBS, 0, s>>>(part1.as<double>(), nblk, scal.as<double>() + slot);
   }
   // coef[off .. off+nv) (=|+=) V[0..nv)^H w
-  void multidot(const double2* V, int64_t ld, int nv, const double2* w, int off, bool acc) {
-    dim3 g(nblk, nv);
-    k_multidot<<<g, kBS, 0, s>>>(n, V, ld, w, part.as<double2>());
+  void multidot(const double2* V, int64_t ld, int nv, const double2* w, int off, bool acc, bool fp64 = false) {
+    if (df && !fp64) {
+      dim3 g(nblk, (nv + 7) / 8);
+      k_df_multidot<<<g, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(V), ld, nv,
+                                       reinterpret_cast<const float4*>(w), part.as<double2>());
+    } else {
+      dim3 g(nblk, nv);
+      k_multidot<<<g, kBS, 0, s>>>(n, V, ld, w, part.as<double2>());
+    }
     k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), nblk, coef.as<double2>() + off, acc ? 1 : 0);
   }
   // w -= V[0..nv) coef[off..], optionally scal[slot] = |w|^2
-  void multiaxpy(const double2* V, int64_t ld, int nv, double2* w, int off, int norm_slot) {
-    k_multiaxpy<<<nblk, kBS, 0, s>>>(n, V, ld, nv, coef.as<double2>() + off, w,
-                                     norm_slot >= 0 ? part1.as<double>() : nullptr);
+  void multiaxpy(const double2* V, int64_t ld, int nv, double2* w, int off, int norm_slot, bool fp64 = false) {
+    if (df && !fp64)
+      k_df_multiaxpy<<<nblk, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(V), ld, nv, coef.as<double2>() + off,
+                                          reinterpret_cast<float4*>(w),
+                                          norm_slot >= 0 ? part1.as<double>() : nullptr);
+    else
+      k_multiaxpy<<<nblk, kBS, 0, s>>>(n, V, ld, nv, coef.as<double2>() + off, w,
+                                       norm_slot >= 0 ? part1.as<double>() : nullptr);
     if (norm_slot >= 0) k_reduce_part1<<<1, kBS, 0, s>>>(part1.as<double>(), nblk, scal.as<double>() + norm_slot);
   }
   void check() { SED_CUDA(cudaGetLastError()); }
@@ -414,19 +606,21 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
   double2* V = Vb.as<double2>();
   double2* W = Wb.as<double2>();
   double2* R = Rb.as<double2>();
-  VecOps ops(n, s);
+  VecOps ops(n, s, mixed);
   auto vec = [&](int j) { return V + (size_t)j * ld; };
   const int gblk = ops.nblk;
   auto normalize = [&](const double2* w, int slot, double2* out, bool to_xs) {
     if (mixed)
-      k_normalize<float2><<<gblk, kBS, 0, s>>>(n, w, ops.scal.as<double>() + slot, out, C.stab.as<uint8_t>(),
-                                               to_xs ? xs.as<float2>() : nullptr);
+      k_df_normalize<<<gblk, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(w), ops.scal.as<double>() + slot,
+                                          reinterpret_cast<float4*>(out), C.stab.as<uint8_t>(),
+                                          to_xs ? xs.as<float2>() : nullptr);
     else
       k_normalize<double2><<<gblk, kBS, 0, s>>>(n, w, ops.scal.as<double>() + slot, out, C.stab.as<uint8_t>(),
                                                 to_xs ? xs.as<double2>() : nullptr);
   };
   // start vector
   k_start<<<gblk, kBS, 0, s>>>(n, S.rowflag.as<uint8_t>(), seed, W);
+  if (mixed) k_df_from_d<<<gblk, kBS, 0, s>>>(n, W);
   ops.norm2(W, 0);
   normalize(W, 0, vec(0), true);
   ops.check();
@@ -440,6 +634,7 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
     int jend = m;
     for (int j = k; j < m; ++j) {
       op_apply_orbit(op, xs.p, (double*)W, s);
+      if (mixed) k_df_from_d<<<gblk, kBS, 0, s>>>(n, W);
       // local step: CGS against the two newest basis vectors (they carry the
       // large alpha_j and beta_{j-1} components), then one full CGS pass
       // against the whole basis; a second full pass only when the first one
@@ -510,7 +705,11 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
     for (int l = 0; l < msz; ++l)
       for (int c = 0; c < keep; ++c) Sc[((size_t)l * keep + c) * 2] = Z[(size_t)l * msz + c];
     SED_CUDA(cudaMemcpyAsync(Sd.p, Sc.data(), Sc.size() * 8, cudaMemcpyHostToDevice, s));
-    k_rotate<<<dim3(gblk, (keep + 7) / 8), kBS, 0, s>>>(n, V, ld, msz, Sd.as<double2>(), keep, R);
+    if (mixed)
+      k_df_rotate<<<dim3(gblk, (keep + 7) / 8), kBS, 0, s>>>(n, reinterpret_cast<const float4*>(V), ld, msz,
+                                                             Sd.as<double2>(), keep, reinterpret_cast<float4*>(R));
+    else
+      k_rotate<<<dim3(gblk, (keep + 7) / 8), kBS, 0, s>>>(n, V, ld, msz, Sd.as<double2>(), keep, R);
     SED_CUDA(cudaMemcpyAsync(V, R, (size_t)keep * ld * 16, cudaMemcpyDeviceToDevice, s));
     ops.check();
     if (!final_rot)  // the last normalised residual direction (slot m) continues the basis
@@ -534,14 +733,16 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
       double2* HB = R;
       double2* Yr = R + (size_t)nw * ld;
       double2* HYr = R + (size_t)(2 * nw) * ld;
+      double2* B64 = R + (size_t)(3 * nw) * ld;  // FP64 copies of the Ritz vectors
+      k_df_to_d<<<gblk, kBS, 0, s>>>(n * nw, reinterpret_cast<const float4*>(V), B64);
       for (int i = 0; i < nw; ++i) {
-        op_scale_to_xs_prec(op, (const double*)(V + (size_t)i * ld), xs64.p, false, s);
+        op_scale_to_xs_prec(op, (const double*)(B64 + (size_t)i * ld), xs64.p, false, s);
         op_apply_orbit64(op, xs64.p, (double*)(HB + (size_t)i * ld), s);
         ++res.matvecs64;
       }
       std::vector<double> M((size_t)nw * nw * 2), lam, U;
       for (int bcol = 0; bcol < nw; ++bcol) {
-        ops.multidot(V, ld, nw, HB + (size_t)bcol * ld, 0, false);
+        ops.multidot(B64, ld, nw, HB + (size_t)bcol * ld, 0, false, true);
         ops.check();
         SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.p, (size_t)nw * 16, cudaMemcpyDeviceToHost, s));
         SED_CUDA(cudaStreamSynchronize(s));
@@ -561,11 +762,11 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
         }
       eigh_complex_herm(nw, M, lam, U);
       SED_CUDA(cudaMemcpyAsync(Sd.p, U.data(), U.size() * 8, cudaMemcpyHostToDevice, s));
-      k_rotate<<<dim3(gblk, (nw + 7) / 8), kBS, 0, s>>>(n, V, ld, nw, Sd.as<double2>(), nw, Yr);
+      k_rotate<<<dim3(gblk, (nw + 7) / 8), kBS, 0, s>>>(n, B64, ld, nw, Sd.as<double2>(), nw, Yr);
       k_rotate<<<dim3(gblk, (nw + 7) / 8), kBS, 0, s>>>(n, HB, ld, nw, Sd.as<double2>(), nw, HYr);
       for (int i = 0; i < nev_out; ++i) {
         k_residual<<<gblk, kBS, 0, s>>>(n, HYr + (size_t)i * ld, Yr + (size_t)i * ld, lam[i], W);
-        ops.norm2(W, 4);
+        ops.norm2(W, 4, true);
         SED_CUDA(cudaMemcpyAsync(ops.host + i, ops.scal.as<double>() + 4, 8, cudaMemcpyDeviceToHost, s));
       }
       ops.check();
