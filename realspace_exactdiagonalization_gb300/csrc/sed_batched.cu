@@ -82,7 +82,7 @@ struct BatchArgs {
 
 struct BatchSmem {
   size_t x, tchi, eta, chi64, T, Z, theta, coef, red, isr, rank, rec, off, inv, perm, misc, pw32, pw64, mask, basek,
-      pwc, zdf, cdf, total;
+      pwc, zdf, cdf, dfc, zc, total;
 };
 
 template <class VT>
@@ -114,6 +114,10 @@ static BatchSmem batch_layout(const BatchArgs& a, bool x_in_smem) {
   o = al(o + kMaxM * kMaxM * 8);
   L.cdf = o;
   o = al(o + (kMaxM + 8) * 16);
+  L.dfc = o;  // sqrt(stab) and 1/sqrt(stab) as double-float pairs
+  o = al(o + 2 * 65 * 8);
+  L.zc = o;  // complex polish rotation, double-float
+  o = al(o + kMaxNev * kMaxNev * 16);
   L.misc = o;
   o = al(o + 64 * 8);
   L.rank = o;
@@ -716,6 +720,107 @@ __device__ void df_rotate(const BatchArgs& a, const float4* V, int msz, const fl
   }
 }
 
+// x = sqrt(stab) v in double-float (the polish's matvec input)
+__device__ __forceinline__ void df_scale_xs(const BatchArgs& a, const float4* v, float4* x, const float2* s_sq) {
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    const float4 y = v[o];
+    const float2 q = s_sq[a.stab[o]];
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    df_mac(r.x, r.z, y.x, y.z, q.x, q.y);
+    df_mac(r.y, r.w, y.y, y.w, q.x, q.y);
+    df_renorm(r.x, r.z);
+    df_renorm(r.y, r.w);
+    x[o] = r;
+  }
+}
+
+// The hop-table matvec in double-float (the FP64-class polish): per hop the
+// coefficient tchi[uh] * pwc[phi] and its product with x[c], each a complex
+// double-float product (TwoProd/TwoSum on the FP32 pipe); rows scaled by
+// 1/sqrt(stab) in double-float.
+__device__ __forceinline__ void block_matvec_tab_df(const BatchArgs& a, const float4* __restrict__ x,
+                                                    const float4* __restrict__ tchi, const float4* __restrict__ pwc,
+                                                    const float2* s_isr_df, const uint8_t* __restrict__ rowflag,
+                                                    float4* __restrict__ w) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    if (!rowflag[o]) {
+      w[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
+    const int64_t sl = o >> 5;
+    const uint64_t* rp = a.hop + a.sl_off[sl] + lane;
+    const int wdt = a.sl_w[sl];
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    {
+      const double2 dg = a.diag[o];
+      float2 dr, di;
+      d_to_df(dg.x, dr.x, dr.y);
+      d_to_df(dg.y, di.x, di.y);
+      const float4 xo = x[o];
+      df_mac(acc.x, acc.z, dr.x, dr.y, xo.x, xo.z);
+      df_mac(acc.x, acc.z, -di.x, -di.y, xo.y, xo.w);
+      df_mac(acc.y, acc.w, dr.x, dr.y, xo.y, xo.w);
+      df_mac(acc.y, acc.w, di.x, di.y, xo.x, xo.z);
+    }
+#pragma unroll 2
+    for (int k = 0; k < wdt; ++k) {
+      const uint64_t r = __ldg(rp + 32 * k);
+      const float4 t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
+      const float4 ph = pwc[(uint32_t)(r >> 42)];
+      const float4 xc = x[(uint32_t)r & 0xFFFFFFu];
+      float4 cf = make_float4(0.f, 0.f, 0.f, 0.f);
+      df_mac(cf.x, cf.z, t.x, t.z, ph.x, ph.z);
+      df_mac(cf.x, cf.z, -t.y, -t.w, ph.y, ph.w);
+      df_mac(cf.y, cf.w, t.x, t.z, ph.y, ph.w);
+      df_mac(cf.y, cf.w, t.y, t.w, ph.x, ph.z);
+      df_renorm(cf.x, cf.z);
+      df_renorm(cf.y, cf.w);
+      df_mac(acc.x, acc.z, cf.x, cf.z, xc.x, xc.z);
+      df_mac(acc.x, acc.z, -cf.y, -cf.w, xc.y, xc.w);
+      df_mac(acc.y, acc.w, cf.x, cf.z, xc.y, xc.w);
+      df_mac(acc.y, acc.w, cf.y, cf.w, xc.x, xc.z);
+    }
+    df_renorm(acc.x, acc.z);
+    df_renorm(acc.y, acc.w);
+    const float2 is = s_isr_df[a.stab[o]];
+    float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
+    df_mac(y.x, y.z, acc.x, acc.z, is.x, is.y);
+    df_mac(y.y, y.w, acc.y, acc.w, is.x, is.y);
+    df_renorm(y.x, y.z);
+    df_renorm(y.y, y.w);
+    w[o] = y;
+  }
+}
+
+// out_c = sum_l V[l] S[l][c] for c < nw, S complex double-float (row stride kMaxNev)
+__device__ void df_rotate_c(const BatchArgs& a, const float4* V, int nb, const float4* S, int nw, float4* out) {
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    float4 acc[kMaxNev];
+#pragma unroll
+    for (int c = 0; c < kMaxNev; ++c) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int l = 0; l < nb; ++l) {
+      const float4 v = V[(size_t)l * a.ld + o];
+#pragma unroll
+      for (int c = 0; c < kMaxNev; ++c)
+        if (c < nw) {
+          const float4 t = S[l * kMaxNev + c];
+          df_mac(acc[c].x, acc[c].z, v.x, v.z, t.x, t.z);
+          df_mac(acc[c].x, acc[c].z, -v.y, -v.w, t.y, t.w);
+          df_mac(acc[c].y, acc[c].w, v.x, v.z, t.y, t.w);
+          df_mac(acc[c].y, acc[c].w, v.y, v.w, t.x, t.z);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kMaxNev; ++c)
+      if (c < nw) {
+        df_renorm(acc[c].x, acc[c].z);
+        df_renorm(acc[c].y, acc[c].w);
+        out[(size_t)c * a.ld + o] = acc[c];
+      }
+  }
+}
+
 // out_c = sum_l V[l] S[l][c], complex coefficients (row stride kPolCap)
 __device__ void block_rotate_c(const BatchArgs& a, const double2* V, int nb, const double2* S, int nw, double2* out) {
   for (int c0 = 0; c0 < nw; c0 += 8) {
@@ -789,6 +894,9 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
   uint64_t* s_mask = reinterpret_cast<uint64_t*>(smem + L.mask);
   double2* s_basek = reinterpret_cast<double2*>(smem + L.basek);
   V* s_pwc = reinterpret_cast<V*>(smem + L.pwc);
+  float2* s_sq_df = reinterpret_cast<float2*>(smem + L.dfc);
+  float2* s_isr_df = s_sq_df + 65;
+  float4* s_zc = reinterpret_cast<float4*>(smem + L.zc);
   int* s_int = reinterpret_cast<int*>(s_misc + 48);
 
   for (int i = threadIdx.x; i < a.rp.total; i += blockDim.x) s_rank[i] = a.rank_tab[i];
@@ -801,6 +909,8 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
     s_sqrt[i] = sqrt((double)i);
     s_isrf[i] = (float)s_isr[i];
     s_sqrtf[i] = (float)s_sqrt[i];
+    d_to_df(s_sqrt[i], s_sq_df[i].x, s_sq_df[i].y);
+    d_to_df(s_isr[i], s_isr_df[i].x, s_isr_df[i].y);
   }
 
   const size_t slots = (size_t)a.m + 1;
@@ -928,7 +1038,11 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           p = make_double2(q.x * p3.x - q.y * p3.y, -(q.x * p3.y + q.y * p3.x));
           if ((d >> 24) & 1) p = make_double2(-p.x, -p.y);
         }
-        pwc64[f] = p;
+        // the polish reads double-float pairs (re_hi, im_hi, re_lo, im_lo)
+        float4 pd;
+        d_to_df(p.x, pd.x, pd.z);
+        d_to_df(p.y, pd.y, pd.w);
+        reinterpret_cast<float4*>(pwc64)[f] = pd;
         s_pwc[f].x = p.x;
         s_pwc[f].y = p.y;
       }
@@ -943,7 +1057,14 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       const double2 t = amp[k], c0 = chi[h], bk = s_basek[h];
       const double2 c = make_double2(c0.x * bk.x + c0.y * bk.y, c0.y * bk.x - c0.x * bk.y);  // chi conj(base^k)
       const double2 v = make_double2(t.x * c.x + t.y * c.y, t.x * c.y - t.y * c.x);          // conj(t) chi'
-      tchi64[i] = v;
+      if (a.use_tab) {  // double-float pairs for the table-path polish
+        float4 vd;
+        d_to_df(v.x, vd.x, vd.z);
+        d_to_df(v.y, vd.y, vd.w);
+        reinterpret_cast<float4*>(tchi64)[i] = vd;
+      } else {
+        tchi64[i] = v;
+      }
       s_tchi[i].x = v.x;
       s_tchi[i].y = v.y;
     }
@@ -1125,56 +1246,114 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         // the Lanczos resumes with a tighter threshold; a stagnated run is
         // re-solved by the FP64 kernel (status kPolishFailed).
         const int nw = min(nev, msz);
-        double2* HB = Rb64;
-        double2* Yr = Rb64 + (size_t)nw * a.ld;
-        double2* HYr = Rb64 + (size_t)(2 * nw) * a.ld;
-        double2* B64 = Rb64 + (size_t)(3 * nw) * a.ld;  // the Ritz vectors in FP64
-        for (int i = 0; i < nw; ++i)
-          for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
-            const float4 v = Vb[(size_t)i * a.ld + o];
-            B64[(size_t)i * a.ld + o] = make_double2(df_to_d(v.x, v.z), df_to_d(v.y, v.w));
-          }
-        __syncthreads();
         double2* M = reinterpret_cast<double2*>(s_Z);  // kPolCap^2 complex fit in kMaxM^2 doubles
         double2* Zc = reinterpret_cast<double2*>(s_T);
-        for (int i = 0; i < nw; ++i) {
-          block_normalize<double2>(a, B64 + (size_t)i * a.ld, 1.0, nullptr, X64, s_sqrt);
-          __syncthreads();
-          if (a.use_tab)
-            block_matvec_tab<P64>(a, X64, tchi64, pwc64, s_isr, s_isrf, rowflag, HB + (size_t)i * a.ld);
-          else
-            block_matvec<P64, FERMI, PHASES>(a, X64, tchi64, phase, s_isr, s_isrf, s_rank, s_rec, s_off, s_inv,
-                                             rowflag, HB + (size_t)i * a.ld, pcl64);
-          __syncthreads();
-        }
-        n64 += nw;
-        for (int bcol = 0; bcol < nw; ++bcol) {
-          block_dots(a, B64, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
-          if (threadIdx.x < nw) M[threadIdx.x * kPolCap + bcol] = s_coef[threadIdx.x];
-          __syncthreads();
-        }
-        if (threadIdx.x == 0)
-          for (int i = 0; i < nw; ++i)
-            for (int j = i; j < nw; ++j) {
-              const double re = 0.5 * (M[i * kPolCap + j].x + M[j * kPolCap + i].x);
-              const double im = 0.5 * (M[i * kPolCap + j].y - M[j * kPolCap + i].y);
-              M[i * kPolCap + j] = make_double2(re, im);
-              M[j * kPolCap + i] = make_double2(re, -im);
-            }
-        __syncthreads();
-        if (threadIdx.x < 32) warp_jacobi_herm(nw, M, Zc, s_lam);
-        __syncthreads();
-        block_rotate_c(a, B64, nw, Zc, nw, Yr);
-        block_rotate_c(a, HB, nw, Zc, nw, HYr);
         double rr[kMaxNev];
 #pragma unroll
         for (int i = 0; i < kMaxNev; ++i) rr[i] = 0.0;
-        for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
-          for (int i = 0; i < nev_out; ++i) {
-            const double2 hy = HYr[(size_t)i * a.ld + o], y = Yr[(size_t)i * a.ld + o];
-            const double rx = hy.x - s_lam[i] * y.x, ry = hy.y - s_lam[i] * y.y;
-            rr[i] += rx * rx + ry * ry;
+        if (a.use_tab) {
+          // double-float polish: B = Vb[0..nw) as stored, H B through the
+          // hop table with double-float coefficients, Rayleigh-Ritz and the
+          // FP64-class residuals of the rotated pairs
+          float4* HB = Rb;
+          float4* Yr = Rb + (size_t)nw * a.ld;
+          float4* HYr = Rb + (size_t)(2 * nw) * a.ld;
+          float4* Xd = reinterpret_cast<float4*>(X64);
+          for (int i = 0; i < nw; ++i) {
+            df_scale_xs(a, Vb + (size_t)i * a.ld, Xd, s_sq_df);
+            __syncthreads();
+            block_matvec_tab_df(a, Xd, reinterpret_cast<const float4*>(tchi64),
+                                reinterpret_cast<const float4*>(pwc64), s_isr_df, rowflag, HB + (size_t)i * a.ld);
+            __syncthreads();
           }
+          n64 += nw;
+          for (int bcol = 0; bcol < nw; ++bcol) {
+            df_dots(a, Vb, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
+            if (threadIdx.x < nw) M[threadIdx.x * kPolCap + bcol] = s_coef[threadIdx.x];
+            __syncthreads();
+          }
+          if (threadIdx.x == 0)
+            for (int i = 0; i < nw; ++i)
+              for (int j = i; j < nw; ++j) {
+                const double re = 0.5 * (M[i * kPolCap + j].x + M[j * kPolCap + i].x);
+                const double im = 0.5 * (M[i * kPolCap + j].y - M[j * kPolCap + i].y);
+                M[i * kPolCap + j] = make_double2(re, im);
+                M[j * kPolCap + i] = make_double2(re, -im);
+              }
+          __syncthreads();
+          if (threadIdx.x < 32) warp_jacobi_herm(nw, M, Zc, s_lam);
+          __syncthreads();
+          if (threadIdx.x < nw * nw) {
+            const int l = threadIdx.x / nw, c = threadIdx.x % nw;
+            const double2 z = Zc[l * kPolCap + c];
+            float4 t;
+            d_to_df(z.x, t.x, t.z);
+            d_to_df(z.y, t.y, t.w);
+            s_zc[l * kMaxNev + c] = t;
+          }
+          __syncthreads();
+          df_rotate_c(a, Vb, nw, s_zc, nw, Yr);
+          df_rotate_c(a, HB, nw, s_zc, nw, HYr);
+          __syncthreads();
+          float2 lam[kMaxNev];
+#pragma unroll
+          for (int i = 0; i < kMaxNev; ++i) lam[i] = make_float2(0.f, 0.f);
+          for (int i = 0; i < nev_out; ++i) d_to_df(s_lam[i], lam[i].x, lam[i].y);
+          for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
+            for (int i = 0; i < nev_out; ++i) {
+              float4 hy = HYr[(size_t)i * a.ld + o];
+              const float4 y = Yr[(size_t)i * a.ld + o];
+              df_mac(hy.x, hy.z, -lam[i].x, -lam[i].y, y.x, y.z);
+              df_mac(hy.y, hy.w, -lam[i].x, -lam[i].y, y.y, y.w);
+              float nh = 0.f, nl = 0.f;
+              df_mac(nh, nl, hy.x, hy.z, hy.x, hy.z);
+              df_mac(nh, nl, hy.y, hy.w, hy.y, hy.w);
+              rr[i] += df_to_d(nh, nl);
+            }
+        } else {
+          double2* HB = Rb64;
+          double2* Yr = Rb64 + (size_t)nw * a.ld;
+          double2* HYr = Rb64 + (size_t)(2 * nw) * a.ld;
+          double2* B64 = Rb64 + (size_t)(3 * nw) * a.ld;  // the Ritz vectors in FP64
+          for (int i = 0; i < nw; ++i)
+            for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+              const float4 v = Vb[(size_t)i * a.ld + o];
+              B64[(size_t)i * a.ld + o] = make_double2(df_to_d(v.x, v.z), df_to_d(v.y, v.w));
+            }
+          __syncthreads();
+          for (int i = 0; i < nw; ++i) {
+            block_normalize<double2>(a, B64 + (size_t)i * a.ld, 1.0, nullptr, X64, s_sqrt);
+            __syncthreads();
+            block_matvec<P64, FERMI, PHASES>(a, X64, tchi64, phase, s_isr, s_isrf, s_rank, s_rec, s_off, s_inv,
+                                             rowflag, HB + (size_t)i * a.ld, pcl64);
+            __syncthreads();
+          }
+          n64 += nw;
+          for (int bcol = 0; bcol < nw; ++bcol) {
+            block_dots(a, B64, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
+            if (threadIdx.x < nw) M[threadIdx.x * kPolCap + bcol] = s_coef[threadIdx.x];
+            __syncthreads();
+          }
+          if (threadIdx.x == 0)
+            for (int i = 0; i < nw; ++i)
+              for (int j = i; j < nw; ++j) {
+                const double re = 0.5 * (M[i * kPolCap + j].x + M[j * kPolCap + i].x);
+                const double im = 0.5 * (M[i * kPolCap + j].y - M[j * kPolCap + i].y);
+                M[i * kPolCap + j] = make_double2(re, im);
+                M[j * kPolCap + i] = make_double2(re, -im);
+              }
+          __syncthreads();
+          if (threadIdx.x < 32) warp_jacobi_herm(nw, M, Zc, s_lam);
+          __syncthreads();
+          block_rotate_c(a, B64, nw, Zc, nw, Yr);
+          block_rotate_c(a, HB, nw, Zc, nw, HYr);
+          for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
+            for (int i = 0; i < nev_out; ++i) {
+              const double2 hy = HYr[(size_t)i * a.ld + o], y = Yr[(size_t)i * a.ld + o];
+              const double rx = hy.x - s_lam[i] * y.x, ry = hy.y - s_lam[i] * y.y;
+              rr[i] += rx * rx + ry * ry;
+            }
+        }
         block_sum<kMaxNev>(rr, s_red, s_misc + 8);
         const double thL = msz > nw ? s_theta[nw] : HUGE_VAL;
         bool ok = true;
