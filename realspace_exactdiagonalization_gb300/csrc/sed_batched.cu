@@ -638,20 +638,31 @@ __device__ __forceinline__ void df_coefs(const double2* coef, int nv, float4* cd
 }
 
 // w -= V[0..nv) c (c double-float in shared memory); returns this thread's
-// partial |w|^2 in FP64
-__device__ __forceinline__ double df_axpy(const BatchArgs& a, const float4* V, int nv, const float4* cdf,
+// partial |w|^2 in FP64.  The basis is read in groups of eight vectors whose
+// loads are issued before the arithmetic, so a thread keeps eight 16-byte HBM
+// reads in flight.  The function stays out of line: inlined, those registers
+// would add to the solver's peak and spill.
+__device__ __noinline__ double df_axpy(const BatchArgs& a, const float4* V, int nv, const float4* cdf,
                                           float4* w) {
   float nh = 0.f, nl = 0.f;
   for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
     float4 x = w[o];
-    for (int q = 0; q < nv; ++q) {
-      const float4 v = V[(size_t)q * a.ld + o];
-      const float4 c = cdf[q];
-      // x -= c v: re -= cr vr - ci vi, im -= cr vi + ci vr
-      df_mac(x.x, x.z, -c.x, -c.z, v.x, v.z);
-      df_mac(x.x, x.z, c.y, c.w, v.y, v.w);
-      df_mac(x.y, x.w, -c.x, -c.z, v.y, v.w);
-      df_mac(x.y, x.w, -c.y, -c.w, v.x, v.z);
+    for (int q0 = 0; q0 < nv; q0 += 8) {
+      const int cn = min(8, nv - q0);
+      float4 v[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn) v[c] = V[(size_t)(q0 + c) * a.ld + o];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn) {
+          const float4 cf = cdf[q0 + c];
+          // x -= c v: re -= cr vr - ci vi, im -= cr vi + ci vr
+          df_mac(x.x, x.z, -cf.x, -cf.z, v[c].x, v[c].z);
+          df_mac(x.x, x.z, cf.y, cf.w, v[c].y, v[c].w);
+          df_mac(x.y, x.w, -cf.x, -cf.z, v[c].y, v[c].w);
+          df_mac(x.y, x.w, -cf.y, -cf.w, v[c].x, v[c].z);
+        }
     }
     df_renorm(x.x, x.z);
     df_renorm(x.y, x.w);
@@ -691,22 +702,38 @@ __device__ __forceinline__ void df_normalize(const BatchArgs& a, const float4* w
   }
 }
 
-// out[c] = sum_l V[l] Z[l][c] for c < keep, Z real double-float (row stride kMaxM)
+// out[c] = sum_l V[l] Z[l][c] for c < keep, Z real double-float (row stride
+// kMaxM).  Outputs go in chunks of eight accumulators.  With more than one
+// chunk the block splits into two halves that sweep the same elements at the
+// same time, half h taking chunks h, h + 2, ..., so each basis vector streams
+// from HBM once and the other half's read of it hits the caches.  Loads are
+// issued four vectors ahead of the arithmetic.
 __device__ void df_rotate(const BatchArgs& a, const float4* V, int msz, const float2* Z, int keep, float4* out) {
-  for (int c0 = 0; c0 < keep; c0 += 8) {
-    const int cn = min(8, keep - c0);
-    for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+  const int nch = (keep + 7) / 8;
+  const int ng = nch > 1 ? 2 : 1;
+  const int gsz = blockDim.x / ng, grp = threadIdx.x / gsz, t = threadIdx.x - grp * gsz;
+  for (int ch = grp; ch < nch; ch += ng) {
+    const int c0 = ch * 8, cn = min(8, keep - c0);
+    for (int64_t o = t; o < a.n_orb; o += gsz) {
       float4 acc[8];
 #pragma unroll
       for (int c = 0; c < 8; ++c) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int q = 0; q < msz; ++q) {
-        const float4 v = V[(size_t)q * a.ld + o];
+      for (int q0 = 0; q0 < msz; q0 += 4) {
+        const int qn = min(4, msz - q0);
+        float4 v[4];
 #pragma unroll
-        for (int c = 0; c < 8; ++c)
-          if (c < cn) {
-            const float2 z = Z[q * kMaxM + c0 + c];
-            df_mac(acc[c].x, acc[c].z, v.x, v.z, z.x, z.y);
-            df_mac(acc[c].y, acc[c].w, v.y, v.w, z.x, z.y);
+        for (int u = 0; u < 4; ++u)
+          if (u < qn) v[u] = V[(size_t)(q0 + u) * a.ld + o];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (u < qn) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+              if (c < cn) {
+                const float2 z = Z[(q0 + u) * kMaxM + c0 + c];
+                df_mac(acc[c].x, acc[c].z, v[u].x, v[u].z, z.x, z.y);
+                df_mac(acc[c].y, acc[c].w, v[u].y, v[u].w, z.x, z.y);
+              }
           }
       }
 #pragma unroll
@@ -913,12 +940,12 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
     d_to_df(s_isr[i], s_isr_df[i].x, s_isr_df[i].y);
   }
 
-  const size_t slots = (size_t)a.m + 1;
-  const size_t rslots = (size_t)max(a.m, 5 * (a.nev + 2));
-  // Lanczos basis, restart buffer and work vector: double-float complex
+  // Lanczos basis, restart buffer and work vector: double-float complex.  The
+  // basis and restart buffers have the same capacity and trade places at
+  // every restart, so the rotated vectors are never copied back.
+  const size_t slots = (size_t)max(a.m + 1, 5 * (a.nev + 2));
   float4* Vb = reinterpret_cast<float4*>(a.V + (size_t)blockIdx.x * slots * a.ld);
-  float4* Rb = reinterpret_cast<float4*>(a.R + (size_t)blockIdx.x * rslots * a.ld);
-  double2* Rb64 = reinterpret_cast<double2*>(Rb);  // the FP64 polish reuses the restart buffer
+  float4* Rb = reinterpret_cast<float4*>(a.R + (size_t)blockIdx.x * slots * a.ld);
   float4* W = reinterpret_cast<float4*>(a.W + (size_t)blockIdx.x * a.ld);
   double2* X64 = a.X64 + (size_t)blockIdx.x * a.ld;
   double2* tchi64 = a.tchi64 + (size_t)blockIdx.x * a.n_bil * a.G;
@@ -1225,14 +1252,15 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       }
       __syncthreads();
       df_rotate(a, Vb, msz, s_zdf, keep, Rb);
-      __syncthreads();
-      for (int c = 0; c < keep; ++c)
-        for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
-          Vb[(size_t)c * a.ld + o] = Rb[(size_t)c * a.ld + o];
       if (!final_rot)  // the last normalised residual direction continues the basis
         for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
-          Vb[(size_t)keep * a.ld + o] = Vb[(size_t)m * a.ld + o];
+          Rb[(size_t)keep * a.ld + o] = Vb[(size_t)m * a.ld + o];
       __syncthreads();
+      {
+        float4* t = Vb;
+        Vb = Rb;
+        Rb = t;
+      }
       if (done && !mixed) {
         status = (nconv >= nev_out || invariant || stagnated) ? 0 : SED_ERR_NOT_CONVERGED;
         break;
@@ -1311,6 +1339,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
               rr[i] += df_to_d(nh, nl);
             }
         } else {
+          double2* Rb64 = reinterpret_cast<double2*>(Rb);  // the FP64 polish reuses the restart buffer
           double2* HB = Rb64;
           double2* Yr = Rb64 + (size_t)nw * a.ld;
           double2* HYr = Rb64 + (size_t)(2 * nw) * a.ld;
@@ -1829,13 +1858,14 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   dispatch_prepare(*B, a, L, ncta, precision == 0);
   B->smem = L.total;
   // per-block workspace, bounded to 16 GB
-  const size_t per_cta = ((size_t)(B->m + 1) + (size_t)std::max(B->m, 5 * (nev + 2)) + 2) * B->ld * 16 +
-                         (size_t)n_bil * G.n_ops * 16 + B->ld;
+  // basis and restart buffers of equal capacity (they trade places), work vector, FP64 input
+  const size_t slots = (size_t)std::max(B->m + 1, 5 * (nev + 2));
+  const size_t per_cta = (2 * slots + 2) * B->ld * 16 + (size_t)n_bil * G.n_ops * 16 + B->ld;
   ncta = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)ncta, (int64_t)max_req,
                                                       (int64_t)((16ull << 30) / std::max<size_t>(per_cta, 1))}));
   B->n_cta = ncta;
-  B->V.alloc((size_t)ncta * (B->m + 1) * B->ld * 16);
-  B->R.alloc((size_t)ncta * std::max(B->m, 5 * (nev + 2)) * B->ld * 16);
+  B->V.alloc((size_t)ncta * slots * B->ld * 16);
+  B->R.alloc((size_t)ncta * slots * B->ld * 16);
   B->W.alloc((size_t)ncta * B->ld * 16);
   B->X64.alloc((size_t)ncta * B->ld * 16);
   B->tchi64.alloc((size_t)ncta * std::max(n_bil * G.n_ops, 1) * 16);
