@@ -282,67 +282,133 @@ __device__ __forceinline__ void rr_pair(int t, int k, int np, int& p, int& q) {
   }
 }
 
-// Parallel cyclic Jacobi for a real symmetric n x n matrix A (row stride
-// kMaxM) in shared memory, by the whole block: each step rotates the n/2
-// disjoint pairs of the round-robin ordering at once, so the FP64 row, column
-// and eigenvector updates of a step spread over every warp (and all four SM
-// sub-partitions) instead of one warp.  Eigenvalues ascending in w,
-// eigenvectors in the columns of Z; A is destroyed.  cs holds kMaxM doubles
-// of scratch, out2 two.
+// Parallel cyclic Jacobi for a real symmetric n x n matrix A (n <= 32, row
+// stride kMaxM) in shared memory, by the whole block.  Each round-robin step
+// rotates the n/2 disjoint pairs at once, one warp per pair: lane 0 computes
+// the rotation and shuffles it to its warp, lane i updates column i (rows p,
+// q), and after one barrier row i (columns p, q of A and of the eigenvector
+// matrix).  Everything inside the sweeps runs on the FP32 pipe in
+// double-float arithmetic, with A and Z held as (hi, lo) float pairs in their
+// own double slots: GB300 issues FP64 at 1/64 of the FP32 rate, and each FP64
+// warp instruction, however few of its lanes are active, holds that pipe for
+// many cycles.  The sweeps stop when the off-diagonal norm is below 1e-13 of
+// the total (the double-float rounding level).  Eigenvalues ascending in w,
+// eigenvectors (FP64) in the columns of Z; A is destroyed.  cs holds kMaxM
+// ints of scratch, red the block-sum scratch, out2 two doubles.
+__device__ __forceinline__ float2 df_rot(float ah, float al, float bh, float bl, float2 x, float2 y) {
+  // a x + b y
+  float h = 0.f, l = 0.f;
+  df_mac(h, l, ah, al, x.x, x.y);
+  df_mac(h, l, bh, bl, y.x, y.y);
+  df_renorm(h, l);
+  return make_float2(h, l);
+}
+
+// Rotation (c, s) zeroing the off-diagonal of [[app, apq], [apq, aqq]]
+// (double-float entries).  The angle comes from the FP32 formula
+// t = sign(th) / (|th| + sqrt(th^2 + 1)), th = (aqq - app) / (2 apq); it only
+// has to shrink apq, and the next sweep removes what is left.  c and s are
+// then normalised to double-float precision: with n2 = c^2 + s^2 = 1 + d
+// evaluated exactly (TwoProd, TwoSum), 1/sqrt(n2) = 1 - d/2 + 3 d^2/8 to
+// O(d^3) ~ 1e-21, so c^2 + s^2 = 1 within double-float rounding.
+__device__ __forceinline__ void jacobi_cs_df(float2 app, float2 aqq, float2 apq, float& ch, float& cl, float& sh,
+                                             float& sl) {
+  const float d = __fadd_rn(__fsub_rn(aqq.x, app.x), __fsub_rn(aqq.y, app.y));
+  const float th = d / (2.0f * __fadd_rn(apq.x, apq.y));
+  const float t = (th >= 0.f ? 1.f : -1.f) / (fabsf(th) + sqrtf(fmaf(th, th, 1.f)));
+  const float c = rsqrtf(fmaf(t, t, 1.f)), sn = t * c;
+  const float p1 = __fmul_rn(c, c), e1 = __fmaf_rn(c, c, -p1);
+  const float p2 = __fmul_rn(sn, sn), e2 = __fmaf_rn(sn, sn, -p2);
+  float nh, nl;
+  df_two_sum(p1, p2, nh, nl);
+  const float dd = __fadd_rn(__fsub_rn(nh, 1.0f), __fadd_rn(nl, __fadd_rn(e1, e2)));  // n2 - 1, nh - 1 exact
+  const float fl = __fmaf_rn(0.375f * dd, dd, -0.5f * dd);                            // 1/sqrt(n2) - 1
+  ch = c;
+  cl = c * fl;
+  sh = sn;
+  sl = sn * fl;
+  df_renorm(ch, cl);
+  df_renorm(sh, sl);
+}
+
+// sum of two floats over the block (fixed order); result in out[0..2)
+__device__ __forceinline__ void block_sum2f(float a0, float a1, double* red, double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_xor_sync(0xFFFFFFFFu, a0, o);
+    a1 += __shfl_xor_sync(0xFFFFFFFFu, a1, o);
+  }
+  float* r = reinterpret_cast<float*>(red);
+  if (lane == 0) {
+    r[wid * 2] = a0;
+    r[wid * 2 + 1] = a1;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    float sum = 0.f;
+    for (int w = 0; w < kNW; ++w) sum += r[w * 2 + threadIdx.x];
+    out[threadIdx.x] = sum;
+  }
+  __syncthreads();
+}
+
 __device__ void block_jacobi(int n, double* A, double* Z, double* w, double* cs, double* red, double* out2) {
-  const int t = threadIdx.x, bd = blockDim.x;
+  const int t = threadIdx.x, bd = blockDim.x, lane = t & 31, wid = t >> 5;
   const int np = (n + 1) & ~1;  // an odd size gets a dummy player n
   const int half = np / 2;
-  for (int i = t; i < n * kMaxM; i += bd) Z[i] = 0.0;
+  float2* Ad = reinterpret_cast<float2*>(A);  // a double slot holds one (hi, lo) pair
+  float2* Zd = reinterpret_cast<float2*>(Z);
+  for (int e = t; e < n * n; e += bd) {
+    const int i = e / n, j = e % n;
+    float2 d;
+    d_to_df(A[i * kMaxM + j], d.x, d.y);
+    Ad[i * kMaxM + j] = d;
+    Zd[i * kMaxM + j] = make_float2(i == j ? 1.f : 0.f, 0.f);
+  }
   __syncthreads();
-  for (int i = t; i < n; i += bd) Z[i * kMaxM + i] = 1.0;
   for (int sweep = 0; sweep < 40; ++sweep) {
-    double sums[2] = {0.0, 0.0};  // off-diagonal and total squared norm
+    float off = 0.f, tot = 0.f;  // squared norms (hi parts; a stopping test only)
     for (int e = t; e < n * n; e += bd) {
       const int i = e / n, j = e % n;
-      const double v = A[i * kMaxM + j] * A[i * kMaxM + j];
-      sums[1] += v;
-      if (i != j) sums[0] += v;
+      const float v = Ad[i * kMaxM + j].x;
+      tot = fmaf(v, v, tot);
+      if (i != j) off = fmaf(v, v, off);
     }
-    block_sum<2>(sums, red, out2);
-    if (out2[0] <= 1e-29 * fmax(out2[1], 1e-300)) break;  // rounding level of the off-diagonal part
+    block_sum2f(off, tot, red, out2);
+    if (out2[0] <= 1e-26 * fmax(out2[1], 1e-300)) break;
     for (int step = 0; step < np - 1; ++step) {
-      if (t < half) {
-        int p, q;
-        rr_pair(step, t, np, p, q);
-        double c = 1.0, sn = 0.0;
+      int p = 0, q = n;
+      float ch = 1.f, cl = 0.f, sh = 0.f, sl = 0.f;
+      if (wid < half) {
+        rr_pair(step, wid, np, p, q);
         if (q < n) {
-          const double apq = A[p * kMaxM + q];
-          const double app = A[p * kMaxM + p], aqq = A[q * kMaxM + q];
-          if (!(fabs(apq) <= 1e-18 * (fabs(app) + fabs(aqq)) + 1e-300)) jacobi_cs(app, aqq, apq, &c, &sn);
+          if (lane == 0) {
+            const float2 dpq = Ad[p * kMaxM + q], dpp = Ad[p * kMaxM + p], dqq = Ad[q * kMaxM + q];
+            if (!(fabsf(dpq.x) <= 1e-16f * (fabsf(dpp.x) + fabsf(dqq.x)) + 1e-36f))
+              jacobi_cs_df(dpp, dqq, dpq, ch, cl, sh, sl);
+          }
+          ch = __shfl_sync(0xFFFFFFFFu, ch, 0);
+          cl = __shfl_sync(0xFFFFFFFFu, cl, 0);
+          sh = __shfl_sync(0xFFFFFFFFu, sh, 0);
+          sl = __shfl_sync(0xFFFFFFFFu, sl, 0);
         }
-        cs[2 * t] = c;
-        cs[2 * t + 1] = sn;
+      }
+      const bool rot = q < n && sh != 0.f;  // uniform over the warp
+      if (rot && lane < n) {                // rows p, q
+        const float2 x = Ad[p * kMaxM + lane], y = Ad[q * kMaxM + lane];
+        Ad[p * kMaxM + lane] = df_rot(ch, cl, -sh, -sl, x, y);
+        Ad[q * kMaxM + lane] = df_rot(sh, sl, ch, cl, x, y);
       }
       __syncthreads();
-      for (int e = t; e < half * n; e += bd) {  // rows p, q of A
-        const int k = e / n, i = e % n;
-        const double c = cs[2 * k], sn = cs[2 * k + 1];
-        if (sn == 0.0) continue;
-        int p, q;
-        rr_pair(step, k, np, p, q);
-        const double apk = A[p * kMaxM + i], aqk = A[q * kMaxM + i];
-        A[p * kMaxM + i] = c * apk - sn * aqk;
-        A[q * kMaxM + i] = sn * apk + c * aqk;
-      }
-      __syncthreads();
-      for (int e = t; e < 2 * half * n; e += bd) {  // columns p, q of A and of Z
-        const int which = e >= half * n;
-        const int e2 = which ? e - half * n : e;
-        const int k = e2 / n, i = e2 % n;
-        const double c = cs[2 * k], sn = cs[2 * k + 1];
-        if (sn == 0.0) continue;
-        int p, q;
-        rr_pair(step, k, np, p, q);
-        double* M = which ? Z : A;
-        const double akp = M[i * kMaxM + p], akq = M[i * kMaxM + q];
-        M[i * kMaxM + p] = c * akp - sn * akq;
-        M[i * kMaxM + q] = sn * akp + c * akq;
+      if (rot && lane < n) {  // columns p, q of A and of Z
+        float2 x = Ad[lane * kMaxM + p], y = Ad[lane * kMaxM + q];
+        Ad[lane * kMaxM + p] = df_rot(ch, cl, -sh, -sl, x, y);
+        Ad[lane * kMaxM + q] = df_rot(sh, sl, ch, cl, x, y);
+        x = Zd[lane * kMaxM + p];
+        y = Zd[lane * kMaxM + q];
+        Zd[lane * kMaxM + p] = df_rot(ch, cl, -sh, -sl, x, y);
+        Zd[lane * kMaxM + q] = df_rot(sh, sl, ch, cl, x, y);
       }
       __syncthreads();
     }
@@ -351,10 +417,12 @@ __device__ void block_jacobi(int n, double* A, double* Z, double* w, double* cs,
   // eigenvector columns through A
   int* rank = reinterpret_cast<int*>(cs);
   if (t < n) {
-    const double wi = A[t * kMaxM + t];
+    const float2 di = Ad[t * kMaxM + t];
+    const double wi = df_to_d(di.x, di.y);
     int r = 0;
     for (int j = 0; j < n; ++j) {
-      const double wj = A[j * kMaxM + j];
+      const float2 dj = Ad[j * kMaxM + j];
+      const double wj = df_to_d(dj.x, dj.y);
       r += (wj < wi) || (wj == wi && j < t);
     }
     rank[t] = r;
@@ -363,7 +431,8 @@ __device__ void block_jacobi(int n, double* A, double* Z, double* w, double* cs,
   __syncthreads();
   for (int e = t; e < n * n; e += bd) {
     const int i = e / n, j = e % n;
-    A[i * kMaxM + rank[j]] = Z[i * kMaxM + j];
+    const float2 z = Zd[i * kMaxM + j];
+    A[i * kMaxM + rank[j]] = df_to_d(z.x, z.y);
   }
   __syncthreads();
   for (int e = t; e < n * n; e += bd) {
@@ -516,7 +585,7 @@ __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typen
     const V xo = x[o];
     S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
     S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
-#pragma unroll 4
+#pragma unroll 8
     for (int k = 0; k < wdt; ++k) {
       const uint64_t r = __ldg(rp + 32 * k);
       const V t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
@@ -602,6 +671,34 @@ __device__ void block_rotate(const BatchArgs& a, const double2* V, int msz, cons
   }
 }
 
+// ------------------------------------------------- L2 prefetch of the basis
+// The basis streams from HBM (152 blocks x up to 33 vectors of 16 B per
+// element exceed the L2 many times over), and with one 512-thread block per SM
+// the threads' own loads leave too few bytes in flight to cover HBM latency.
+// So the vector sweeps run in chunks of one block-stride of elements and, a
+// chunk or two ahead of the loads, one thread per vector asks the TMA unit to
+// bring that vector's next chunk into L2 (cp.async.bulk.prefetch: no
+// registers, no shared memory, no completion to wait for).
+__device__ __forceinline__ void l2_prefetch_bulk(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// chunks that the prefetch runs ahead: about 128 KB per block in flight
+// (none for the two-vector local step, whose loads are few enough already)
+__device__ __forceinline__ int prefetch_dist(int nv) { return nv <= 2 ? 0 : (nv <= 8 ? 2 : 1); }
+
+// thread t < nv * nch issues chunk c0 + t / nv of vector t % nv (elements
+// [chunk * span, chunk * span + span) clipped to n_orb; 16-byte aligned, a
+// multiple of 16 bytes)
+__device__ __forceinline__ void prefetch_chunks(const BatchArgs& a, const float4* V, int nv, int64_t c0, int nch,
+                                                int span, int t) {
+  if (nch > 0 && t < nv * nch) {
+    const int64_t p0 = (c0 + t / nv) * span;
+    if (p0 < a.n_orb)
+      l2_prefetch_bulk(V + (size_t)(t % nv) * a.ld + p0, (uint32_t)min((int64_t)span, a.n_orb - p0) * 16u);
+  }
+}
+
 // coef[l0..l0+nv) = V[0..nv)^H w for double-float vectors, in chunks of 8
 __device__ void df_dots(const BatchArgs& a, const float4* V, int nv, const float4* w, double* red, double2* coef) {
   for (int l0 = 0; l0 < nv; l0 += 8) {
@@ -609,12 +706,18 @@ __device__ void df_dots(const BatchArgs& a, const float4* V, int nv, const float
 #pragma unroll
     for (int c = 0; c < 16; ++c) h[c] = l[c] = 0.f;
     const int cn = min(8, nv - l0);
-    for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    const int span = blockDim.x, pd = prefetch_dist(cn);
+    const float4* Vl = V + (size_t)l0 * a.ld;
+    prefetch_chunks(a, Vl, cn, 0, pd, span, threadIdx.x);
+    for (int64_t o0 = 0, ch = 0; o0 < a.n_orb; o0 += span, ++ch) {
+      if (pd) prefetch_chunks(a, Vl, cn, ch + pd, 1, span, threadIdx.x);
+      const int64_t o = o0 + threadIdx.x;
+      if (o >= a.n_orb) continue;
       const float4 x = w[o];
 #pragma unroll
       for (int c = 0; c < 8; ++c)
         if (c < cn) {
-          const float4 v = V[(size_t)(l0 + c) * a.ld + o];
+          const float4 v = Vl[(size_t)c * a.ld + o];
           // conj(v) x = (vr xr + vi xi) + i (vr xi - vi xr)
           df_mac(h[2 * c], l[2 * c], v.x, v.z, x.x, x.z);
           df_mac(h[2 * c], l[2 * c], v.y, v.w, x.y, x.w);
@@ -645,7 +748,12 @@ __device__ __forceinline__ void df_coefs(const double2* coef, int nv, float4* cd
 __device__ __noinline__ double df_axpy(const BatchArgs& a, const float4* V, int nv, const float4* cdf,
                                           float4* w) {
   float nh = 0.f, nl = 0.f;
-  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+  const int span = blockDim.x, pd = prefetch_dist(nv);
+  prefetch_chunks(a, V, nv, 0, pd, span, threadIdx.x);
+  for (int64_t o0 = 0, ch = 0; o0 < a.n_orb; o0 += span, ++ch) {
+    if (pd) prefetch_chunks(a, V, nv, ch + pd, 1, span, threadIdx.x);
+    const int64_t o = o0 + threadIdx.x;
+    if (o >= a.n_orb) continue;
     float4 x = w[o];
     for (int q0 = 0; q0 < nv; q0 += 8) {
       const int cn = min(8, nv - q0);
