@@ -729,6 +729,51 @@ __device__ void df_dots(const BatchArgs& a, const float4* V, int nv, const float
   }
 }
 
+// The local step's update folded into the first chunk of the full pass:
+// w -= Vl[0..nl) cl (cl double-float in shared memory), then coef[0..cn) =
+// V[0..cn)^H w (cn <= 7) and |w|^2 in the same sweep and the same block
+// reduction (slot 14).  Returns |w|^2.  Out of line for the same register
+// reason as df_axpy.
+__device__ __noinline__ double df_dots_local(const BatchArgs& a, const float4* V, int cn, const float4* Vl, int nl,
+                                const float4* cl, float4* w, double* red, double2* coef) {
+  float h[16], l[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) h[c] = l[c] = 0.f;
+  const int span = blockDim.x, pd = prefetch_dist(cn);
+  prefetch_chunks(a, V, cn, 0, pd, span, threadIdx.x);
+  for (int64_t o0 = 0, ch = 0; o0 < a.n_orb; o0 += span, ++ch) {
+    if (pd) prefetch_chunks(a, V, cn, ch + pd, 1, span, threadIdx.x);
+    const int64_t o = o0 + threadIdx.x;
+    if (o >= a.n_orb) continue;
+    float4 x = w[o];
+    for (int q = 0; q < nl; ++q) {
+      const float4 v = Vl[(size_t)q * a.ld + o];
+      const float4 cf = cl[q];
+      df_mac(x.x, x.z, -cf.x, -cf.z, v.x, v.z);
+      df_mac(x.x, x.z, cf.y, cf.w, v.y, v.w);
+      df_mac(x.y, x.w, -cf.x, -cf.z, v.y, v.w);
+      df_mac(x.y, x.w, -cf.y, -cf.w, v.x, v.z);
+    }
+    df_renorm(x.x, x.z);
+    df_renorm(x.y, x.w);
+    w[o] = x;
+    df_mac(h[14], l[14], x.x, x.z, x.x, x.z);
+    df_mac(h[14], l[14], x.y, x.w, x.y, x.w);
+#pragma unroll
+    for (int c = 0; c < 7; ++c)
+      if (c < cn) {
+        const float4 v = V[(size_t)c * a.ld + o];
+        df_mac(h[2 * c], l[2 * c], v.x, v.z, x.x, x.z);
+        df_mac(h[2 * c], l[2 * c], v.y, v.w, x.y, x.w);
+        df_mac(h[2 * c + 1], l[2 * c + 1], v.x, v.z, x.y, x.w);
+        df_mac(h[2 * c + 1], l[2 * c + 1], -v.y, -v.w, x.x, x.z);
+      }
+  }
+  double* out = reinterpret_cast<double*>(coef);
+  block_sum_df16(h, l, red, out);
+  return out[14];
+}
+
 // split FP64 coefficients into double-float (one thread each)
 __device__ __forceinline__ void df_coefs(const double2* coef, int nv, float4* cdf) {
   if (threadIdx.x < nv) {
@@ -1291,11 +1336,12 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         const int l0 = j > 0 ? j - 1 : 0;
         df_dots(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, W, s_red, s_coef);
         df_coefs(s_coef, j + 1 - l0, s_cdf);
-        double n0 = df_axpy(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, s_cdf, W);
         double alpha = s_coef[j - l0].x;
-        __syncthreads();
-        n0 = block_sum1(n0, s_red, s_misc);
-        df_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
+        // the local update rides on the first chunk of the full pass's dots
+        const int c0n = min(7, j + 1);
+        const double n0 = df_dots_local(a, Vb, c0n, Vb + (size_t)l0 * a.ld, j + 1 - l0, s_cdf, W, s_red,
+                                        s_coef + kMaxM + 8);
+        if (j + 1 > c0n) df_dots(a, Vb + (size_t)c0n * a.ld, j + 1 - c0n, W, s_red, s_coef + kMaxM + 8 + c0n);
         df_coefs(s_coef + kMaxM + 8, j + 1, s_cdf);
         double n1 = df_axpy(a, Vb, j + 1, s_cdf, W);
         alpha += s_coef[kMaxM + 8 + j].x;
