@@ -38,6 +38,14 @@ static constexpr int kMaxNev = 8;
 static constexpr int kNW = kBT / 32;
 static constexpr int kPolCap = 22;         // polish basis capacity (complex Rayleigh-Ritz matrix <= 22 x 22)
 static constexpr int kPolishFailed = 100;  // internal status: the FP64 polish missed its target
+// Mixed precision reorthogonalises selectively: the full pass's dot products
+// are always taken (double-float), and the update is applied only when the
+// largest of them exceeds this fraction of |w|.  Between updates the basis
+// stays orthogonal to about this level, the unit roundoff of the complex64
+// matvec, so the projected matrix keeps the accuracy that matvec allows
+// (Simon's semi-orthogonality); the Rayleigh-Ritz check then orthonormalises
+// its Ritz block explicitly.
+static constexpr double kSelReorth = 1e-7;
 
 struct BatchArgs {
   int64_t n_orb, ld;
@@ -1042,6 +1050,92 @@ __device__ __forceinline__ void block_normalize(const BatchArgs& a, const double
 }
 
 // ---------------------------------------------------------------- the kernel
+// Rayleigh-Ritz on a block B that is only semi-orthogonal (kSelReorth): with
+// G = B^H B = L L^H (Cholesky), B L^-H is orthonormal and its projected matrix
+// is L^-1 M L^-H, M = B^H H B.  M (row stride kPolCap) is overwritten by the
+// projected matrix and G (row stride kMaxNev) by X = L^-1 (lower triangular);
+// T is kMaxNev^2 of scratch.  The factorisation runs on thread 0 (nw <= 8),
+// the products on nw^2 threads.
+__device__ void rr_orthonormalise(int nw, double2* M, double2* G, double2* T) {
+  constexpr int SG = kMaxNev;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < nw; ++k) {  // Cholesky, lower
+      double d = G[k * SG + k].x;
+      for (int p = 0; p < k; ++p) d -= G[k * SG + p].x * G[k * SG + p].x + G[k * SG + p].y * G[k * SG + p].y;
+      const double lkk = sqrt(d), inv = 1.0 / lkk;
+      G[k * SG + k] = make_double2(lkk, 0.0);
+      for (int i = k + 1; i < nw; ++i) {
+        double2 sm = G[i * SG + k];
+        for (int p = 0; p < k; ++p) {  // -= L_ip conj(L_kp)
+          const double2 u = G[i * SG + p], v = G[k * SG + p];
+          sm.x -= u.x * v.x + u.y * v.y;
+          sm.y -= u.y * v.x - u.x * v.y;
+        }
+        G[i * SG + k] = make_double2(sm.x * inv, sm.y * inv);
+      }
+    }
+    // X = L^-1 in place, row by row: X_ij = -(sum_{k=j}^{i-1} L_ik X_kj) / L_ii
+    // reads L_ik only for k >= j, so entry j of row i can be overwritten
+    for (int i = 0; i < nw; ++i) {
+      const double inv = 1.0 / G[i * SG + i].x;
+      for (int j = 0; j < i; ++j) {
+        double2 sm = make_double2(0.0, 0.0);
+        for (int k = j; k < i; ++k) {
+          const double2 u = G[i * SG + k], v = G[k * SG + j];
+          sm.x += u.x * v.x - u.y * v.y;
+          sm.y += u.x * v.y + u.y * v.x;
+        }
+        G[i * SG + j] = make_double2(-sm.x * inv, -sm.y * inv);
+      }
+      G[i * SG + i] = make_double2(inv, 0.0);
+    }
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < nw * nw) {  // T = M X^H
+    const int p = t / nw, j = t % nw;
+    double2 sm = make_double2(0.0, 0.0);
+    for (int q = 0; q <= j; ++q) {
+      const double2 u = M[p * kPolCap + q], v = G[j * SG + q];
+      sm.x += u.x * v.x + u.y * v.y;
+      sm.y += u.y * v.x - u.x * v.y;
+    }
+    T[p * SG + j] = sm;
+  }
+  __syncthreads();
+  if (t < nw * nw) {  // M = X T
+    const int i = t / nw, j = t % nw;
+    double2 sm = make_double2(0.0, 0.0);
+    for (int p = 0; p <= i; ++p) {
+      const double2 u = G[i * SG + p], v = T[p * SG + j];
+      sm.x += u.x * v.x - u.y * v.y;
+      sm.y += u.x * v.y + u.y * v.x;
+    }
+    M[i * kPolCap + j] = sm;
+  }
+  __syncthreads();
+}
+
+// eigenvectors U of the projected matrix (Z, row stride kPolCap) -> block
+// coefficients C = X^H U, so that the Ritz vectors are B C
+__device__ void rr_back(int nw, const double2* G, double2* Z, double2* T) {
+  constexpr int SG = kMaxNev;
+  const int t = threadIdx.x;
+  if (t < nw * nw) {
+    const int i = t / nw, c = t % nw;
+    double2 sm = make_double2(0.0, 0.0);
+    for (int k = i; k < nw; ++k) {  // conj(X_ki) U_kc
+      const double2 u = G[k * SG + i], v = Z[k * kPolCap + c];
+      sm.x += u.x * v.x + u.y * v.y;
+      sm.y += u.x * v.y - u.y * v.x;
+    }
+    T[i * SG + c] = sm;
+  }
+  __syncthreads();
+  if (t < nw * nw) Z[(t / nw) * kPolCap + t % nw] = T[(t / nw) * SG + t % nw];
+  __syncthreads();
+}
+
 template <class P, bool FERMI, bool PHASES, bool X_SMEM>
 __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
   using V = typename P::V;
@@ -1342,19 +1436,30 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         const double n0 = df_dots_local(a, Vb, c0n, Vb + (size_t)l0 * a.ld, j + 1 - l0, s_cdf, W, s_red,
                                         s_coef + kMaxM + 8);
         if (j + 1 > c0n) df_dots(a, Vb + (size_t)c0n * a.ld, j + 1 - c0n, W, s_red, s_coef + kMaxM + 8 + c0n);
-        df_coefs(s_coef + kMaxM + 8, j + 1, s_cdf);
-        double n1 = df_axpy(a, Vb, j + 1, s_cdf, W);
-        alpha += s_coef[kMaxM + 8 + j].x;
-        __syncthreads();
-        n1 = block_sum1(n1, s_red, s_misc + 1);
-        double nf = n1;
-        if (n1 < 0.5 * n0) {
-          df_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
+        // mixed precision: update only when the measured loss of orthogonality
+        // exceeds kSelReorth (the test is uniform over the block)
+        double cmax = 0.0;
+        if (mixed)
+          for (int i = 0; i <= j; ++i) {
+            const double2 c = s_coef[kMaxM + 8 + i];
+            cmax = fmax(cmax, fabs(c.x) + fabs(c.y));
+          }
+        double nf = n0;
+        if (!mixed || cmax > kSelReorth * sqrt(n0)) {
           df_coefs(s_coef + kMaxM + 8, j + 1, s_cdf);
-          double n2 = df_axpy(a, Vb, j + 1, s_cdf, W);
+          double n1 = df_axpy(a, Vb, j + 1, s_cdf, W);
           alpha += s_coef[kMaxM + 8 + j].x;
           __syncthreads();
-          nf = block_sum1(n2, s_red, s_misc + 2);
+          n1 = block_sum1(n1, s_red, s_misc + 1);
+          nf = n1;
+          if (n1 < 0.5 * n0) {
+            df_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
+            df_coefs(s_coef + kMaxM + 8, j + 1, s_cdf);
+            double n2 = df_axpy(a, Vb, j + 1, s_cdf, W);
+            alpha += s_coef[kMaxM + 8 + j].x;
+            __syncthreads();
+            nf = block_sum1(n2, s_red, s_misc + 2);
+          }
         }
         beta = sqrt(nf);
         if (threadIdx.x == 0) {
@@ -1421,7 +1526,8 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       }
       if (done) {
         // FP64 check of the complex64 candidate: one Rayleigh-Ritz step with
-        // FP64 matvecs over its nev + 2 Ritz vectors B = Vb[0..nw); accepted
+        // FP64 matvecs over its nev + 2 Ritz vectors B = Vb[0..nw), the block
+        // orthonormalised through its Gram matrix (rr_orthonormalise); accepted
         // when every requested pair meets the residual tolerance or the
         // quadratic bound |dE| <= |r|^2 / gap (gap to the first Lanczos Ritz
         // value outside the block) is below kMixedRelTarget |E|.  Otherwise
@@ -1429,6 +1535,8 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         // re-solved by the FP64 kernel (status kPolishFailed).
         const int nw = min(nev, msz);
         double2* M = reinterpret_cast<double2*>(s_Z);  // kPolCap^2 complex fit in kMaxM^2 doubles
+        double2* Gm = M + kPolCap * kMaxNev;           // Gram matrix, then L^-1 (stride kMaxNev)
+        double2* Tm = Gm + kMaxNev * kMaxNev;          // scratch
         double2* Zc = reinterpret_cast<double2*>(s_T);
         double rr[kMaxNev];
 #pragma unroll
@@ -1453,7 +1561,11 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
             df_dots(a, Vb, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
             if (threadIdx.x < nw) M[threadIdx.x * kPolCap + bcol] = s_coef[threadIdx.x];
             __syncthreads();
+            df_dots(a, Vb, nw, Vb + (size_t)bcol * a.ld, s_red, s_coef);
+            if (threadIdx.x < nw) Gm[threadIdx.x * kMaxNev + bcol] = s_coef[threadIdx.x];
+            __syncthreads();
           }
+          rr_orthonormalise(nw, M, Gm, Tm);
           if (threadIdx.x == 0)
             for (int i = 0; i < nw; ++i)
               for (int j = i; j < nw; ++j) {
@@ -1465,6 +1577,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           __syncthreads();
           if (threadIdx.x < 32) warp_jacobi_herm(nw, M, Zc, s_lam);
           __syncthreads();
+          rr_back(nw, Gm, Zc, Tm);
           if (threadIdx.x < nw * nw) {
             const int l = threadIdx.x / nw, c = threadIdx.x % nw;
             const double2 z = Zc[l * kPolCap + c];
@@ -1516,7 +1629,11 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
             block_dots(a, B64, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
             if (threadIdx.x < nw) M[threadIdx.x * kPolCap + bcol] = s_coef[threadIdx.x];
             __syncthreads();
+            block_dots(a, B64, nw, B64 + (size_t)bcol * a.ld, s_red, s_coef);
+            if (threadIdx.x < nw) Gm[threadIdx.x * kMaxNev + bcol] = s_coef[threadIdx.x];
+            __syncthreads();
           }
+          rr_orthonormalise(nw, M, Gm, Tm);
           if (threadIdx.x == 0)
             for (int i = 0; i < nw; ++i)
               for (int j = i; j < nw; ++j) {
@@ -1528,6 +1645,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           __syncthreads();
           if (threadIdx.x < 32) warp_jacobi_herm(nw, M, Zc, s_lam);
           __syncthreads();
+          rr_back(nw, Gm, Zc, Tm);
           block_rotate_c(a, B64, nw, Zc, nw, Yr);
           block_rotate_c(a, HB, nw, Zc, nw, HYr);
           for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
