@@ -38,14 +38,6 @@ static constexpr int kMaxNev = 8;
 static constexpr int kNW = kBT / 32;
 static constexpr int kPolCap = 22;         // polish basis capacity (complex Rayleigh-Ritz matrix <= 22 x 22)
 static constexpr int kPolishFailed = 100;  // internal status: the FP64 polish missed its target
-// Mixed precision reorthogonalises selectively: the full pass's dot products
-// are always taken (double-float), and the update is applied only when the
-// largest of them exceeds this fraction of |w|.  Between updates the basis
-// stays orthogonal to about this level, the unit roundoff of the complex64
-// matvec, so the projected matrix keeps the accuracy that matvec allows
-// (Simon's semi-orthogonality); the Rayleigh-Ritz check then orthonormalises
-// its Ritz block explicitly.
-static constexpr double kSelReorth = 1e-7;
 
 struct BatchArgs {
   int64_t n_orb, ld;

@@ -231,6 +231,14 @@ static constexpr int64_t kDenseMaxDim = 500;
 // bound |r|^2 / gap is below this fraction of |E| (one tenth of the 1e-9
 // relative accuracy the mixed path promises).
 static constexpr double kMixedRelTarget = 1e-10;
+// Mixed precision reorthogonalises selectively: the full pass's dot products
+// are always taken (FP64-class), and the update is applied only when the
+// largest of them exceeds this fraction of |w|.  Between updates the basis
+// stays orthogonal to about this level, the unit roundoff of the complex64
+// matvec, so the projected matrix keeps the accuracy that matvec allows
+// (Simon's semi-orthogonality); the Rayleigh-Ritz check orthonormalises its
+// Ritz block explicitly (Gram matrix, Cholesky).
+static constexpr double kSelReorth = 1e-7;
 
 // small dense eigen-solvers (host)
 void eigh_real_sym(int n, std::vector<double>& A, std::vector<double>& w, std::vector<double>& Z);

@@ -10,13 +10,15 @@
 // complex128; the projected matrix and its eigen-decomposition stay on the host.
 //
 // Mixed precision (SED_PREC_MIXED): the matvec reads complex64 inputs and
-// accumulates in FP32, everything else stays FP64.  Once the Ritz estimates of
+// accumulates in FP32, everything else stays FP64-class (double-float
+// vectors), and the full reorthogonalisation is selective (kSelReorth).  Once the Ritz estimates of
 // the requested pairs fall below 1e-6 |E|, one Rayleigh-Ritz step with FP64
 // matvecs over the nev + 2 Ritz vectors polishes the eigenvalues, and the
 // result is accepted by the quadratic bound |dE| <= |r|^2 / gap (see solve).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <complex>
 #include <cstring>
 
 #include "sed_dfloat.cuh"
@@ -408,7 +410,8 @@ __global__ void __launch_bounds__(kBS) k_df_multidot(int64_t n, const float4* __
 // w -= sum_l c_l V_l (double-float), optionally the block partial of |w|^2
 __global__ void __launch_bounds__(kBS) k_df_multiaxpy(int64_t n, const float4* __restrict__ V, int64_t ld, int nv,
                                                       const double2* __restrict__ c, float4* __restrict__ w,
-                                                      double* __restrict__ norm_part) {
+                                                      double* __restrict__ norm_part, const int* __restrict__ skip) {
+  if (skip && *skip) return;  // selective reorthogonalisation: no update this step
   __shared__ float4 sc[128];
   for (int l = threadIdx.x; l < nv; l += blockDim.x) {
     float4 t;
@@ -438,6 +441,16 @@ __global__ void __launch_bounds__(kBS) k_df_multiaxpy(int64_t n, const float4* _
     const double2 r = block_sum2(df_to_d(nh, nl), 0.0);
     if (threadIdx.x == 0) norm_part[blockIdx.x] = r.x;
   }
+}
+
+// selective reorthogonalisation: skip = (max_l |c_l| <= eta |w|), with |c| bounded
+// by |re| + |im| and |w|^2 from the local step
+__global__ void k_sel_flag(const double2* __restrict__ c, int nv, const double* __restrict__ w2, double eta,
+                           int* __restrict__ skip) {
+  double m = 0.0;
+  for (int l = threadIdx.x; l < nv; l += 32) m = fmax(m, fabs(c[l].x) + fabs(c[l].y));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+  if (threadIdx.x == 0) *skip = m <= eta * sqrt(*w2) ? 1 : 0;
 }
 
 // v = w / sqrt(nrm2) (double-float); xs = sqrt(stab) v in complex64
@@ -510,6 +523,67 @@ __global__ void __launch_bounds__(kBS) k_df_rotate(int64_t n, const float4* __re
   }
 }
 
+// ------------------------------------------------ semi-orthogonal Ritz block
+// Rayleigh-Ritz on a block B with Gram matrix G = B^H B (complex, row-major
+// re/im pairs): G = L L^H (Cholesky), X = L^-1, and M = B^H H B is replaced
+// by X M X^H, the projection onto the orthonormal block B X^H.
+void gram_orthonormalise(int n, const std::vector<double>& G, std::vector<double>& M, std::vector<double>& X) {
+  using C = std::complex<double>;
+  std::vector<C> L((size_t)n * n, C(0.0, 0.0)), Xc((size_t)n * n, C(0.0, 0.0)), Mc((size_t)n * n), T((size_t)n * n);
+  for (int i = 0; i < n * n; ++i) Mc[i] = C(M[2 * i], M[2 * i + 1]);
+  for (int k = 0; k < n; ++k) {
+    double d = G[((size_t)k * n + k) * 2];
+    for (int p = 0; p < k; ++p) d -= std::norm(L[(size_t)k * n + p]);
+    SED_REQUIRE(d > 0.0, 4, "Ritz block is numerically dependent");
+    const double lkk = std::sqrt(d);
+    L[(size_t)k * n + k] = lkk;
+    for (int i = k + 1; i < n; ++i) {
+      C sm(G[((size_t)i * n + k) * 2], G[((size_t)i * n + k) * 2 + 1]);
+      for (int p = 0; p < k; ++p) sm -= L[(size_t)i * n + p] * std::conj(L[(size_t)k * n + p]);
+      L[(size_t)i * n + k] = sm / lkk;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    Xc[(size_t)i * n + i] = 1.0 / L[(size_t)i * n + i];
+    for (int j = 0; j < i; ++j) {
+      C sm(0.0, 0.0);
+      for (int k = j; k < i; ++k) sm += L[(size_t)i * n + k] * Xc[(size_t)k * n + j];
+      Xc[(size_t)i * n + j] = -sm / L[(size_t)i * n + i];
+    }
+  }
+  for (int p = 0; p < n; ++p)  // T = M X^H
+    for (int j = 0; j < n; ++j) {
+      C sm(0.0, 0.0);
+      for (int q = 0; q < n; ++q) sm += Mc[(size_t)p * n + q] * std::conj(Xc[(size_t)j * n + q]);
+      T[(size_t)p * n + j] = sm;
+    }
+  X.assign((size_t)n * n * 2, 0.0);
+  for (int i = 0; i < n; ++i)  // M = X T
+    for (int j = 0; j < n; ++j) {
+      C sm(0.0, 0.0);
+      for (int p = 0; p < n; ++p) sm += Xc[(size_t)i * n + p] * T[(size_t)p * n + j];
+      M[((size_t)i * n + j) * 2] = sm.real();
+      M[((size_t)i * n + j) * 2 + 1] = sm.imag();
+      X[((size_t)i * n + j) * 2] = Xc[(size_t)i * n + j].real();
+      X[((size_t)i * n + j) * 2 + 1] = Xc[(size_t)i * n + j].imag();
+    }
+}
+
+// block coefficients X^H U of the Ritz vectors (U: eigenvectors of X M X^H)
+std::vector<double> gram_back(int n, const std::vector<double>& X, const std::vector<double>& U) {
+  std::vector<double> R((size_t)n * n * 2, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < n; ++c) {
+      std::complex<double> sm(0.0, 0.0);
+      for (int k = 0; k < n; ++k)
+        sm += std::conj(std::complex<double>(X[((size_t)k * n + i) * 2], X[((size_t)k * n + i) * 2 + 1])) *
+              std::complex<double>(U[((size_t)k * n + c) * 2], U[((size_t)k * n + c) * 2 + 1]);
+      R[((size_t)i * n + c) * 2] = sm.real();
+      R[((size_t)i * n + c) * 2 + 1] = sm.imag();
+    }
+  return R;
+}
+
 // ------------------------------------------------------------- host driver
 namespace {
 
@@ -517,7 +591,7 @@ struct VecOps {
   int64_t n;
   int nblk;
   cudaStream_t s;
-  DevBuf part, part1, coef, scal;  // partial sums, coefficients, scalars
+  DevBuf part, part1, coef, scal, flag;  // partial sums, coefficients, scalars, skip flag
   double* host = nullptr;          // pinned scratch
   bool df = false;                 // vectors are double-float (mixed precision)
   VecOps(int64_t n_, cudaStream_t s_, bool df_) : n(n_), s(s_), df(df_) {
@@ -527,6 +601,7 @@ struct VecOps {
     part1.alloc((size_t)nblk * 8);
     coef.alloc(256 * 16);
     scal.alloc(64);
+    flag.alloc(16);
     SED_CUDA(cudaMallocHost((void**)&host, 4096));
   }
   ~VecOps() {
@@ -553,11 +628,13 @@ struct VecOps {
     k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), nblk, coef.as<double2>() + off, acc ? 1 : 0);
   }
   // w -= V[0..nv) coef[off..], optionally scal[slot] = |w|^2
-  void multiaxpy(const double2* V, int64_t ld, int nv, double2* w, int off, int norm_slot, bool fp64 = false) {
+  // (skip: device flag of the selective reorthogonalisation, double-float only)
+  void multiaxpy(const double2* V, int64_t ld, int nv, double2* w, int off, int norm_slot, bool fp64 = false,
+                 const int* skip = nullptr) {
     if (df && !fp64)
       k_df_multiaxpy<<<nblk, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(V), ld, nv, coef.as<double2>() + off,
                                           reinterpret_cast<float4*>(w),
-                                          norm_slot >= 0 ? part1.as<double>() : nullptr);
+                                          norm_slot >= 0 ? part1.as<double>() : nullptr, skip);
     else
       k_multiaxpy<<<nblk, kBS, 0, s>>>(n, V, ld, nv, coef.as<double2>() + off, w,
                                        norm_slot >= 0 ? part1.as<double>() : nullptr);
@@ -643,17 +720,25 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
       ops.multidot(vec(l0), ld, j + 1 - l0, W, 0, false);
       ops.multiaxpy(vec(l0), ld, j + 1 - l0, W, 0, 5);
       ops.multidot(V, ld, j + 1, W, 128, false);
-      ops.multiaxpy(V, ld, j + 1, W, 128, 1);
+      // mixed precision: the update only when the measured loss of
+      // orthogonality exceeds kSelReorth (decided on the device)
+      if (mixed)
+        k_sel_flag<<<1, 32, 0, s>>>(ops.coef.as<double2>() + 128, j + 1, ops.scal.as<double>() + 5, kSelReorth,
+                                    ops.flag.as<int>());
+      ops.multiaxpy(V, ld, j + 1, W, 128, 1, false, mixed ? ops.flag.as<int>() : nullptr);
       ops.check();
       SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.as<double2>() + (j - l0), 16, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaMemcpyAsync(ops.host + 2, ops.coef.as<double2>() + 128 + j, 16, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaMemcpyAsync(ops.host + 4, ops.scal.as<double>() + 1, 8, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaMemcpyAsync(ops.host + 5, ops.scal.as<double>() + 5, 8, cudaMemcpyDeviceToHost, s));
+      if (mixed) SED_CUDA(cudaMemcpyAsync(ops.host + 6, ops.flag.p, 4, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaStreamSynchronize(s));
       ++res.matvecs;
-      double alpha = ops.host[0] + ops.host[2];
-      double nrm2 = ops.host[4];
-      if (nrm2 < 0.5 * ops.host[5]) {
+      int skipped = 0;
+      if (mixed) std::memcpy(&skipped, ops.host + 6, 4);
+      double alpha = ops.host[0] + (skipped ? 0.0 : ops.host[2]);
+      double nrm2 = skipped ? ops.host[5] : ops.host[4];
+      if (!skipped && nrm2 < 0.5 * ops.host[5]) {
         ops.multidot(V, ld, j + 1, W, 128, false);
         ops.multiaxpy(V, ld, j + 1, W, 128, 1);
         ops.check();
@@ -751,6 +836,21 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
           M[((size_t)a2 * nw + bcol) * 2 + 1] = ops.host[2 * a2 + 1];
         }
       }
+      // the block is only semi-orthogonal (kSelReorth): with its Gram matrix
+      // G = B^H B = L L^H, B L^-H is orthonormal and projects H to L^-1 M L^-H
+      std::vector<double> Gm((size_t)nw * nw * 2);
+      for (int bcol = 0; bcol < nw; ++bcol) {
+        ops.multidot(B64, ld, nw, B64 + (size_t)bcol * ld, 0, false, true);
+        ops.check();
+        SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.p, (size_t)nw * 16, cudaMemcpyDeviceToHost, s));
+        SED_CUDA(cudaStreamSynchronize(s));
+        for (int a2 = 0; a2 < nw; ++a2) {
+          Gm[((size_t)a2 * nw + bcol) * 2] = ops.host[2 * a2];
+          Gm[((size_t)a2 * nw + bcol) * 2 + 1] = ops.host[2 * a2 + 1];
+        }
+      }
+      std::vector<double> X;
+      gram_orthonormalise(nw, Gm, M, X);
       for (int a2 = 0; a2 < nw; ++a2)  // Hermitian part
         for (int b2 = a2; b2 < nw; ++b2) {
           const double r = 0.5 * (M[((size_t)a2 * nw + b2) * 2] + M[((size_t)b2 * nw + a2) * 2]);
@@ -761,6 +861,7 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
           M[((size_t)b2 * nw + a2) * 2 + 1] = -im;
         }
       eigh_complex_herm(nw, M, lam, U);
+      U = gram_back(nw, X, U);  // Ritz vectors B X^H U
       SED_CUDA(cudaMemcpyAsync(Sd.p, U.data(), U.size() * 8, cudaMemcpyHostToDevice, s));
       k_rotate<<<dim3(gblk, (nw + 7) / 8), kBS, 0, s>>>(n, B64, ld, nw, Sd.as<double2>(), nw, Yr);
       k_rotate<<<dim3(gblk, (nw + 7) / 8), kBS, 0, s>>>(n, HB, ld, nw, Sd.as<double2>(), nw, HYr);
