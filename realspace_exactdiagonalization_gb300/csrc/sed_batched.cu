@@ -19,9 +19,11 @@
 // sector dimensions); a request's result depends only on its own inputs and
 // seed, never on the other requests in the launch.  No block waits on another.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <unordered_map>
 
 #include "../../include/sed_capi.h"
@@ -2152,13 +2154,39 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   return B;
 }
 
+// Every request's term list must be Hermitian and invariant under its own
+// group.  Large batches are checked on up to eight host threads (requests
+// interleaved); the error reported is the one of the lowest failing request,
+// as a serial check would report it.
 static void validate_requests(BatchImpl& B, int n_req, const double* phase, const double* amp) {
   const GroupImpl& G = *B.cat->group;
-  GroupImpl Gr = G;
-  for (int b = 0; b < n_req; ++b) {
-    Gr.phase.assign(phase + (size_t)b * G.n_ops * G.n_site * 2, phase + (size_t)(b + 1) * G.n_ops * G.n_site * 2);
-    check_hermitian_symmetric(Gr, B.n_bil, B.bil_ij.data(), amp + (size_t)b * B.n_bil * 2);
+  const int nthr = n_req >= 64 ? (int)std::min(8u, std::max(1u, std::thread::hardware_concurrency())) : 1;
+  std::vector<int> first_bad(nthr, INT_MAX);
+  std::vector<Error> err(nthr);
+  auto work = [&](int t) {
+    GroupImpl Gr = G;
+    for (int b = t; b < n_req; b += nthr) {
+      Gr.phase.assign(phase + (size_t)b * G.n_ops * G.n_site * 2, phase + (size_t)(b + 1) * G.n_ops * G.n_site * 2);
+      try {
+        check_hermitian_symmetric(Gr, B.n_bil, B.bil_ij.data(), amp + (size_t)b * B.n_bil * 2);
+      } catch (const Error& e) {
+        first_bad[t] = b;
+        err[t] = e;
+        return;
+      }
+    }
+  };
+  if (nthr == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthr; ++t) pool.emplace_back(work, t);
+    for (auto& th : pool) th.join();
   }
+  int tb = 0;
+  for (int t = 1; t < nthr; ++t)
+    if (first_bad[t] < first_bad[tb]) tb = t;
+  if (first_bad[tb] != INT_MAX) throw err[tb];
 }
 
 // Launch on device-resident buffers (asynchronous on the batch stream).

@@ -70,35 +70,54 @@ void build_term_tables(const GroupImpl& G, int n_bil, const int32_t* bil_ij, con
 // (i -> j, t) needs its partner (j -> i, conj t), and the group must map it to
 // (perm_g(i) -> perm_g(j), t * eta_g(j) * conj(eta_g(i))).
 void check_hermitian_symmetric(const GroupImpl& G, int n_bil, const int32_t* bil_ij, const double* bil_t) {
-  std::map<std::pair<int, int>, std::pair<double, double>> T;
+  // summed amplitude of every (i, j) in a dense N x N table (N <= 64), kept
+  // zero between calls: a batch validates hundreds of requests per launch
+  const int N = G.n_site;
+  thread_local std::vector<double> tab(64 * 64 * 2, 0.0);
+  thread_local std::vector<uint8_t> used(64 * 64, 0);
+  std::vector<int> keys;
+  keys.reserve(n_bil);
+  struct Reset {  // restores the all-zero state on every exit, a throw included
+    std::vector<int>& k;
+    ~Reset() {
+      for (int e : k) {
+        tab[2 * e] = tab[2 * e + 1] = 0.0;
+        used[e] = 0;
+      }
+    }
+  } reset{keys};
   double scale = 0.0;
   for (int k = 0; k < n_bil; ++k) {
-    auto& e = T[{bil_ij[2 * k], bil_ij[2 * k + 1]}];
-    e.first += bil_t[2 * k];
-    e.second += bil_t[2 * k + 1];
+    const int i = bil_ij[2 * k], j = bil_ij[2 * k + 1];
+    SED_REQUIRE(i >= 0 && i < N && j >= 0 && j < N, 1, "bilinear term site index out of range");
+    const int e = i * N + j;
+    if (!used[e]) {
+      used[e] = 1;
+      keys.push_back(e);
+    }
+    tab[2 * e] += bil_t[2 * k];
+    tab[2 * e + 1] += bil_t[2 * k + 1];
     scale = std::max(scale, std::hypot(bil_t[2 * k], bil_t[2 * k + 1]));
   }
-  const double tol = 1e-9 * std::max(scale, 1e-300);
-  auto get = [&](int i, int j) {
-    auto it = T.find({i, j});
-    return it == T.end() ? std::make_pair(0.0, 0.0) : it->second;
-  };
-  for (auto& kv : T) {
-    const int i = kv.first.first, j = kv.first.second;
-    const auto t = kv.second;
-    const auto r = get(j, i);
-    SED_REQUIRE(std::hypot(t.first - r.first, t.second + r.second) <= tol, 6,
+  std::sort(keys.begin(), keys.end());  // (i, j) in lexicographic order
+  const double tol = 1e-9 * std::max(scale, 1e-300), tol2 = tol * tol;
+  for (int e : keys) {
+    const int i = e / N, j = e % N;
+    const double tr = tab[2 * e], ti = tab[2 * e + 1];
+    const int er = j * N + i;
+    const double hr = tr - tab[2 * er], hi = ti + tab[2 * er + 1];
+    SED_REQUIRE(hr * hr + hi * hi <= tol2, 6,
                 "bilinear terms are not Hermitian-closed: (i, j, t) needs (j, i, conj(t))");
-    const int N = G.n_site;
     for (int g = 0; g < G.n_ops; ++g) {
       const int pi = G.perm[(size_t)g * N + i], pj = G.perm[(size_t)g * N + j];
       const double eir = G.phase[((size_t)g * N + i) * 2], eii = G.phase[((size_t)g * N + i) * 2 + 1];
       const double ejr = G.phase[((size_t)g * N + j) * 2], eji = G.phase[((size_t)g * N + j) * 2 + 1];
       // t * eta_j * conj(eta_i)
       const double ar = ejr * eir + eji * eii, ai = eji * eir - ejr * eii;
-      const double er = t.first * ar - t.second * ai, ei = t.first * ai + t.second * ar;
-      const auto s = get(pi, pj);
-      SED_REQUIRE(std::hypot(er - s.first, ei - s.second) <= tol, 6,
+      const double xr = tr * ar - ti * ai, xi = tr * ai + ti * ar;
+      const int es = pi * N + pj;
+      const double dr = xr - tab[2 * es], di = xi - tab[2 * es + 1];
+      SED_REQUIRE(dr * dr + di * di <= tol2, 6,
                   "bilinear terms are not invariant under the symmetry group");
     }
   }

@@ -91,6 +91,9 @@ def test_terms_validation(lib):
         bad = t.copy()
         bad[0] *= 1.5  # breaks Hermiticity and translation invariance
         assert lib.sed_terms_validate(g, len(t), vp(ij), vp(bad)) == _lib.SED_ERR_NOT_HERMITIAN
+        # the validator's term table is reused across calls: a rejected list
+        # leaves no residue behind
+        assert lib.sed_terms_validate(g, len(t), vp(ij), vp(t)) == 0, lib.sed_last_error()
         if th != (0.0, 0.0):
             # twist phases applied without the matching group gauge
             G0 = L.build_translation_group(spec.lattice, (0.0, 0.0))

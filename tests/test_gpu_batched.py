@@ -109,3 +109,28 @@ def test_hop_table_fermion_flux_matches_on_the_fly():
     assert not s_fly.last_stats()["hop_table"]
     assert np.array_equal(a["dims"], b["dims"])
     np.testing.assert_allclose(a["evals"], b["evals"], rtol=0, atol=1e-9)
+
+
+def test_batch_rejects_a_bad_request_in_a_large_batch():
+    """Every request's term list is validated before the launch (on several
+    host threads for a large batch): one non-Hermitian request among 96 fails
+    the whole call with SED_ERR_NOT_HERMITIAN, and the solver stays usable."""
+    import dataclasses
+
+    from realspace_exactdiagonalization_gb300 import _lib
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.checkerboard(3, 2, n_filled=4)
+    twists = [(a / 4, b / 4) for a in range(4) for b in range(4)]
+    reqs = flux_scan_requests(spec, twists)
+    assert len(reqs) == 96
+    solver = _solver(spec, "mixed", max_requests=128)
+    bad = list(reqs)
+    amps = list(bad[70].amplitudes)
+    amps[0] *= 1.5
+    bad[70] = dataclasses.replace(bad[70], amplitudes=amps)
+    with pytest.raises(_lib.SEDError) as e:
+        solver.run(bad)
+    assert e.value.code == _lib.SED_ERR_NOT_HERMITIAN
+    out = solver.run(reqs[:8])
+    assert (out["status"] == 0).all()
