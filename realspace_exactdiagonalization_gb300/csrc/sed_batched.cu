@@ -2007,6 +2007,12 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
   upload(B.fmask_dev, fmask, s);
   const int64_t tot = B.hop_records;
   DevBuf keyd((size_t)std::max<int64_t>(tot, 1) * 4);
+  // k_hop_fill writes the rows of the catalog only: the lanes past the last
+  // orbit in the last slice are set here to padding (zero record, no phase
+  // key), so the compaction below never reads what an allocation happened to
+  // hold
+  SED_CUDA(cudaMemsetAsync(keyd.p, 0xFF, (size_t)std::max<int64_t>(tot, 1) * 4, s));
+  SED_CUDA(cudaMemsetAsync(B.hop.p, 0, (size_t)std::max<int64_t>(tot, 1) * 8, s));
   if (G.stats == 1)
     k_hop_fill<true><<<grid, 256, 0, s>>>(n, C.reps.as<uint64_t>(), C.state.as<uint64_t>(), C.rank.dev.as<uint32_t>(),
                                           C.rank.rp, B.site_off.as<uint16_t>(), B.rec.as<uint32_t>(),
@@ -2025,22 +2031,34 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
   SED_CUDA(cudaMemcpyAsync(recs.data(), B.hop.p, (size_t)tot * 8, cudaMemcpyDeviceToHost, s));
   SED_CUDA(cudaMemcpyAsync(keys.data(), keyd.p, (size_t)tot * 4, cudaMemcpyDeviceToHost, s));
   SED_CUDA(cudaStreamSynchronize(s));
-  // compact the phase keys (first-appearance order) into phase ids
+  // compact the phase keys (first-appearance order) into phase ids; every
+  // descriptor is checked against the tables the kernel indexes with it
+  // (group element < |G|, class counts <= N_filled), so no key can reach
+  // outside them
   std::unordered_map<uint32_t, uint32_t> id;
   std::vector<uint32_t> desc;
   for (int64_t t = 0; t < tot; ++t) {
     if (keys[t] == 0xFFFFFFFFu) continue;
     auto it = id.find(keys[t]);
     if (it == id.end()) {
+      const uint32_t d = keys[t];
+      const int kf = C.n_filled;
+      SED_REQUIRE((int)(d & 0x3F) < G.n_ops && (int)((d >> 6) & 0x3F) <= kf && (int)((d >> 12) & 0x3F) <= kf &&
+                      (int)((d >> 18) & 0x3F) <= kf && (d >> 25) == 0,
+                  5, "internal error: hop-table phase key out of range");
       if ((int)desc.size() + 1 >= B.phi_cap) return false;
       it = id.emplace(keys[t], (uint32_t)desc.size()).first;
       desc.push_back(keys[t]);
     }
   }
   const uint64_t zero_id = desc.size();
+  const uint64_t n_tchi = (uint64_t)B.n_bil * G.n_ops;
   for (int64_t t = 0; t < tot; ++t) {
-    const uint64_t phi = keys[t] == 0xFFFFFFFFu ? zero_id : id[keys[t]];
-    recs[t] = (recs[t] & ((1ULL << 42) - 1)) | (phi << 42);
+    const bool pad = keys[t] == 0xFFFFFFFFu;
+    SED_REQUIRE(pad || ((recs[t] & 0xFFFFFFu) < (uint64_t)C.n_orbits && ((recs[t] >> 24) & 0x3FFFFu) < n_tchi), 5,
+                "internal error: hop-table record out of range");
+    const uint64_t phi = pad ? zero_id : id[keys[t]];
+    recs[t] = (pad ? 0 : recs[t] & ((1ULL << 42) - 1)) | (phi << 42);
   }
   SED_CUDA(cudaMemcpyAsync(B.hop.p, recs.data(), (size_t)tot * 8, cudaMemcpyHostToDevice, s));
   upload(B.phi_desc, desc, s);

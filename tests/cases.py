@@ -88,3 +88,27 @@ def x_ramp(n: int) -> np.ndarray:
 def x_random(n: int, seed: int = 7) -> np.ndarray:
     r = np.random.default_rng(seed)
     return r.standard_normal(n) + 1j * r.standard_normal(n)
+
+
+def assert_lanczos_spectrum(vals, ref, tol, msg=""):
+    """Lanczos semantics (the reference's KrylovKit branch, n > 500): every
+    returned value is an eigenvalue; the distinct returned values are exactly
+    the lowest distinct eigenvalues (none skipped), each copy at most as often
+    as its multiplicity.  A single-vector Krylov method may return an exactly
+    degenerate level fewer times than its multiplicity."""
+    distinct, mult = [], []
+    for e in ref:
+        if distinct and abs(e - distinct[-1]) <= 1e-8 * max(1.0, abs(e)):
+            mult[-1] += 1
+        else:
+            distinct.append(e)
+            mult.append(1)
+    got = []
+    for v in vals:
+        i = int(np.argmin([abs(v - d) for d in distinct]))
+        assert abs(v - distinct[i]) <= tol, (msg, v, distinct[:6])
+        got.append(i)
+    assert got == sorted(got), msg
+    assert sorted(set(got)) == list(range(len(set(got)))), (msg, got)
+    for i in set(got):
+        assert got.count(i) <= mult[i], (msg, got, mult[:6])

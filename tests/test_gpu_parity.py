@@ -8,7 +8,7 @@ diagonalisation of the oracle's matrix-mode sector block.
 import numpy as np
 import pytest
 
-from cases import case_by_name, oracle_objects, small_cases, x_ramp, x_random
+from cases import assert_lanczos_spectrum, case_by_name, oracle_objects, small_cases, x_ramp, x_random
 
 pytestmark = pytest.mark.gpu
 
@@ -114,30 +114,6 @@ def test_hop_table_matvec_matches_oracle(oracle, name, precision):
         assert np.abs(y - y_fly).max() <= (1e-13 if precision == "fp64" else 1e-6) * scale, (name, k, precision)
         H.set_hop_table(H.HOP_TABLE_OFF)
         assert not H.hop_table_info()["built"]
-
-
-def assert_lanczos_spectrum(vals, ref, tol, msg=""):
-    """Lanczos semantics (the reference's KrylovKit branch, n > 500): every
-    returned value is an eigenvalue; the distinct returned values are exactly
-    the lowest distinct eigenvalues (none skipped), each copy at most as often
-    as its multiplicity.  A single-vector Krylov method may return an exactly
-    degenerate level fewer times than its multiplicity."""
-    distinct, mult = [], []
-    for e in ref:
-        if distinct and abs(e - distinct[-1]) <= 1e-8 * max(1.0, abs(e)):
-            mult[-1] += 1
-        else:
-            distinct.append(e)
-            mult.append(1)
-    got = []
-    for v in vals:
-        i = int(np.argmin([abs(v - d) for d in distinct]))
-        assert abs(v - distinct[i]) <= tol, (msg, v, distinct[:6])
-        got.append(i)
-    assert got == sorted(got), msg
-    assert sorted(set(got)) == list(range(len(set(got)))), (msg, got)
-    for i in set(got):
-        assert got.count(i) <= mult[i], (msg, got, mult[:6])
 
 
 @pytest.mark.parametrize("name", CASES)
