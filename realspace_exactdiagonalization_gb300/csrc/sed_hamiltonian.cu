@@ -545,6 +545,15 @@ void op_apply_orbit(OpImpl& op, const void* xs, double* ypad, cudaStream_t s) {
   apply_impl(op, op.precision == 1, xs, ypad, s);
 }
 
+bool op_apply_orbit_df(OpImpl& op, const void* xs, double* ypad, cudaStream_t s) {
+  if (op.tab_built && op.precision == 1 && op.sec->cat->n_orbits > 0) {
+    apply_table(op, true, xs, ypad, s, true);
+    return true;
+  }
+  apply_impl(op, op.precision == 1, xs, ypad, s);
+  return false;
+}
+
 // FP64 matvec regardless of the op precision (the polish step of mixed solves)
 void op_apply_orbit64(OpImpl& op, const void* xs64, double* ypad, cudaStream_t s) {
   apply_impl(op, false, xs64, ypad, s);

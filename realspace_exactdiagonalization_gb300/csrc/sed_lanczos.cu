@@ -479,47 +479,65 @@ __global__ void k_df_normalize(int64_t n, const float4* __restrict__ w, const do
   }
 }
 
-// out_c = sum_l V_l S[l][c] for c in [c0, c0+8): complex FP64 coefficients
-// (row stride keep) split to double-float in shared memory
-__global__ void __launch_bounds__(kBS) k_df_rotate(int64_t n, const float4* __restrict__ V, int64_t ld, int msz,
-                                                   const double2* __restrict__ S, int keep, float4* __restrict__ out) {
-  __shared__ float4 sS[121 * 8];
-  const int c0 = blockIdx.y * 8;
-  const int cn = min(8, keep - c0);
-  for (int idx = threadIdx.x; idx < msz * 8; idx += blockDim.x) {
-    const int l = idx >> 3, c = idx & 7;
-    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (c < cn) {
-      const double2 v = S[(size_t)l * keep + c0 + c];
-      d_to_df(v.x, t.x, t.z);
-      d_to_df(v.y, t.y, t.w);
-    }
-    sS[idx] = t;
+// Restart rotation out[c] = sum_l V[l] Z[l][c], Z real (the Ritz vectors of
+// the real projected matrix) as double-float pairs, row-major [l][keep].
+// Block row blockIdx.y takes outputs [c0, c0 + cs): up to kRotCh outputs per
+// pass, so the basis is read ceil(keep / kRotCh) times, and a complex-by-real
+// product costs two double-float multiply-adds.
+// The chunk width CH is a template parameter, chosen per launch as the exact
+// chunk size: an unrolled loop guarded by a runtime count would issue its
+// masked-off iterations too.
+static constexpr int kRotCh = 16;
+template <int CH>
+__global__ void __launch_bounds__(kBS) k_df_rotate_re(int64_t n, const float4* __restrict__ V, int64_t ld, int msz,
+                                                      const float2* __restrict__ Z, int keep,
+                                                      float4* __restrict__ out) {
+  __shared__ float2 sZ[121 * CH];
+  const int c0 = blockIdx.y * CH;
+  const int cn = min(CH, keep - c0);
+  for (int idx = threadIdx.x; idx < msz * CH; idx += blockDim.x) {
+    const int l = idx / CH, c = idx % CH;
+    sZ[idx] = c < cn ? Z[(size_t)l * keep + c0 + c] : make_float2(0.f, 0.f);
   }
   __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    float4 acc[8];
+    float4 acc[CH];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int c = 0; c < CH; ++c) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int l = 0; l < msz; ++l) {
       const float4 v = V[(size_t)l * ld + i];
 #pragma unroll
-      for (int c = 0; c < 8; ++c)
-        if (c < cn) {
-          const float4 t = sS[l * 8 + c];
-          df_mac(acc[c].x, acc[c].z, v.x, v.z, t.x, t.z);
-          df_mac(acc[c].x, acc[c].z, -v.y, -v.w, t.y, t.w);
-          df_mac(acc[c].y, acc[c].w, v.x, v.z, t.y, t.w);
-          df_mac(acc[c].y, acc[c].w, v.y, v.w, t.x, t.z);
-        }
+      for (int c = 0; c < CH; ++c) {  // padding columns of the last chunk have z = 0
+        const float2 z = sZ[l * CH + c];
+        df_mac(acc[c].x, acc[c].z, v.x, v.z, z.x, z.y);
+        df_mac(acc[c].y, acc[c].w, v.y, v.w, z.x, z.y);
+      }
     }
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
+    for (int c = 0; c < CH; ++c)
       if (c < cn) {
         df_renorm(acc[c].x, acc[c].z);
         df_renorm(acc[c].y, acc[c].w);
         out[(size_t)(c0 + c) * ld + i] = acc[c];
       }
+  }
+}
+
+// out[0..keep) = V[0..msz) Z in ceil(keep / kRotCh) chunks of equal width
+static void df_rotate_re(int64_t n, const float4* V, int64_t ld, int msz, const float2* Z, int keep, float4* out,
+                         int gblk, cudaStream_t s) {
+  const int nch = (keep + kRotCh - 1) / kRotCh, cs = (keep + nch - 1) / nch;
+  const dim3 g(gblk, nch);
+  switch (cs) {
+#define SED_ROT(W) \
+  case W:          \
+    k_df_rotate_re<W><<<g, kBS, 0, s>>>(n, V, ld, msz, Z, keep, out); \
+    break;
+    SED_ROT(1) SED_ROT(2) SED_ROT(3) SED_ROT(4) SED_ROT(5) SED_ROT(6) SED_ROT(7) SED_ROT(8)
+    SED_ROT(9) SED_ROT(10) SED_ROT(11) SED_ROT(12) SED_ROT(13) SED_ROT(14) SED_ROT(15) SED_ROT(16)
+#undef SED_ROT
+    default:
+      SED_REQUIRE(false, 5, "internal error: rotation chunk width");
   }
 }
 
@@ -589,7 +607,7 @@ namespace {
 
 struct VecOps {
   int64_t n;
-  int nblk;
+  int nblk, nblk_dot;
   cudaStream_t s;
   DevBuf part, part1, coef, scal, flag;  // partial sums, coefficients, scalars, skip flag
   double* host = nullptr;          // pinned scratch
@@ -597,7 +615,13 @@ struct VecOps {
   VecOps(int64_t n_, cudaStream_t s_, bool df_) : n(n_), s(s_), df(df_) {
     const int64_t sms = device_sm_count();
     nblk = (int)std::max<int64_t>(1, std::min<int64_t>((n + kBS * 4 - 1) / (kBS * 4), sms * 4));
-    part.alloc((size_t)nblk * 130 * 16);
+    // the double-float dot kernel holds 80 registers a thread, so fewer of
+    // its blocks are resident: its grid is one full wave of them
+    int per_sm = 1;
+    SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_df_multidot, kBS, 0));
+    nblk_dot = (int)std::max<int64_t>(1, std::min<int64_t>((n + kBS * 4 - 1) / (kBS * 4),
+                                                            sms * std::max(per_sm, 1)));
+    part.alloc((size_t)std::max(nblk, nblk_dot) * 130 * 16);
     part1.alloc((size_t)nblk * 8);
     coef.alloc(256 * 16);
     scal.alloc(64);
@@ -617,15 +641,17 @@ struct VecOps {
   }
   // coef[off .. off+nv) (=|+=) V[0..nv)^H w
   void multidot(const double2* V, int64_t ld, int nv, const double2* w, int off, bool acc, bool fp64 = false) {
+    int nb = nblk;
     if (df && !fp64) {
-      dim3 g(nblk, (nv + 7) / 8);
+      nb = nblk_dot;
+      dim3 g(nb, (nv + 7) / 8);
       k_df_multidot<<<g, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(V), ld, nv,
                                        reinterpret_cast<const float4*>(w), part.as<double2>());
     } else {
-      dim3 g(nblk, nv);
+      dim3 g(nb, nv);
       k_multidot<<<g, kBS, 0, s>>>(n, V, ld, w, part.as<double2>());
     }
-    k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), nblk, coef.as<double2>() + off, acc ? 1 : 0);
+    k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), nb, coef.as<double2>() + off, acc ? 1 : 0);
   }
   // w -= V[0..nv) coef[off..], optionally scal[slot] = |w|^2
   // (skip: device flag of the selective reorthogonalisation, double-float only)
@@ -710,8 +736,10 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
   for (;;) {
     int jend = m;
     for (int j = k; j < m; ++j) {
-      op_apply_orbit(op, xs.p, (double*)W, s);
-      if (mixed) k_df_from_d<<<gblk, kBS, 0, s>>>(n, W);
+      if (!mixed)
+        op_apply_orbit(op, xs.p, (double*)W, s);
+      else if (!op_apply_orbit_df(op, xs.p, (double*)W, s))
+        k_df_from_d<<<gblk, kBS, 0, s>>>(n, W);
       // local step: CGS against the two newest basis vectors (they carry the
       // large alpha_j and beta_{j-1} components), then one full CGS pass
       // against the whole basis; a second full pass only when the first one
@@ -786,15 +814,25 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
     // iteration can resume if the FP64 check rejects it
     const bool final_rot = done && (!mixed || invariant);
     const int keep = final_rot ? std::min(nev, msz) : std::min(msz - 1, std::max(nev + (m - nev) / 2, nev + 1));
-    std::vector<double> Sc((size_t)msz * keep * 2, 0.0);
-    for (int l = 0; l < msz; ++l)
-      for (int c = 0; c < keep; ++c) Sc[((size_t)l * keep + c) * 2] = Z[(size_t)l * msz + c];
-    SED_CUDA(cudaMemcpyAsync(Sd.p, Sc.data(), Sc.size() * 8, cudaMemcpyHostToDevice, s));
-    if (mixed)
-      k_df_rotate<<<dim3(gblk, (keep + 7) / 8), kBS, 0, s>>>(n, reinterpret_cast<const float4*>(V), ld, msz,
-                                                             Sd.as<double2>(), keep, reinterpret_cast<float4*>(R));
-    else
+    if (mixed) {
+      std::vector<float> Zf((size_t)msz * keep * 2);  // real Ritz vectors as double-float pairs
+      for (int l = 0; l < msz; ++l)
+        for (int c = 0; c < keep; ++c) {
+          const double z = Z[(size_t)l * msz + c];
+          const float h = (float)z;
+          Zf[((size_t)l * keep + c) * 2] = h;
+          Zf[((size_t)l * keep + c) * 2 + 1] = (float)(z - (double)h);
+        }
+      SED_CUDA(cudaMemcpyAsync(Sd.p, Zf.data(), Zf.size() * 4, cudaMemcpyHostToDevice, s));
+      df_rotate_re(n, reinterpret_cast<const float4*>(V), ld, msz, Sd.as<float2>(), keep,
+                   reinterpret_cast<float4*>(R), gblk, s);
+    } else {
+      std::vector<double> Sc((size_t)msz * keep * 2, 0.0);
+      for (int l = 0; l < msz; ++l)
+        for (int c = 0; c < keep; ++c) Sc[((size_t)l * keep + c) * 2] = Z[(size_t)l * msz + c];
+      SED_CUDA(cudaMemcpyAsync(Sd.p, Sc.data(), Sc.size() * 8, cudaMemcpyHostToDevice, s));
       k_rotate<<<dim3(gblk, (keep + 7) / 8), kBS, 0, s>>>(n, V, ld, msz, Sd.as<double2>(), keep, R);
+    }
     SED_CUDA(cudaMemcpyAsync(V, R, (size_t)keep * ld * 16, cudaMemcpyDeviceToDevice, s));
     ops.check();
     if (!final_rot)  // the last normalised residual direction (slot m) continues the basis

@@ -28,6 +28,7 @@
 #include <complex>
 #include <vector>
 
+#include "sed_dfloat.cuh"
 #include "sed_internal.cuh"
 #include "sed_rowgather.cuh"
 
@@ -101,7 +102,9 @@ __global__ void k_optab_fill(int64_t n_orb, const uint64_t* __restrict__ reps, c
   }
 }
 
-template <class P>
+// DF: the row is stored as a double-float complex (re_hi, im_hi, re_lo,
+// im_lo), the form the mixed-precision Lanczos keeps its vectors in
+template <class P, bool DF = false>
 __global__ void __launch_bounds__(kTabBS) k_apply_tab(int64_t n_orb, const uint64_t* __restrict__ hop,
                                                       const int64_t* __restrict__ sl_off,
                                                       const int32_t* __restrict__ sl_w,
@@ -143,7 +146,15 @@ __global__ void __launch_bounds__(kTabBS) k_apply_tab(int64_t n_orb, const uint6
       ai = P::mad(cf.y, xc.x, ai);
     }
     const double is = s_isr[stab[o]];
-    y[o] = make_double2((double)ar * is, (double)ai * is);
+    const double yr = (double)ar * is, yi = (double)ai * is;
+    if (DF) {
+      float4 d;
+      d_to_df(yr, d.x, d.z);
+      d_to_df(yi, d.y, d.w);
+      reinterpret_cast<float4*>(y)[o] = d;
+    } else {
+      y[o] = make_double2(yr, yi);
+    }
   }
 }
 
@@ -258,7 +269,7 @@ void op_drop_table(OpImpl& op) {
   op.tab_records = op.tab_coefs = 0;
 }
 
-void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s) {
+void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s, bool df_out) {
   const SectorImpl& S = *op.sec;
   const CatalogImpl& C = *S.cat;
   const int64_t n = C.n_orbits;
@@ -269,7 +280,12 @@ void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream
   const size_t smem = (size_t)smem_coef * el;
   const int64_t want = (n + kTabBS - 1) / kTabBS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * 4));
-  if (fp32)
+  if (fp32 && df_out)
+    k_apply_tab<P32, true><<<grid, kTabBS, smem, s>>>(n, op.tab_hop.as<uint64_t>(), op.tab_off.as<int64_t>(),
+                                                      op.tab_w.as<int32_t>(), op.tab_coef32.as<float2>(), smem_coef,
+                                                      (const float2*)xs, op.diag.as<double2>(),
+                                                      S.rowflag.as<uint8_t>(), C.stab.as<uint8_t>(), (double2*)ypad);
+  else if (fp32)
     k_apply_tab<P32><<<grid, kTabBS, smem, s>>>(n, op.tab_hop.as<uint64_t>(), op.tab_off.as<int64_t>(),
                                                 op.tab_w.as<int32_t>(), op.tab_coef32.as<float2>(), smem_coef,
                                                 (const float2*)xs, op.diag.as<double2>(), S.rowflag.as<uint8_t>(),
