@@ -134,6 +134,27 @@ int sed_sector_expand_fock(const sed_sector* s, const double* c_reim, int64_t di
                            int64_t n_states, int is_device_ptr, double* norm2);
 void sed_sector_destroy(sed_sector* s);
 
+/* ------------------------------------------------- flux-torus observables */
+/* _position_operator_matrix (observables/charge_pump.jl:47-91): Resta's
+ * position operator U_d = exp(2 pi i X_d / L_d), given by its per-site phases
+ * site_phase_reim[n_site] (many_body_position_phases, charge_pump.jl:17-33),
+ * projected from sector `from` to sector `to` of the same catalog and group.
+ * U_d maps every orbit to itself, so column c of the (dim_to x dim_from)
+ * matrix has one entry: row_to[c] (0-based, -1 when the representative is
+ * not in `to` or the entry is below the reference's 1e-13 cut) with value
+ * elem_reim[c] = (1/|G|) sum_g chi_to(g) conj(chi_from(g)) prod_{j in g(rep)}
+ * phase_j.  Host output buffers of length dim_from. */
+int sed_position_operator(const sed_sector* to, const sed_sector* from, const double* site_phase_reim,
+                          int64_t* row_to, double* elem_reim);
+/* _subspace_overlap_matrix / _fock_amplitude_overlap
+ * (observables/many_body_chern_number.jl:46-71): m_reim[i * nb + j] =
+ * <a_i|b_j> = sum_s conj(a_i[s]) b_j[s] for na + nb dense Fock-amplitude
+ * vectors of n_states complex entries each (the layout of
+ * sed_sector_expand_fock, rows contiguous).  With is_device_ptr the inputs
+ * are device memory; m_reim is always host memory. */
+int sed_fock_overlaps(const double* a_reim, int na, const double* b_reim, int nb, int64_t n_states, int is_device_ptr,
+                      double* m_reim);
+
 /* --------------------------------------------------------------- operator */
 /* MatrixFreeHamiltonian (SRE:767-791) / hamiltonian_linear_operator
  * (SRE:891-897).  Bilinear term t moves a particle from site bil_ij[2k] to

@@ -10,5 +10,8 @@ raises if it has not been built.
 from .api import *  # noqa: F401,F403
 from .api import __all__ as _api_all
 from .lattice import build_translation_group, build_translation_irrep_list  # noqa: F401
+from .observables import (flux_charge_pump, many_body_chern_number,  # noqa: F401
+                          many_body_position_phases, position_operator_matrix)
 
-__all__ = list(_api_all) + ["build_translation_group", "build_translation_irrep_list"]
+__all__ = list(_api_all) + ["build_translation_group", "build_translation_irrep_list", "flux_charge_pump",
+                            "many_body_chern_number", "many_body_position_phases", "position_operator_matrix"]

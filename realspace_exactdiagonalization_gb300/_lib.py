@@ -61,6 +61,8 @@ SIGNATURES = [
     ("sed_sector_get", _i32, [_p, _p, _p, _p]),
     ("sed_sector_project", _i32, [_p, _i64, _p, _p, _p]),
     ("sed_sector_expand_fock", _i32, [_p, _p, _i64, _dbl, _p, _i64, _i32, _p]),
+    ("sed_position_operator", _i32, [_p, _p, _p, _p, _p]),
+    ("sed_fock_overlaps", _i32, [_p, C.c_int, _p, C.c_int, C.c_int64, C.c_int, _p]),
     ("sed_sector_destroy", None, [_p]),
     ("sed_op_create", _i32, [_p, _i32, _p, _p, _i32, _p, _p, _i32, _p]),
     ("sed_terms_validate", _i32, [_p, _i32, _p, _p]),

@@ -158,6 +158,17 @@ int sed_sector_expand_fock(const sed_sector* s, const double* c_reim, int64_t di
   });
 }
 void sed_sector_destroy(sed_sector* s) { delete s; }
+int sed_position_operator(const sed_sector* to, const sed_sector* from, const double* site_phase_reim,
+                          int64_t* row_to, double* elem_reim) {
+  return guarded([&] {
+    REQ(to && from, "NULL sector");
+    sed::position_operator(*to->p, *from->p, site_phase_reim, row_to, elem_reim);
+  });
+}
+int sed_fock_overlaps(const double* a_reim, int na, const double* b_reim, int nb, int64_t n_states, int is_device_ptr,
+                      double* m_reim) {
+  return guarded([&] { sed::fock_overlaps(a_reim, na, b_reim, nb, n_states, is_device_ptr, m_reim); });
+}
 
 int sed_op_create(const sed_sector* s, int n_bil, const int32_t* bil_ij, const double* bil_t_reim, int n_den,
                   const int32_t* den_ij, const double* den_v_reim, int precision, sed_op** out) {

@@ -202,6 +202,10 @@ void catalog_update_phases(CatalogImpl& c, std::shared_ptr<GroupImpl> g);
 std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> c, const double* chi, double atol,
                                          std::shared_ptr<GroupImpl> g = nullptr);
 void sector_readback(const SectorImpl& s, uint64_t* reps, int32_t* stab, int32_t* orbit);
+// flux-torus observables (sed_observables.cu)
+void position_operator(const SectorImpl& to, const SectorImpl& from, const double* site_phase, int64_t* row_out,
+                       double* elem_out);
+void fock_overlaps(const double* A, int na, const double* B, int nb, int64_t n, int is_device, double* M);
 void sector_project(const SectorImpl& s, int64_t n, const uint64_t* masks, int64_t* rows, double* coeff);
 void sector_expand_fock(const SectorImpl& S, const double* c, int64_t dim, double atol, double* out,
                         int64_t n_states, int is_device, double* norm2_out);

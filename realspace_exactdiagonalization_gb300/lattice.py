@@ -52,6 +52,12 @@ class Real_Space_Lattice:
     pbc_indicator: Tuple[bool, bool] = (True, True)
     name: str = ""
     twisted_phases_over_2pi: List[float] = field(default_factory=lambda: [0.0, 0.0])
+    # crystal coordinates of the sublattice sites inside a cell (``sub_crys_list``)
+    sub_crys_list: List[Tuple[float, float]] = field(default_factory=list)
+
+    def sub_crys(self, sub: int) -> Tuple[float, float]:
+        """Offset of sublattice ``sub`` (1-based); zero when none was given."""
+        return tuple(self.sub_crys_list[sub - 1]) if self.sub_crys_list else (0.0, 0.0)
 
     @property
     def n_site(self) -> int:
@@ -64,7 +70,8 @@ class Real_Space_Lattice:
 
 def initialize_real_space_lattice(sample_size: Sequence[int], n_sub: int, name: str = "",
                                   order: str = "cell_major",
-                                  pbc_indicator: Sequence[bool] = (True, True)) -> Real_Space_Lattice:
+                                  pbc_indicator: Sequence[bool] = (True, True),
+                                  sub_crys_list: Sequence[Sequence[float]] = ()) -> Real_Space_Lattice:
     """Number the sites of an ``L1 x L2`` sample with ``n_sub`` sublattices.
 
     ``order="cell_major"``: index = (x*L2 + y)*n_sub + sub; ``"sub_major"``:
@@ -86,7 +93,10 @@ def initialize_real_space_lattice(sample_size: Sequence[int], n_sub: int, name: 
     else:
         raise ValueError(f"unknown site order {order!r}")
     idx = {key: i + 1 for i, key in enumerate(sites)}
-    return Real_Space_Lattice((L1, L2), n_sub, sites, idx, tuple(bool(b) for b in pbc_indicator), name)
+    if sub_crys_list and len(sub_crys_list) != n_sub:
+        raise ValueError("sub_crys_list needs one offset per sublattice")
+    return Real_Space_Lattice((L1, L2), n_sub, sites, idx, tuple(bool(b) for b in pbc_indicator), name,
+                              sub_crys_list=[tuple(float(v) for v in c) for c in sub_crys_list])
 
 
 @dataclass
@@ -236,7 +246,7 @@ def heisenberg_ring(N: int, J: float = 1.0) -> ModelSpec:
 def haldane_honeycomb(L1: int, L2: int, t: float = 1.0, tp: float = 0.6, tpp: float = -0.58,
                       phi_over_2pi: float = 0.2, n_filled: int | None = None) -> ModelSpec:
     """Haldane honeycomb hard-core bosons (reference benchmark/benchmark.jl:114-152)."""
-    lat = initialize_real_space_lattice((L1, L2), 2, f"haldane{L1}x{L2}")
+    lat = initialize_real_space_lattice((L1, L2), 2, f"haldane{L1}x{L2}", sub_crys_list=[(0.0, 0.0), (1 / 3, 1 / 3)])
     tb = TightBindingModel(lat)
     s = 2 * math.pi * phi_over_2pi
     e = cmath.exp(1j * s)
@@ -262,7 +272,7 @@ def checkerboard(L1: int, L2: int, t: float = 1.0, tp1: float = 0.3, tp2: float 
                  n_filled: int | None = None, statistics: str = "fermionic") -> ModelSpec:
     """Checkerboard spinless fermions with staggered flux (reference
     phase_exploration/src/model.jl:1-71, bond list and density rules)."""
-    lat = initialize_real_space_lattice((L1, L2), 2, f"checkerboard{L1}x{L2}")
+    lat = initialize_real_space_lattice((L1, L2), 2, f"checkerboard{L1}x{L2}", sub_crys_list=[(0.5, 0.0), (0.0, 0.5)])
     tb = TightBindingModel(lat)
     ph = 2 * math.pi * phi_over_2pi
     add_hopping_term(tb, (((0, 0), 1), ((0, 0), 2)), -t * cmath.exp(-1j * ph))
