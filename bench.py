@@ -427,7 +427,7 @@ def run_large(args):
     stream = torch.cuda.current_stream()
     res = {}
     peak, peak_kind = measured_peak()
-    for prec in ("fp64", "mixed"):
+    for prec in (("fp64", "mixed") if args.large_precision == "both" else (args.large_precision,)):
         H = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms(), spec.density_terms, precision=prec)
         info = H.info()
         from realspace_exactdiagonalization_gb300 import _lib
@@ -571,6 +571,8 @@ def main():
     ap.add_argument("--large-shape", type=int, nargs=3, default=[4, 6, 8], metavar=("L1", "L2", "NP"))
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--large-model", default="checkerboard", choices=["checkerboard", "hubbard"])
+    ap.add_argument("--large-precision", default="both", choices=["both", "fp64", "mixed"],
+                    help="which precisions the large-sector workload measures")
     args = ap.parse_args()
     if args.workload == "large":
         run_large(args)

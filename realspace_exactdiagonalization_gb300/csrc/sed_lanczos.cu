@@ -380,6 +380,25 @@ __global__ void __launch_bounds__(kBS) k_df_norm2_part(int64_t n, const float4* 
 
 // part[l*nblk + b] = block b's share of conj(V_l) w for the 8 vectors of
 // chunk blockIdx.y: w is read once per 8 basis vectors
+// L2 prefetch of the vectors a grid-stride sweep reads: at each step, thread
+// t < nv of the block asks the TMA unit for its chunk of vector t two strides
+// ahead (cp.async.bulk.prefetch: no registers, nothing to wait for), so the
+// loads of the coming iterations find their lines in L2.  Used by the dot
+// kernel (eight vectors a block); for the update kernel, which sweeps all
+// basis vectors at once, the prefetched lines would crowd the L2 and it
+// measured slower.
+__device__ __forceinline__ void df_prefetch_ahead(const float4* V, int64_t ld, int nv, const float4* w, int64_t n,
+                                                  int64_t b, int64_t stride) {
+  const int t = threadIdx.x;
+  if (t > nv) return;
+  const int64_t pb = b + 2 * stride;
+  if (pb >= n) return;
+  const float4* p = t < nv ? V + (size_t)t * ld + pb : w + pb;
+  if (!p) return;
+  const uint32_t bytes = (uint32_t)min((int64_t)blockDim.x, n - pb) * 16u;
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 __global__ void __launch_bounds__(kBS) k_df_multidot(int64_t n, const float4* __restrict__ V, int64_t ld, int nv,
                                                      const float4* __restrict__ w, double2* __restrict__ part) {
   const int l0 = blockIdx.y * 8;
@@ -387,7 +406,11 @@ __global__ void __launch_bounds__(kBS) k_df_multidot(int64_t n, const float4* __
   float h[16], lo[16];
 #pragma unroll
   for (int c = 0; c < 16; ++c) h[c] = lo[c] = 0.f;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x; b < n; b += stride) {
+    df_prefetch_ahead(V + (size_t)l0 * ld, ld, cn, w, n, b, stride);
+    const int64_t i = b + threadIdx.x;
+    if (i >= n) continue;
     const float4 x = w[i];
 #pragma unroll
     for (int c = 0; c < 8; ++c)
