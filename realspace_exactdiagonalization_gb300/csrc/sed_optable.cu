@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kTabBS) k_apply_tab(int64_t n_orb, const uint6
     const V xo = xs[o];
     S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
     S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
-#pragma unroll 4
+#pragma unroll 8
     for (int k = 0; k < wdt; ++k) {
       const uint64_t r = __ldcs(reinterpret_cast<const unsigned long long*>(rp + 32 * (int64_t)k));
       const V cf = cf_tab[r >> kCBits];
@@ -278,8 +278,18 @@ void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream
   // (with the kernel's 520 bytes of static shared memory)
   const int smem_coef = op.tab_coefs * el <= 44 * 1024 ? (int)op.tab_coefs : 0;
   const size_t smem = (size_t)smem_coef * el;
+  // one full wave of resident blocks: the kernel is bound by the latency of
+  // its record and gather loads, so every resident warp helps
   const int64_t want = (n + kTabBS - 1) / kTabBS;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * 4));
+  int per_sm = 1;
+  if (fp32 && df_out)
+    SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_tab<P32, true>, kTabBS, smem));
+  else if (fp32)
+    SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_tab<P32>, kTabBS, smem));
+  else
+    SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_tab<P64>, kTabBS, smem));
+  const int grid =
+      (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * std::max(per_sm, 1)));
   if (fp32 && df_out)
     k_apply_tab<P32, true><<<grid, kTabBS, smem, s>>>(n, op.tab_hop.as<uint64_t>(), op.tab_off.as<int64_t>(),
                                                       op.tab_w.as<int32_t>(), op.tab_coef32.as<float2>(), smem_coef,
