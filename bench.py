@@ -525,7 +525,7 @@ def run_served(args):
     plain_ev = {}
     for name in sorted(fams):
         sample = [r for r in done if r.family == name][: args.plain_per_family]
-        times = []
+        times, mixed_times = [], []
         fam = srv.families[name]
         for r in sample:
             G = L.build_translation_group(fam.spec.lattice, r.twist)
@@ -538,8 +538,22 @@ def run_served(args):
                 plain_ev[r.rid] = vals[0]
                 del H
             times.append(time.perf_counter() - t1)
+            if fam.route == "large" and basis.dim:
+                # the same request alone through the served large route's mixed solve
+                t1 = time.perf_counter()
+                basis = A.build_symmetry_sector_basis(fam.catalog, irr, group=G)
+                H = A.MatrixFreeHamiltonian(basis, fam.spec.bilinear_terms(r.twist), fam.spec.density_terms,
+                                            precision="mixed")
+                H.solve(1, tol=1e-10, seed=r.seed, want_vectors=False)
+                del H
+                mixed_times.append(time.perf_counter() - t1)
+        mine = [r for r in done if r.family == name]
         per_fam[name] = {"plain_fp64_s": float(np.mean(times)) if times else None, "route": fam.route,
-                         "n_orbits": fam.n_orbits, "served": sum(1 for r in done if r.family == name)}
+                         "n_orbits": fam.n_orbits, "served": len(mine),
+                         # time from the start of the request's solve (or of its batch) to its answer
+                         "mean_service_s": float(np.mean([r.t_end - r.t_start for r in mine])) if mine else None,
+                         "mean_wait_s": float(np.mean([r.t_start - r.arrival for r in mine])) if mine else None,
+                         "mixed_alone_s": float(np.mean(mixed_times)) if mixed_times else None}
     mix_s = np.mean([per_fam[r.family]["plain_fp64_s"] for r in done])
     rel = [abs(done[i].evals[0] - e) / abs(e) for i, e in plain_ev.items()]
     line = {"workload": "served_config5", "requests": len(done), "rate_per_s": args.served_rate,
