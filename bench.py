@@ -462,7 +462,8 @@ def run_large(args):
         t_fly = time_matvec()
         b_alg = info["dim"] * (8 + 4 + 2 * s) + info["hops"] * (4 + 1 + 4 + s)
         r = {"matvec_ms": 1e3 * t_fly, "bytes_alg": b_alg, "achieved_gbs": b_alg / t_fly / 1e9,
-             "frac": b_alg / t_fly / 1e9 / peak, "hops": info["hops"]}
+             "frac": b_alg / t_fly / 1e9 / peak, "hops": info["hops"],
+             "gather_shape_threads_per_row_block": list(H.apply_shape(prec == "mixed"))}
         # the stored hop table (8 bytes per hop, streamed)
         torch.cuda.synchronize()
         t0 = time.perf_counter()

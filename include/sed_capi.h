@@ -172,6 +172,17 @@ int sed_terms_validate(const sed_group* g, int n_bil, const int32_t* bil_ij, con
  * is_device_ptr the pointers are device memory on this op's stream; the call
  * is then asynchronous. */
 int sed_op_apply(sed_op* op, const double* x_reim, double* y_reim, int64_t n, int is_device_ptr);
+/* Launch shape of the matrix-free gather (no reference counterpart): threads
+ * per row (1, 2, 4 or 8 lanes of a warp split a row's hops) and threads per
+ * block (256 or 512).  By default an autotuner times all eight shapes on an
+ * operator's first gather matvec, per precision, and keeps the fastest,
+ * remembered per catalog shape for the process; the environment variable
+ * SED_APPLY_SHAPE="tpr,block" pins one.  sed_op_set_apply_shape pins a shape
+ * for this operator ((0, 0) lets the autotuner choose again);
+ * sed_op_apply_shape reports the shape in use (0, 0 before the first gather).
+ * The shape changes results only through the order of a row's sum. */
+int sed_op_set_apply_shape(sed_op* op, int threads_per_row, int threads_per_block);
+int sed_op_apply_shape(const sed_op* op, int complex64, int* threads_per_row, int* threads_per_block);
 /* dim = sector dimension, n_orbits = length of the orbit-indexed device
  * vectors, hops = valid hops one matvec evaluates (counted on the device). */
 int sed_op_info(const sed_op* op, int64_t* dim, int64_t* n_orbits, int64_t* hops);
@@ -252,6 +263,10 @@ int sed_batch_last_stats(const sed_batch* b, int64_t* hops, int64_t* t_start_ns,
  * precision target (0 for SED_PREC_FP64), whether the matvecs streamed the hop
  * table, and its size in 8-byte records. */
 int sed_batch_last_info(const sed_batch* b, int32_t* n_fallback, int32_t* hop_table, int64_t* hop_records);
+/* The batch launch (request-queue reset + persistent kernel) is a CUDA graph,
+ * captured once per launch configuration and replayed while it repeats:
+ * how many captures and replays this batch object has made. */
+int sed_batch_graph_info(const sed_batch* b, int32_t* captures, int32_t* replays);
 /* The hop table (on by default): the requests of a batch share the catalog and
  * the (i, j) term list, hence every sector matrix's sparsity pattern, which is
  * enumerated once into 8-byte records (column orbit, term x group element,

@@ -67,6 +67,8 @@ SIGNATURES = [
     ("sed_op_create", _i32, [_p, _i32, _p, _p, _i32, _p, _p, _i32, _p]),
     ("sed_terms_validate", _i32, [_p, _i32, _p, _p]),
     ("sed_op_apply", _i32, [_p, _p, _p, _i64, _i32]),
+    ("sed_op_set_apply_shape", _i32, [_p, _i32, _i32]),
+    ("sed_op_apply_shape", _i32, [_p, _i32, _p, _p]),
     ("sed_op_info", _i32, [_p, _p, _p, _p]),
     ("sed_op_set_hop_table", _i32, [_p, _i32]),
     ("sed_op_hop_table_info", _i32, [_p, _p, _p, _p]),
@@ -79,6 +81,7 @@ SIGNATURES = [
     ("sed_batch_run", _i32, [_p, _i32, _p, _p, _p, _p, _dbl, _i32, _p, _p, _p, _p, _p]),
     ("sed_batch_last_stats", _i32, [_p, _p, _p, _p]),
     ("sed_batch_last_info", _i32, [_p, _p, _p, _p]),
+    ("sed_batch_graph_info", _i32, [_p, _p, _p]),
     ("sed_batch_set_hop_table", _i32, [_p, _i32]),
     ("sed_batch_run_device", _i32, [_p, _i32, _p, _p, _p, _p, _dbl, _i32, _p, _p, _p, _p, _p]),
     ("sed_batch_set_stream", _i32, [_p, _p]),

@@ -375,6 +375,16 @@ class MatrixFreeHamiltonian(_Handle):
 
     HOP_TABLE_OFF, HOP_TABLE_AUTO, HOP_TABLE_NOW = 0, 1, 2
 
+    def set_apply_shape(self, threads_per_row: int = 0, threads_per_block: int = 0) -> None:
+        """Pin the gather matvec's launch shape ((0, 0): let the autotuner choose)."""
+        check(_lib.load().sed_op_set_apply_shape(self._h, int(threads_per_row), int(threads_per_block)))
+
+    def apply_shape(self, complex64: bool = False) -> tuple:
+        """(threads per row, threads per block) of the gather matvec; (0, 0) before the first gather."""
+        t, b = C.c_int(0), C.c_int(0)
+        check(_lib.load().sed_op_apply_shape(self._h, int(bool(complex64)), C.byref(t), C.byref(b)))
+        return t.value, b.value
+
     def set_hop_table(self, mode: int) -> None:
         """The stored form of this operator's matvec (8 bytes per hop): 0 off,
         1 built at the first solve when it fits (default), 2 built now."""

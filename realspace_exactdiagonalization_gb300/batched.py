@@ -115,8 +115,11 @@ class BatchedSectorSolver:
         check(_lib.load().sed_batch_last_stats(self._h, ptr(hops), ptr(t0), ptr(t1)))
         nf, tab, nrec = C.c_int32(0), C.c_int32(0), C.c_int64(0)
         check(_lib.load().sed_batch_last_info(self._h, C.byref(nf), C.byref(tab), C.byref(nrec)))
+        caps, reps = C.c_int32(0), C.c_int32(0)
+        check(_lib.load().sed_batch_graph_info(self._h, C.byref(caps), C.byref(reps)))
         return {"hops": hops, "t_start_ns": t0, "t_end_ns": t1, "fp64_fallbacks": int(nf.value),
-                "hop_table": bool(tab.value), "hop_records": int(nrec.value)}
+                "hop_table": bool(tab.value), "hop_records": int(nrec.value),
+                "graph_captures": int(caps.value), "graph_replays": int(reps.value)}
 
     def set_hop_table(self, enable: bool) -> None:
         """Stream the shared hop table (default) or derive every hop on the fly."""

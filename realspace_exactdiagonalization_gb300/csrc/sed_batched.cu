@@ -1721,7 +1721,21 @@ struct BatchImpl {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   bool fermi = false;
+  // the captured launch (queue reset + persistent kernel) and the launch
+  // configuration it was captured for
+  std::vector<unsigned char> graph_key;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_captures = 0, graph_replays = 0;
+  void drop_graph() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    graph_exec = nullptr;
+    graph = nullptr;
+    graph_key.clear();
+  }
   ~BatchImpl() {
+    drop_graph();
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
@@ -1821,6 +1835,47 @@ static void dispatch_launch(BatchImpl& B, const BatchArgs& a, const BatchSmem& L
     if (B.fermi) batch_launch<P64, true, true, false>(a, L, ncta, s);
     else batch_launch<P64, false, true, false>(a, L, ncta, s);
   }
+}
+
+// One batch launch -- the request-queue reset and the persistent kernel -- as
+// a CUDA graph: captured the first time a launch configuration is seen
+// (kernel arguments, shared-memory layout, grid, precision), replayed with
+// cudaGraphLaunch while it repeats, as it does for every step of a flux scan
+// or a serving lane.  Capture is thread-local, so host threads that allocate
+// or launch on other streams meanwhile are not affected.
+static void graph_launch(BatchImpl& B, const BatchArgs& a, const BatchSmem& L, int ncta, cudaStream_t s, bool fp64) {
+  std::vector<unsigned char> key(sizeof(BatchArgs) + sizeof(BatchSmem) + 2 * sizeof(int));
+  std::memcpy(key.data(), &a, sizeof(BatchArgs));
+  std::memcpy(key.data() + sizeof(BatchArgs), &L, sizeof(BatchSmem));
+  const int tail[2] = {ncta, fp64 ? 1 : 0};
+  std::memcpy(key.data() + sizeof(BatchArgs) + sizeof(BatchSmem), tail, sizeof(tail));
+  if (!B.graph_exec || key != B.graph_key) {
+    B.drop_graph();
+    cudaGraph_t g = nullptr;
+    SED_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      SED_CUDA(cudaMemsetAsync(B.queue.p, 0, 16, s));
+      dispatch_launch(B, a, L, ncta, s, fp64);
+    } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    SED_CUDA(cudaStreamEndCapture(s, &g));
+    cudaGraphExec_t x = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&x, g, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      SED_CUDA(e);
+    }
+    B.graph = g;
+    B.graph_exec = x;
+    B.graph_key.swap(key);
+    ++B.graph_captures;
+  } else {
+    ++B.graph_replays;
+  }
+  SED_CUDA(cudaGraphLaunch(B.graph_exec, s));
 }
 
 // ------------------------------------------------------------ hop table
@@ -2219,7 +2274,6 @@ void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const doubl
   B.n_fallback = 0;
   if (n_req == 0) return;
   cudaStream_t s = B.stream;
-  SED_CUDA(cudaMemsetAsync(B.queue.p, 0, 16, s));
   BatchArgs a = base_args(B);
   a.n_req = n_req;
   a.tol = tol;
@@ -2266,7 +2320,7 @@ void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const doubl
   int ncta = 1;
   dispatch_prepare(B, a, L, ncta, B.precision == 0);
   ncta = std::min(B.n_cta, n_req);
-  dispatch_launch(B, a, L, ncta, s, B.precision == 0);
+  graph_launch(B, a, L, ncta, s, B.precision == 0);
   if (B.precision == 1) {
     // requests whose FP64 polish missed its residual target are answered by
     // the all-FP64 kernel (same inputs, same seed), so no unconverged pair is
@@ -2434,6 +2488,13 @@ int sed_batch_info(const sed_batch* b, int64_t* smem_bytes, int64_t* n_blocks, i
   });
 }
 
+int sed_batch_graph_info(const sed_batch* b, int* captures, int* replays) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    if (captures) *captures = b->p->graph_captures;
+    if (replays) *replays = b->p->graph_replays;
+  });
+}
 void sed_batch_destroy(sed_batch* b) { delete b; }
 
 }  // extern "C"

@@ -188,6 +188,20 @@ int sed_terms_validate(const sed_group* g, int n_bil, const int32_t* bil_ij, con
     sed::check_hermitian_symmetric(*g->p, n_bil, bil_ij, bil_t_reim);
   });
 }
+int sed_op_set_apply_shape(sed_op* op, int threads_per_row, int threads_per_block) {
+  return guarded([&] {
+    REQ(op, "NULL operator");
+    sed::op_set_apply_shape(*op->p, threads_per_row, threads_per_block);
+  });
+}
+int sed_op_apply_shape(const sed_op* op, int complex64, int* threads_per_row, int* threads_per_block) {
+  return guarded([&] {
+    REQ(op, "NULL operator");
+    const int k = complex64 ? 1 : 0;
+    if (threads_per_row) *threads_per_row = op->p->apply_tpr[k];
+    if (threads_per_block) *threads_per_block = op->p->apply_block[k];
+  });
+}
 int sed_op_apply(sed_op* op, const double* x_reim, double* y_reim, int64_t n, int is_device_ptr) {
   return guarded([&] {
     REQ(op, "NULL operator");

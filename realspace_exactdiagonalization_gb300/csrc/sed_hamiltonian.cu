@@ -16,6 +16,9 @@
 // where tchi[u][h] = conj(t_u) chi(h) is tabulated per distinct amplitude u and
 // P_h(new) is the per-site phase product of a flux-twisted group (1 otherwise).
 #include <algorithm>
+#include <cstdlib>
+#include <cstdio>
+#include <tuple>
 #include <cmath>
 #include <complex>
 #include <map>
@@ -241,7 +244,10 @@ struct SmemLayout {
 // resident blocks per SM, i.e. 1536 threads keeping random loads in flight.
 static constexpr int kApplyBS = 512;
 
-template <class P, bool FERMI, bool PHASES, bool TABLE>
+// TPR threads per row (1, 2, 4 or 8 lanes of one warp); the block size, and
+// so the rows per block, is the launch's.  Both are picked per operator by the
+// autotuner in launch_apply.
+template <class P, bool FERMI, bool PHASES, bool TABLE, int TPR>
 __global__ void __launch_bounds__(kApplyBS) k_apply(ApplyArgs a, SmemLayout<typename P::V> L,
                                                const typename P::V* __restrict__ xs, double2* __restrict__ y) {
   using V = typename P::V;
@@ -276,19 +282,56 @@ __global__ void __launch_bounds__(kApplyBS) k_apply(ApplyArgs a, SmemLayout<type
   __syncthreads();
   const V* __restrict__ eta = reinterpret_cast<const V*>(a.eta);
   const PhaseClasses<V> pcl{a.phase_mode, a.kp1, s_mask, s_pw};
-  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < a.n_orb; o += (int64_t)gridDim.x * blockDim.x) {
-    if (!a.rowflag[o]) {
-      y[o] = make_double2(0.0, 0.0);
-      continue;
+  if (TPR == 1) {
+    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < a.n_orb;
+         o += (int64_t)gridDim.x * blockDim.x) {
+      if (!a.rowflag[o]) {
+        y[o] = make_double2(0.0, 0.0);
+        continue;
+      }
+      const double2 dg = a.diag[o];
+      const V xo = xs[o];
+      S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
+      S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
+      row_gather<P, FERMI, PHASES, TABLE>(a.reps[o], xs, s_tchi, s_chi, a.G, eta, a.N, s_rank, a.rp, s_rec, s_off,
+                                          s_inv, a.state, ar, ai, pcl);
+      const double is = s_isr[a.stab[o]];
+      y[o] = make_double2((double)ar * is, (double)ai * is);
     }
-    const double2 dg = a.diag[o];
-    const V xo = xs[o];
-    S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
-    S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
-    row_gather<P, FERMI, PHASES, TABLE>(a.reps[o], xs, s_tchi, s_chi, a.G, eta, a.N, s_rank, a.rp, s_rec, s_off,
-                                        s_inv, a.state, ar, ai, pcl);
-    const double is = s_isr[a.stab[o]];
-    y[o] = make_double2((double)ar * is, (double)ai * is);
+    return;
+  }
+  // TPR consecutive lanes share a row; their partial sums meet by shuffles
+  // within the group, and lane 0 of the group adds the diagonal and stores
+  const int q = threadIdx.x % TPR;
+  const unsigned gmask = ((1u << TPR) - 1u) << ((threadIdx.x & 31) & ~(TPR - 1));
+  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / TPR;
+  for (int64_t o = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TPR; o < a.n_orb; o += ngrp) {
+    const bool on = a.rowflag[o] != 0;
+    S ar = 0, ai = 0;
+    if (on) {
+      if (q == 0) {
+        const double2 dg = a.diag[o];
+        const V xo = xs[o];
+        ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
+        ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
+      }
+      row_gather_split<P, FERMI, PHASES, TABLE>(a.reps[o], q, TPR, xs, s_tchi, s_chi, a.G, eta, a.N, s_rank, a.rp,
+                                                s_rec, s_off, a.state, ar, ai, pcl);
+    }
+    __syncwarp(gmask);
+#pragma unroll
+    for (int off = TPR / 2; off > 0; off >>= 1) {
+      ar += __shfl_xor_sync(gmask, ar, off);
+      ai += __shfl_xor_sync(gmask, ai, off);
+    }
+    if (q == 0) {
+      if (on) {
+        const double is = s_isr[a.stab[o]];
+        y[o] = make_double2((double)ar * is, (double)ai * is);
+      } else {
+        y[o] = make_double2(0.0, 0.0);
+      }
+    }
   }
 }
 
@@ -480,11 +523,20 @@ static ApplyArgs make_args(const OpImpl& op, bool fp32) {
   return a;
 }
 
-template <class P, bool F, bool PH, bool T>
-static void launch_apply(const ApplyArgs& a, const void* xs, double* y, cudaStream_t s) {
+// ------------------------------------------------------------ launch shape
+// The gather's launch shape -- threads per row and threads (so rows) per
+// block -- is chosen per operator by measurement (apply_shape below).
+struct ApplyShape {
+  int tpr, block;
+};
+static constexpr ApplyShape kApplyShapes[] = {{1, 512}, {1, 256}, {2, 512}, {2, 256},
+                                              {4, 512}, {4, 256}, {8, 512}, {8, 256}};
+
+template <class P, bool F, bool PH, bool T, int TPR>
+static void launch_apply_tpr(const ApplyArgs& a, const void* xs, double* y, cudaStream_t s, int block) {
   using V = typename P::V;
   const SmemLayout<V> L = SmemLayout<V>::make(a, T);
-  auto kern = k_apply<P, F, PH, T>;
+  auto kern = k_apply<P, F, PH, T, TPR>;
   SED_REQUIRE(L.total <= 200 * 1024, 5, "operator tables exceed the shared-memory budget");
   // the shared-memory opt-in is a property of the kernel, shared by every
   // operator: raise it (never lower it) and launch under one lock, so a
@@ -497,34 +549,139 @@ static void launch_apply(const ApplyArgs& a, const void* xs, double* y, cudaStre
     configured = L.total;
   }
   int blocks_per_sm = 0;
-  SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kApplyBS, L.total));
+  SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, block, L.total));
   blocks_per_sm = std::max(blocks_per_sm, 1);
-  const int64_t want = (a.n_orb + kApplyBS - 1) / kApplyBS;
+  const int64_t rows_per_block = block / TPR;
+  const int64_t want = (a.n_orb + rows_per_block - 1) / rows_per_block;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * blocks_per_sm));
-  kern<<<grid, kApplyBS, L.total, s>>>(a, L, reinterpret_cast<const V*>(xs), reinterpret_cast<double2*>(y));
+  kern<<<grid, block, L.total, s>>>(a, L, reinterpret_cast<const V*>(xs), reinterpret_cast<double2*>(y));
   SED_CUDA(cudaGetLastError());
+}
+
+template <class P, bool F, bool PH, bool T>
+static void launch_apply(const ApplyArgs& a, const void* xs, double* y, cudaStream_t s, ApplyShape sh) {
+  switch (sh.tpr) {
+    case 1: launch_apply_tpr<P, F, PH, T, 1>(a, xs, y, s, sh.block); break;
+    case 2: launch_apply_tpr<P, F, PH, T, 2>(a, xs, y, s, sh.block); break;
+    case 4: launch_apply_tpr<P, F, PH, T, 4>(a, xs, y, s, sh.block); break;
+    case 8: launch_apply_tpr<P, F, PH, T, 8>(a, xs, y, s, sh.block); break;
+    default: SED_REQUIRE(false, 1, "threads per row must be 1, 2, 4 or 8");
+  }
 }
 
 template <class P>
 static void dispatch_apply(const ApplyArgs& a, bool fermi, bool phases, bool table, const void* xs, double* y,
-                           cudaStream_t s) {
+                           cudaStream_t s, ApplyShape sh) {
   if (fermi) {
     if (phases) {
-      if (table) launch_apply<P, true, true, true>(a, xs, y, s);
-      else launch_apply<P, true, true, false>(a, xs, y, s);
+      if (table) launch_apply<P, true, true, true>(a, xs, y, s, sh);
+      else launch_apply<P, true, true, false>(a, xs, y, s, sh);
     } else {
-      if (table) launch_apply<P, true, false, true>(a, xs, y, s);
-      else launch_apply<P, true, false, false>(a, xs, y, s);
+      if (table) launch_apply<P, true, false, true>(a, xs, y, s, sh);
+      else launch_apply<P, true, false, false>(a, xs, y, s, sh);
     }
   } else {
     if (phases) {
-      if (table) launch_apply<P, false, true, true>(a, xs, y, s);
-      else launch_apply<P, false, true, false>(a, xs, y, s);
+      if (table) launch_apply<P, false, true, true>(a, xs, y, s, sh);
+      else launch_apply<P, false, true, false>(a, xs, y, s, sh);
     } else {
-      if (table) launch_apply<P, false, false, true>(a, xs, y, s);
-      else launch_apply<P, false, false, false>(a, xs, y, s);
+      if (table) launch_apply<P, false, false, true>(a, xs, y, s, sh);
+      else launch_apply<P, false, false, false>(a, xs, y, s, sh);
     }
   }
+}
+
+// The autotuner: the first gather matvec of an operator (per precision)
+// times every shape of kApplyShapes on the operator's own input, one warm-up
+// and two timed launches each (CUDA events on the operator's stream; the trial
+// launches write the caller's output, which the chosen launch then
+// overwrites), and keeps the fastest.  The choice is remembered per catalog
+// shape (orbits, sites, filling, group order, hop records, precision,
+// statistics, twist phases, coefficient placement) for the whole process,
+// so later operators of the same family do not retune.  SED_APPLY_SHAPE=
+// "tpr,block" in the environment, or sed_op_set_apply_shape, pins a shape.
+// Results depend on the shape only through the order in which a row's hops
+// are summed (the row split over tpr lanes).
+struct ShapeKey {
+  int64_t n_orb;
+  int n_site, n_filled, n_ops, n_terms, fp32, fermi, phases, table;
+  bool operator<(const ShapeKey& o) const {
+    return std::tie(n_orb, n_site, n_filled, n_ops, n_terms, fp32, fermi, phases, table) <
+           std::tie(o.n_orb, o.n_site, o.n_filled, o.n_ops, o.n_terms, o.fp32, o.fermi, o.phases, o.table);
+  }
+};
+static std::mutex g_shape_mu;
+static std::map<ShapeKey, ApplyShape> g_shapes;
+
+static bool env_shape(ApplyShape* out) {
+  const char* e = std::getenv("SED_APPLY_SHAPE");
+  if (!e) return false;
+  int t = 0, b = 0;
+  if (std::sscanf(e, "%d,%d", &t, &b) != 2) return false;
+  for (const ApplyShape& sh : kApplyShapes)
+    if (sh.tpr == t && sh.block == b) {
+      *out = sh;
+      return true;
+    }
+  return false;
+}
+
+template <class P>
+static ApplyShape apply_shape(OpImpl& op, const ApplyArgs& a, bool fp32, const void* xs, double* ypad,
+                              cudaStream_t s) {
+  const int k = fp32 ? 1 : 0;
+  if (op.apply_tpr[k] > 0) return ApplyShape{op.apply_tpr[k], op.apply_block[k]};
+  ApplyShape best{1, 512};
+  const GroupImpl& G = *op.sec->group;
+  const bool fermi = G.stats == 1, phases = G.has_phases, table = op.tchi_in_smem;
+  const ShapeKey key{a.n_orb, a.N, op.sec->cat->n_filled, a.G, a.n_terms, k, fermi, phases, table};
+  bool found = env_shape(&best);
+  if (!found) {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    auto it = g_shapes.find(key);
+    if (it != g_shapes.end()) {
+      best = it->second;
+      found = true;
+    }
+  }
+  if (!found) {
+    cudaEvent_t e0, e1;
+    SED_CUDA(cudaEventCreate(&e0));
+    SED_CUDA(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    for (const ApplyShape& sh : kApplyShapes) {
+      dispatch_apply<P>(a, fermi, phases, table, xs, ypad, s, sh);
+      SED_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < 2; ++r) dispatch_apply<P>(a, fermi, phases, table, xs, ypad, s, sh);
+      SED_CUDA(cudaEventRecord(e1, s));
+      SED_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      SED_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = sh;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    g_shapes[key] = best;
+  }
+  op.apply_tpr[k] = best.tpr;
+  op.apply_block[k] = best.block;
+  return best;
+}
+
+void op_set_apply_shape(OpImpl& op, int tpr, int block) {
+  if (tpr == 0 && block == 0) {  // choose again
+    op.apply_tpr[0] = op.apply_tpr[1] = 0;
+    return;
+  }
+  bool ok = false;
+  for (const ApplyShape& sh : kApplyShapes) ok = ok || (sh.tpr == tpr && sh.block == block);
+  SED_REQUIRE(ok, 1, "apply shape must be (1|2|4|8 threads per row, 256|512 threads per block)");
+  op.apply_tpr[0] = op.apply_tpr[1] = tpr;
+  op.apply_block[0] = op.apply_block[1] = block;
 }
 
 static void apply_impl(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s) {
@@ -536,9 +693,11 @@ static void apply_impl(OpImpl& op, bool fp32, const void* xs, double* ypad, cuda
   }
   const ApplyArgs a = make_args(op, fp32);
   if (fp32)
-    dispatch_apply<P32>(a, G.stats == 1, G.has_phases, op.tchi_in_smem, xs, ypad, s);
+    dispatch_apply<P32>(a, G.stats == 1, G.has_phases, op.tchi_in_smem, xs, ypad, s,
+                        apply_shape<P32>(op, a, true, xs, ypad, s));
   else
-    dispatch_apply<P64>(a, G.stats == 1, G.has_phases, op.tchi_in_smem, xs, ypad, s);
+    dispatch_apply<P64>(a, G.stats == 1, G.has_phases, op.tchi_in_smem, xs, ypad, s,
+                        apply_shape<P64>(op, a, false, xs, ypad, s));
 }
 
 void op_apply_orbit(OpImpl& op, const void* xs, double* ypad, cudaStream_t s) {

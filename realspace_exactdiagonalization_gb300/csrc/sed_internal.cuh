@@ -187,8 +187,12 @@ struct OpImpl {
   bool tab_built = false, tab_refused = false;
   DevBuf tab_hop, tab_off, tab_w, tab_coef64, tab_coef32;
   int64_t tab_records = 0, tab_coefs = 0;
+  // the gather matvec's launch shape per precision [FP64, complex64]: threads
+  // per row and threads per block (0: not chosen yet; the autotuner decides)
+  int apply_tpr[2] = {0, 0}, apply_block[2] = {0, 0};
   ~OpImpl();
 };
+void op_set_apply_shape(OpImpl& op, int tpr, int block);
 bool op_build_table(OpImpl& op);
 void op_drop_table(OpImpl& op);
 void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s, bool df_out = false);

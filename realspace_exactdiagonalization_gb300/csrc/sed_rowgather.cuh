@@ -167,4 +167,75 @@ __device__ __forceinline__ void row_gather(uint64_t m, const typename P::V* __re
   }
 }
 
+// The same row split over TPR lanes: lane q of the row's group takes the
+// hops whose index in the row's hop order is q mod TPR (the enumeration itself
+// is cheap; the rank lookup, state word, gather and multiply-adds are not).
+// The lanes' partial sums are combined by the caller.
+template <class P, bool FERMI, bool PHASES, bool TABLE>
+__device__ __forceinline__ void row_gather_split(uint64_t m, int q, int tpr, const typename P::V* __restrict__ xs,
+                                                 const typename P::V* tab, const typename P::V* chi, int G,
+                                                 const typename P::V* __restrict__ eta, int N,
+                                                 const uint32_t* s_rank, const RankParams& rp,
+                                                 const uint32_t* s_rec, const uint16_t* s_off,
+                                                 const uint64_t* __restrict__ state, typename P::S& ar,
+                                                 typename P::S& ai, const PhaseClasses<typename P::V>& pc) {
+  using V = typename P::V;
+  using S = typename P::S;
+  HopIter it;
+  it.init(m, s_off);
+  uint32_t rec;
+  int i;
+  int t = 0;
+  while (it.next(s_off, s_rec, rec, i)) {
+    if ((t++ % tpr) != q) continue;
+    const int j = rec & 0xFF;
+    const uint64_t nw = m ^ ((1ULL << i) | (1ULL << j));
+    const uint64_t w = __ldg(state + dev::rank_of(nw, s_rank, rp));
+    const uint32_t c = (uint32_t)w;
+    int neg = (int)((w >> 40) & 1);
+    const V xc = xs[c];
+    const int h = (int)((w >> 48) & 0xFF);
+    const int u = (int)(rec >> 8);
+    V cf;
+    if (TABLE) {
+      cf = tab[u * G + h];
+    } else {
+      const V tt = tab[u], ch = chi[h];
+      cf = P::make(tt.x * ch.x - tt.y * ch.y, tt.x * ch.y + tt.y * ch.x);
+    }
+    if (FERMI) neg ^= __popcll(m & dev::bits_between(i, j)) & 1;
+    if (PHASES) {
+      S pr = 1, pi = 0;
+      if (pc.mode == 1) {
+        const uint64_t* mk = pc.mask + h * kMaxCls;
+        const V* pw = pc.pw + (size_t)h * kMaxCls * pc.kp1;
+#pragma unroll
+        for (int cl = 0; cl < kMaxCls; ++cl) {
+          const V e = pw[cl * pc.kp1 + __popcll(nw & mk[cl])];
+          const S nr = pr * e.x - pi * e.y;
+          pi = pr * e.y + pi * e.x;
+          pr = nr;
+        }
+      } else if (pc.mode == 2) {
+        uint64_t b = nw;
+        const V* eh = eta + (size_t)h * N;
+        while (b) {
+          const int qq = __ffsll((long long)b) - 1;
+          b &= b - 1;
+          const V e = eh[qq];
+          const S nr = pr * e.x - pi * e.y;
+          pi = pr * e.y + pi * e.x;
+          pr = nr;
+        }
+      }
+      cf = P::make(cf.x * pr + cf.y * pi, cf.y * pr - cf.x * pi);
+    }
+    const V xq = P::flip(xc, neg);
+    ar = P::mad(cf.x, xq.x, ar);
+    ar = P::mad(-cf.y, xq.y, ar);
+    ai = P::mad(cf.x, xq.y, ai);
+    ai = P::mad(cf.y, xq.x, ai);
+  }
+}
+
 }  // namespace sed

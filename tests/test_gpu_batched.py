@@ -138,3 +138,24 @@ def test_batch_rejects_a_bad_request_in_a_large_batch():
     assert e.value.code == _lib.SED_ERR_NOT_HERMITIAN
     out = solver.run(reqs[:8])
     assert (out["status"] == 0).all()
+
+
+def test_batch_launch_is_a_replayed_graph():
+    """The batch launch is captured as a CUDA graph on its first run and
+    replayed while the launch configuration repeats; a replay gives the same
+    bits as the captured run, and a different configuration is captured anew."""
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.checkerboard(3, 2, n_filled=4)
+    reqs = flux_scan_requests(spec, TWISTS[:2])
+    solver = _solver(spec, "mixed")
+    a = solver.run(reqs)
+    st = solver.last_stats()
+    assert (st["graph_captures"], st["graph_replays"]) == (1, 0)
+    b = solver.run(reqs)
+    st = solver.last_stats()
+    assert (st["graph_captures"], st["graph_replays"]) == (1, 1)
+    np.testing.assert_array_equal(a["evals"], b["evals"])
+    solver.run(reqs[:5])
+    st = solver.last_stats()
+    assert st["graph_captures"] == 2

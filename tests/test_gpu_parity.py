@@ -239,3 +239,34 @@ def test_flux_refresh_matches_fresh_build(oracle):
         op = oracle.Op(osec, case.bilinear0(), case.density0())
         x = x_random(osec.dim, seed=k)
         assert np.abs(H(x) - op.apply(x)).max() < 1e-11 * max(1, np.abs(op.apply(x)).max())
+
+
+SHAPES = [(1, 512), (1, 256), (2, 512), (2, 256), (4, 512), (4, 256), (8, 512), (8, 256)]
+
+
+@pytest.mark.parametrize("name", ["checkerboard3x2_f_flux", "hubbard2x4_flux", "ring16"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gather_launch_shapes_match_oracle(oracle, name, precision):
+    """Every launch shape of the matrix-free gather (threads per row x threads
+    per block) gives the oracle's matvec; the autotuner's choice is one of
+    them."""
+    case = case_by_name(name)
+    for k in (0, 1):
+        _, _, op = oracle_objects(oracle, case, k)
+        if op.dim == 0:
+            continue
+        _, _, H = _device(case, k, precision)
+        H.set_hop_table(H.HOP_TABLE_OFF)
+        x = x_random(op.dim, seed=7 + k)
+        ref = op.apply(x, mode=0)
+        scale = max(1.0, np.abs(ref).max())
+        tol = 1e-11 if precision == "fp64" else 3e-6
+        y = H(x)  # autotuned
+        assert H.apply_shape(precision == "mixed") in SHAPES
+        assert np.abs(y - ref).max() <= tol * scale
+        for tpr, block in SHAPES:
+            H.set_apply_shape(tpr, block)
+            y = H(x)
+            assert H.apply_shape(precision == "mixed") == (tpr, block)
+            assert np.abs(y - ref).max() <= tol * scale, (name, k, precision, tpr, block)
+        H.set_apply_shape(0, 0)
