@@ -267,6 +267,10 @@ int sed_batch_last_info(const sed_batch* b, int32_t* n_fallback, int32_t* hop_ta
  * captured once per launch configuration and replayed while it repeats:
  * how many captures and replays this batch object has made. */
 int sed_batch_graph_info(const sed_batch* b, int32_t* captures, int32_t* replays);
+/* Where the mixed kernel keeps its complex64 matvec input: shared memory (the
+ * default whenever it fits beside the tables) or global memory (the choice
+ * for sectors too large for it; 0 forces it, e.g. to compare the two). */
+int sed_batch_set_x_in_shared_memory(sed_batch* b, int enable);
 /* The hop table (on by default): the requests of a batch share the catalog and
  * the (i, j) term list, hence every sector matrix's sparsity pattern, which is
  * enumerated once into 8-byte records (column orbit, term x group element,

@@ -82,6 +82,7 @@ SIGNATURES = [
     ("sed_batch_last_stats", _i32, [_p, _p, _p, _p]),
     ("sed_batch_last_info", _i32, [_p, _p, _p, _p]),
     ("sed_batch_graph_info", _i32, [_p, _p, _p]),
+    ("sed_batch_set_x_in_shared_memory", _i32, [_p, _i32]),
     ("sed_batch_set_hop_table", _i32, [_p, _i32]),
     ("sed_batch_run_device", _i32, [_p, _i32, _p, _p, _p, _p, _dbl, _i32, _p, _p, _p, _p, _p]),
     ("sed_batch_set_stream", _i32, [_p, _p]),

@@ -121,6 +121,11 @@ class BatchedSectorSolver:
                 "hop_table": bool(tab.value), "hop_records": int(nrec.value),
                 "graph_captures": int(caps.value), "graph_replays": int(reps.value)}
 
+    def set_x_in_shared_memory(self, enable: bool) -> None:
+        """Keep the complex64 matvec input in shared memory (default when it
+        fits) or in global memory (the layout of sectors too large for it)."""
+        check(_lib.load().sed_batch_set_x_in_shared_memory(self._h, int(bool(enable))))
+
     def set_hop_table(self, enable: bool) -> None:
         """Stream the shared hop table (default) or derive every hop on the fly."""
         check(_lib.load().sed_batch_set_hop_table(self._h, int(bool(enable))))

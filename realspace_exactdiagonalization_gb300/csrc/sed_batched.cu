@@ -1670,6 +1670,23 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           break;
         }
         tau *= 0.1;
+        if (!X_SMEM) {
+          // the check used x's global buffer for its FP64-class vectors: the
+          // Lanczos resumes from the continuation vector (slot keep), so its
+          // scaled copy, as df_normalize wrote it, goes back into x
+          const float4* vk = Vb + (size_t)keep * a.ld;
+          for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+            const float4 v = vk[o];
+            if (sizeof(V) == 8) {
+              const float sq = s_sqrtf[a.stab[o]];
+              reinterpret_cast<float2*>(x)[o] = make_float2(v.x * sq, v.y * sq);
+            } else {
+              const double sq = s_sqrt[a.stab[o]];
+              reinterpret_cast<double2*>(x)[o] = make_double2(df_to_d(v.x, v.z) * sq, df_to_d(v.y, v.w) * sq);
+            }
+          }
+          __syncthreads();
+        }
       }
       // arrowhead restart matrix
       __syncthreads();
@@ -1715,6 +1732,9 @@ struct BatchImpl {
   int64_t hop_records = 0;
   int last_tab = 0;
   bool tab_enabled = true;
+  // complex64 matvec input in shared memory (else in global memory, for
+  // sectors whose x does not fit beside the tables)
+  bool x_smem = true;
   size_t smem = 0;
   int64_t ld = 0;
   size_t footprint = 0;
@@ -1817,9 +1837,12 @@ static void dispatch_prepare(BatchImpl& B, const BatchArgs& a, BatchSmem& L, int
   const bool mixed = !fp64;
   // Each (precision, statistics) pair is compiled with the twisted-phase
   // product; untwisted requests multiply by exactly 1.
-  if (mixed) {
+  if (mixed && B.x_smem) {
     if (B.fermi) batch_prepare<P32, true, true, true>(B, a, L, ncta);
     else batch_prepare<P32, false, true, true>(B, a, L, ncta);
+  } else if (mixed) {
+    if (B.fermi) batch_prepare<P32, true, true, false>(B, a, L, ncta);
+    else batch_prepare<P32, false, true, false>(B, a, L, ncta);
   } else {
     if (B.fermi) batch_prepare<P64, true, true, false>(B, a, L, ncta);
     else batch_prepare<P64, false, true, false>(B, a, L, ncta);
@@ -1828,9 +1851,12 @@ static void dispatch_prepare(BatchImpl& B, const BatchArgs& a, BatchSmem& L, int
 
 static void dispatch_launch(BatchImpl& B, const BatchArgs& a, const BatchSmem& L, int ncta, cudaStream_t s,
                             bool fp64) {
-  if (!fp64) {
+  if (!fp64 && B.x_smem) {
     if (B.fermi) batch_launch<P32, true, true, true>(a, L, ncta, s);
     else batch_launch<P32, false, true, true>(a, L, ncta, s);
+  } else if (!fp64) {
+    if (B.fermi) batch_launch<P32, true, true, false>(a, L, ncta, s);
+    else batch_launch<P32, false, true, false>(a, L, ncta, s);
   } else {
     if (B.fermi) batch_launch<P64, true, true, false>(a, L, ncta, s);
     else batch_launch<P64, false, true, false>(a, L, ncta, s);
@@ -2186,9 +2212,27 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   // large for both keeps the on-the-fly matvec
   B->phi_cap = kPhiCap;
   BatchArgs a = base_args(*B);
-  const size_t with_tab =
-      precision == 1 ? batch_layout<float2>(a, true).total : batch_layout<double2>(a, false).total;
-  if (with_tab > 220 * 1024) {
+  // Shared memory: the complex64 matvec input x stays in shared memory when it
+  // fits beside the tables, with the hop table's phase coefficients if they
+  // fit too; a sector whose x cannot fit keeps x in global memory (L2) and
+  // the hop table.
+  constexpr size_t kSmemBudget = 220 * 1024;
+  if (precision == 1) {
+    if (batch_layout<float2>(a, true).total > kSmemBudget) {
+      BatchArgs a0 = a;
+      a0.phi_cap = 0;
+      if (batch_layout<float2>(a0, true).total <= kSmemBudget) {
+        B->phi_cap = 0;
+        a.phi_cap = 0;
+      } else {
+        B->x_smem = false;
+        if (batch_layout<float2>(a, false).total > kSmemBudget) {
+          B->phi_cap = 0;
+          a.phi_cap = 0;
+        }
+      }
+    }
+  } else if (batch_layout<double2>(a, false).total > kSmemBudget) {
     B->phi_cap = 0;
     a.phi_cap = 0;
   }
@@ -2488,6 +2532,18 @@ int sed_batch_info(const sed_batch* b, int64_t* smem_bytes, int64_t* n_blocks, i
   });
 }
 
+int sed_batch_set_x_in_shared_memory(sed_batch* b, int enable) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    sed::BatchImpl& B = *b->p;
+    if (enable && !B.x_smem) {
+      sed::BatchArgs a = sed::base_args(B);
+      SED_REQUIRE(B.precision == 1 && sed::batch_layout<float2>(a, true).total <= 220 * 1024, 5,
+                  "the matvec input does not fit in shared memory beside this batch's tables");
+    }
+    B.x_smem = B.precision == 1 && enable != 0;
+  });
+}
 int sed_batch_graph_info(const sed_batch* b, int* captures, int* replays) {
   return bguard([&] {
     SED_REQUIRE(b, 1, "NULL batch");

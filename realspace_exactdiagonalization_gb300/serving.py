@@ -36,9 +36,18 @@ from . import lattice as L
 from .batched import BatchedSectorSolver
 from .groups import statistics_from_name
 
-# sectors whose catalog has at most this many orbits fit the batched kernel's
-# shared-memory vector (complex64, plus the tables)
+# sectors whose catalog has at most this many orbits are solved by the batched
+# kernel, one thread block each (its complex64 matvec input fits in shared
+# memory); larger sectors take concurrent device-wide solves.  The batched
+# kernel also runs larger sectors with that input in global memory, but in
+# the served mix routing 1e5-3e5-orbit families there measured slower: the
+# shared batch lanes then delay the small families, while the large route
+# stays bound by its biggest sectors.  small_max_orbits raises the limit.
 SMALL_MAX_ORBITS = 16384
+# catalogs above this size keep their batch workspace (the per-block Lanczos
+# basis) to MEDIUM_MAX_BATCH concurrent requests per lane
+MEDIUM_ORBITS = 16384
+MEDIUM_MAX_BATCH = 48
 
 
 @dataclass
@@ -136,9 +145,10 @@ class SectorServer:
             fam = Family(name, spec, cat, pairs, route)
             self.resident += cat.n_states * 8 + cat.n_orbits * 9
             if route == "batch":
+                cap = max_batch if cat.n_orbits <= MEDIUM_ORBITS else min(max_batch, MEDIUM_MAX_BATCH)
                 for _ in range(batch_lanes):
                     s = BatchedSectorSolver(cat, pairs, spec.density_terms, precision=precision, nev=nev,
-                                            max_requests=max_batch)
+                                            max_requests=cap)
                     fam.solvers.append(s)
                     self.resident += s.info()["footprint_bytes"]
             self.families[name] = fam
@@ -179,7 +189,8 @@ class SectorServer:
                 if not self._pending_batch and self._closed:
                     return
                 fam_name = self._pending_batch[0].family  # oldest request decides the family
-                take = [r for r in self._pending_batch if r.family == fam_name][: self.max_batch]
+                cap = self.families[fam_name].solvers[lane % len(self.families[fam_name].solvers)].max_requests
+                take = [r for r in self._pending_batch if r.family == fam_name][:cap]
                 for r in take:
                     self._pending_batch.remove(r)
             fam = self.families[fam_name]

@@ -159,3 +159,42 @@ def test_batch_launch_is_a_replayed_graph():
     solver.run(reqs[:5])
     st = solver.last_stats()
     assert st["graph_captures"] == 2
+
+
+def test_batch_x_in_global_memory_matches_shared():
+    """The mixed kernel with its matvec input in global memory (the layout of
+    sectors too large for shared memory) gives the shared-memory layout's
+    results on the same requests."""
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.haldane_honeycomb(2, 4)
+    reqs = flux_scan_requests(spec, TWISTS)
+    solver = _solver(spec, "mixed")
+    a = solver.run(reqs)
+    solver.set_x_in_shared_memory(False)
+    b = solver.run(reqs)
+    assert (a["status"] == 0).all() and (b["status"] == 0).all()
+    np.testing.assert_allclose(b["evals"], a["evals"], rtol=0, atol=1e-12 * np.nanmax(np.abs(a["evals"])))
+    solver.set_x_in_shared_memory(True)
+    np.testing.assert_array_equal(solver.run(reqs)["evals"], a["evals"])
+
+
+def test_batch_sector_too_large_for_shared_memory():
+    """A ring of 22 sites at half filling (32,066 orbits: its complex64 x does
+    not fit in shared memory) through the batched kernel, against device-wide
+    FP64 solves of the same sectors."""
+    import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.ring_xxz(22, 1.0, 2.0)
+    reqs = flux_scan_requests(spec, [(0.0, 0.0), (0.3, 0.0)])[::5]
+    solver = _solver(spec, "mixed", nev=2)
+    out = solver.run(reqs)
+    assert (out["status"] == 0).all()
+    cat = solver.catalog
+    for b, r in enumerate(reqs):
+        basis = A.build_symmetry_sector_basis(cat, r.irrep, group=r.group)
+        H = A.MatrixFreeHamiltonian(basis, [(i, j, t) for (i, j, _), t in zip(spec.bilinear_terms(), r.amplitudes)],
+                                    spec.density_terms)
+        ref, _, _ = H.solve(2, tol=1e-10, want_vectors=False)
+        assert abs(out["evals"][b, 0] - ref[0]) <= 1e-9 * max(1.0, abs(ref[0])), (b, out["evals"][b], ref)
