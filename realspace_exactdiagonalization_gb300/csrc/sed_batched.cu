@@ -1349,11 +1349,12 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       const uint64_t m = a.reps[o];
       int ok = 1;
       for (int g = 0; g < a.G; ++g) {
+        // the phase product (FP64) only for stabilizer elements
+        if (dev::apply_perm(m, s_perm + g * 64) != m) continue;
         double2 al;
-        if (dev::apply_full(m, s_perm + g * 64, phase + (size_t)g * a.N, FERMI ? 1 : 0, &al) == m) {
-          const double2 xg = s_chi[g];
-          if (!((xg.x == al.x && xg.y == al.y) || hypot(xg.x - al.x, xg.y - al.y) <= a.atol)) ok = 0;
-        }
+        dev::apply_full(m, s_perm + g * 64, phase + (size_t)g * a.N, FERMI ? 1 : 0, &al);
+        const double2 xg = s_chi[g];
+        if (!((xg.x == al.x && xg.y == al.y) || hypot(xg.x - al.x, xg.y - al.y) <= a.atol)) ok = 0;
       }
       rowflag[o] = (uint8_t)ok;
       cnt += ok;
@@ -1747,6 +1748,10 @@ struct BatchImpl {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_captures = 0, graph_replays = 0;
+  // the graph is recorded on a private stream: the caller's stream may be the
+  // legacy default stream, which cannot be captured (the replay goes onto the
+  // caller's stream, where it is ordered like a plain launch)
+  cudaStream_t capture_stream = nullptr;
   void drop_graph() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (graph) cudaGraphDestroy(graph);
@@ -1756,6 +1761,7 @@ struct BatchImpl {
   }
   ~BatchImpl() {
     drop_graph();
+    if (capture_stream) cudaStreamDestroy(capture_stream);
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
@@ -1878,16 +1884,18 @@ static void graph_launch(BatchImpl& B, const BatchArgs& a, const BatchSmem& L, i
   if (!B.graph_exec || key != B.graph_key) {
     B.drop_graph();
     cudaGraph_t g = nullptr;
-    SED_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    if (!B.capture_stream) SED_CUDA(cudaStreamCreateWithFlags(&B.capture_stream, cudaStreamNonBlocking));
+    const cudaStream_t cs = B.capture_stream;
+    SED_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
-      SED_CUDA(cudaMemsetAsync(B.queue.p, 0, 16, s));
-      dispatch_launch(B, a, L, ncta, s, fp64);
+      SED_CUDA(cudaMemsetAsync(B.queue.p, 0, 16, cs));
+      dispatch_launch(B, a, L, ncta, cs, fp64);
     } catch (...) {
-      cudaStreamEndCapture(s, &g);
+      cudaStreamEndCapture(cs, &g);
       if (g) cudaGraphDestroy(g);
       throw;
     }
-    SED_CUDA(cudaStreamEndCapture(s, &g));
+    SED_CUDA(cudaStreamEndCapture(cs, &g));
     cudaGraphExec_t x = nullptr;
     const cudaError_t e = cudaGraphInstantiate(&x, g, 0);
     if (e != cudaSuccess) {

@@ -452,12 +452,13 @@ __global__ void k_rb_stab(int64_t n_orb, const uint64_t* __restrict__ reps, cons
     const uint64_t m = reps[o];
     int64_t j = ptr[o];
     for (int g = 0; g < G; ++g) {
+      // integer image first; the FP64 phase product only for stabilizer elements
+      if (dev::apply_perm(m, sperm + g * 64) != m) continue;
       double2 a;
-      if (dev::apply_full(m, sperm + g * 64, phase + (size_t)g * N, fermi, &a) == m) {
-        if (g_out) g_out[j] = g + 1;
-        if (ph_out) ph_out[j] = a;
-        ++j;
-      }
+      dev::apply_full(m, sperm + g * 64, phase + (size_t)g * N, fermi, &a);
+      if (g_out) g_out[j] = g + 1;
+      if (ph_out) ph_out[j] = a;
+      ++j;
     }
   }
 }
@@ -548,11 +549,14 @@ __global__ void __launch_bounds__(256) k_sector_compat(int64_t n_orb, int G, int
       ok = 1;
       const uint64_t m = reps[o];
       for (int g = 0; g < G; ++g) {
+        // the amplitude matters only for stabilizer elements: the integer
+        // image first, the FP64 phase product (GB300's scarce FP64 pipe) only
+        // when the image is the representative itself
+        if (dev::apply_perm(m, sperm + g * 64) != m) continue;
         double2 a;
-        if (dev::apply_full(m, sperm + g * 64, phase + (size_t)g * N, fermi, &a) == m) {
-          const double2 x = schi[g];
-          if (!((x.x == a.x && x.y == a.y) || hypot(x.x - a.x, x.y - a.y) <= atol)) ok = 0;
-        }
+        dev::apply_full(m, sperm + g * 64, phase + (size_t)g * N, fermi, &a);
+        const double2 x = schi[g];
+        if (!((x.x == a.x && x.y == a.y) || hypot(x.x - a.x, x.y - a.y) <= atol)) ok = 0;
       }
       rowflag[o] = (uint8_t)ok;
     }

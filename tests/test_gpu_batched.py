@@ -159,6 +159,13 @@ def test_batch_launch_is_a_replayed_graph():
     solver.run(reqs[:5])
     st = solver.last_stats()
     assert st["graph_captures"] == 2
+    # on the legacy default stream (which cannot itself be captured) the
+    # graph is still captured, replayed, and gives the same bits
+    solver.set_stream(0)
+    np.testing.assert_array_equal(solver.run(reqs)["evals"], a["evals"])
+    np.testing.assert_array_equal(solver.run(reqs)["evals"], a["evals"])
+    st = solver.last_stats()
+    assert (st["graph_captures"], st["graph_replays"]) == (3, 2)
 
 
 def test_batch_x_in_global_memory_matches_shared():
