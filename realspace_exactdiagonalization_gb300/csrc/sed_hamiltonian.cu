@@ -704,13 +704,10 @@ void op_apply_orbit(OpImpl& op, const void* xs, double* ypad, cudaStream_t s) {
   apply_impl(op, op.precision == 1, xs, ypad, s);
 }
 
-bool op_apply_orbit_df(OpImpl& op, const void* xs, double* ypad, cudaStream_t s) {
-  if (op.tab_built && op.precision == 1 && op.sec->cat->n_orbits > 0) {
-    apply_table(op, true, xs, ypad, s, true);
-    return true;
-  }
-  apply_impl(op, op.precision == 1, xs, ypad, s);
-  return false;
+bool op_apply_orbit_cf(OpImpl& op, const void* xs, float2* y, cudaStream_t s) {
+  if (!(op.tab_built && op.precision == 1 && op.sec->cat->n_orbits > 0)) return false;
+  apply_table(op, true, xs, reinterpret_cast<double*>(y), s, true);
+  return true;
 }
 
 // FP64 matvec regardless of the op precision (the polish step of mixed solves)

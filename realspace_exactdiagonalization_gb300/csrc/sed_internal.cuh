@@ -195,7 +195,7 @@ struct OpImpl {
 void op_set_apply_shape(OpImpl& op, int tpr, int block);
 bool op_build_table(OpImpl& op);
 void op_drop_table(OpImpl& op);
-void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s, bool df_out = false);
+void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s, bool cf_out = false);
 
 // ----------------------------------------------------------- entry points
 std::shared_ptr<GroupImpl> make_group(int n_site, int n_ops, const int32_t* perm, const double* phase, int identity,
@@ -220,9 +220,9 @@ void check_hermitian_symmetric(const GroupImpl& G, int n_bil, const int32_t* bil
 void op_apply_host(OpImpl& op, const double* x, double* y, int64_t n, bool device_ptrs);
 // y_pad (complex128, orbit-indexed) = H x given xs = sqrt(stab) * x in the op precision
 void op_apply_orbit(OpImpl& op, const void* xs, double* ypad, cudaStream_t s);
-// the mixed-precision matvec with a double-float output; false when the
-// operator has no hop table and ypad holds the FP64 rows instead
-bool op_apply_orbit_df(OpImpl& op, const void* xs, double* ypad, cudaStream_t s);
+// the mixed-precision matvec streamed from the hop table with a complex64
+// output; false (nothing launched) when the operator has no hop table
+bool op_apply_orbit_cf(OpImpl& op, const void* xs, float2* y, cudaStream_t s);
 // xs = sqrt(stab) * v (cast to the op precision); v orbit-indexed complex128
 void op_scale_to_xs(OpImpl& op, const double* v, void* xs, cudaStream_t s);
 int64_t op_count_hops(OpImpl& op);

@@ -337,105 +337,112 @@ __global__ void k_residual(int64_t n, const double2* __restrict__ a, const doubl
   }
 }
 
-// Davidson correction: w_o <- w_o / (diag_o - theta), the denominator kept
-// at least delta away from zero (diag = density-density diagonal of H).
-// ------------------------------------------------ double-float basis (mixed)
+// ------------------------------------------------ complex64 basis (mixed)
 // The mixed-precision solve keeps its Lanczos basis, work vector and restart
-// buffer as double-float complex (float4 per element, sed_dfloat.cuh): the
-// recurrence, the reorthogonalisation and the restart rotations keep
-// FP64-class accuracy on the FP32 pipe instead of GB300's 1/64-rate FP64
-// pipe, in the same 16 bytes per element.  The complex64 matvec writes FP64,
-// converted in place; the FP64 polish reads FP64 copies of the Ritz vectors.
+// buffer in complex64: 8 bytes per element, half the traffic of an FP64-class
+// basis.  Each stored value is rounded once to FP32 from an accurately
+// computed one:
+// * dot products accumulate FP32 products per thread over short chains (a
+//   grid-stride sweep gives each thread a few tens of elements) and sum the
+//   thread partials in FP64;
+// * updates w -= sum_l c_l v_l apply each coefficient as hi + lo floats, so
+//   the large local coefficients (alpha, beta) cancel without losing bits;
+// * restart rotations accumulate in double-float (TwoProd, TwoSum);
+// * the normalisation multiplies by 1/|w| as hi + lo floats.
+// The storage rounding (2^-24) is the size of the complex64 matvec's own
+// rounding, which already perturbs the recurrence at that level (Paige's
+// local-error model); the FP64 Rayleigh-Ritz check then bounds the
+// eigenvalues.  Vectors sit cf_ld(n) elements apart, so each starts on a
+// 512-byte boundary: the bulk L2 prefetch wants 16-byte aligned chunks.
+static inline int64_t cf_ld(int64_t n) { return (n + 63) / 64 * 64; }
 
-// w (FP64 complex) -> double-float, in place
-__global__ void k_df_from_d(int64_t n, double2* __restrict__ w) {
-  float4* out = reinterpret_cast<float4*>(w);
+// FP64 complex -> complex64
+__global__ void k_d_to_cf(int64_t n, const double2* __restrict__ in, float2* __restrict__ out) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double2 x = w[i];
-    float4 r;
-    d_to_df(x.x, r.x, r.z);
-    d_to_df(x.y, r.y, r.w);
-    out[i] = r;
+    const double2 x = in[i];
+    out[i] = make_float2((float)x.x, (float)x.y);
   }
 }
 
-__global__ void k_df_to_d(int64_t n, const float4* __restrict__ v, double2* __restrict__ out) {
+// vector blockIdx.y: complex64 (stride ldc) -> FP64 (stride ld)
+__global__ void k_cf_to_d(int64_t n, const float2* __restrict__ v, int64_t ldc, double2* __restrict__ out,
+                          int64_t ld) {
+  const float2* __restrict__ src = v + (size_t)blockIdx.y * ldc;
+  double2* __restrict__ dst = out + (size_t)blockIdx.y * ld;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float4 x = v[i];
-    out[i] = make_double2(df_to_d(x.x, x.z), df_to_d(x.y, x.w));
+    const float2 x = src[i];
+    dst[i] = make_double2(x.x, x.y);
   }
 }
 
-__global__ void __launch_bounds__(kBS) k_df_norm2_part(int64_t n, const float4* __restrict__ v,
+__global__ void __launch_bounds__(kBS) k_cf_norm2_part(int64_t n, const float2* __restrict__ v,
                                                        double* __restrict__ part) {
-  float h = 0.f, l = 0.f;
+  float s = 0.f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float4 x = v[i];
-    df_mac(h, l, x.x, x.z, x.x, x.z);
-    df_mac(h, l, x.y, x.w, x.y, x.w);
+    const float2 x = v[i];
+    s = __fmaf_rn(x.x, x.x, __fmaf_rn(x.y, x.y, s));
   }
-  const double2 r = block_sum2(df_to_d(h, l), 0.0);
+  const double2 r = block_sum2((double)s, 0.0);
   if (threadIdx.x == 0) part[blockIdx.x] = r.x;
 }
 
-// part[l*nblk + b] = block b's share of conj(V_l) w for the 8 vectors of
-// chunk blockIdx.y: w is read once per 8 basis vectors
 // L2 prefetch of the vectors a grid-stride sweep reads: at each step, thread
-// t < nv of the block asks the TMA unit for its chunk of vector t two strides
-// ahead (cp.async.bulk.prefetch: no registers, nothing to wait for), so the
-// loads of the coming iterations find their lines in L2.  Used by the dot
-// kernel (eight vectors a block); for the update kernel, which sweeps all
-// basis vectors at once, the prefetched lines would crowd the L2 and it
-// measured slower.
-__device__ __forceinline__ void df_prefetch_ahead(const float4* V, int64_t ld, int nv, const float4* w, int64_t n,
+// t <= nv of the block asks the TMA unit for its chunk of vector t (t = nv:
+// the work vector) two strides ahead (cp.async.bulk.prefetch: no registers,
+// nothing to wait for), so the loads of the coming iterations find their
+// lines in L2.  Chunks start on multiples of the block size (2 KB), and the
+// byte count is rounded up to 16 inside the vector's padding.
+__device__ __forceinline__ void cf_prefetch_ahead(const float2* V, int64_t ld, int nv, const float2* w, int64_t n,
                                                   int64_t b, int64_t stride) {
   const int t = threadIdx.x;
   if (t > nv) return;
   const int64_t pb = b + 2 * stride;
   if (pb >= n) return;
-  const float4* p = t < nv ? V + (size_t)t * ld + pb : w + pb;
-  if (!p) return;
-  const uint32_t bytes = (uint32_t)min((int64_t)blockDim.x, n - pb) * 16u;
+  const float2* p = t < nv ? V + (size_t)t * ld + pb : w + pb;
+  const uint32_t bytes = ((uint32_t)min((int64_t)blockDim.x, n - pb) * 8u + 15u) & ~15u;
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-__global__ void __launch_bounds__(kBS) k_df_multidot(int64_t n, const float4* __restrict__ V, int64_t ld, int nv,
-                                                     const float4* __restrict__ w, double2* __restrict__ part) {
-  const int l0 = blockIdx.y * 8;
-  const int cn = min(8, nv - l0);
-  float h[16], lo[16];
+// part[l*nblk + b] = block b's share of conj(V_l) w for the kDotCh vectors of
+// chunk blockIdx.y: w is read once per kDotCh basis vectors
+static constexpr int kDotCh = 16;
+__global__ void __launch_bounds__(kBS) k_cf_multidot(int64_t n, const float2* __restrict__ V, int64_t ld, int nv,
+                                                     const float2* __restrict__ w, double2* __restrict__ part) {
+  const int l0 = blockIdx.y * kDotCh;
+  const int cn = min(kDotCh, nv - l0);
+  float re[kDotCh], im[kDotCh];
 #pragma unroll
-  for (int c = 0; c < 16; ++c) h[c] = lo[c] = 0.f;
+  for (int c = 0; c < kDotCh; ++c) re[c] = im[c] = 0.f;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t b = (int64_t)blockIdx.x * blockDim.x; b < n; b += stride) {
-    df_prefetch_ahead(V + (size_t)l0 * ld, ld, cn, w, n, b, stride);
+    cf_prefetch_ahead(V + (size_t)l0 * ld, ld, cn, w, n, b, stride);
     const int64_t i = b + threadIdx.x;
     if (i >= n) continue;
-    const float4 x = w[i];
+    const float2 x = w[i];
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
+    for (int c = 0; c < kDotCh; ++c)
       if (c < cn) {
-        const float4 v = V[(size_t)(l0 + c) * ld + i];
-        df_mac(h[2 * c], lo[2 * c], v.x, v.z, x.x, x.z);
-        df_mac(h[2 * c], lo[2 * c], v.y, v.w, x.y, x.w);
-        df_mac(h[2 * c + 1], lo[2 * c + 1], v.x, v.z, x.y, x.w);
-        df_mac(h[2 * c + 1], lo[2 * c + 1], -v.y, -v.w, x.x, x.z);
+        const float2 v = V[(size_t)(l0 + c) * ld + i];
+        re[c] = __fmaf_rn(v.x, x.x, __fmaf_rn(v.y, x.y, re[c]));
+        im[c] = __fmaf_rn(v.x, x.y, __fmaf_rn(-v.y, x.x, im[c]));
       }
   }
 #pragma unroll
-  for (int c = 0; c < 8; ++c)
+  for (int c = 0; c < kDotCh; ++c)
     if (c < cn) {
-      const double2 r = block_sum2(df_to_d(h[2 * c], lo[2 * c]), df_to_d(h[2 * c + 1], lo[2 * c + 1]));
+      const double2 r = block_sum2((double)re[c], (double)im[c]);
       if (threadIdx.x == 0) part[(size_t)(l0 + c) * gridDim.x + blockIdx.x] = r;
     }
 }
 
-// w -= sum_l c_l V_l (double-float), optionally the block partial of |w|^2
-__global__ void __launch_bounds__(kBS) k_df_multiaxpy(int64_t n, const float4* __restrict__ V, int64_t ld, int nv,
-                                                      const double2* __restrict__ c, float4* __restrict__ w,
+// w -= sum_l c_l V_l, each FP64 coefficient applied as hi + lo floats;
+// optionally the block partial of |w|^2.  skip: the device flag of the
+// selective reorthogonalisation (no update this step).
+__global__ void __launch_bounds__(kBS) k_cf_multiaxpy(int64_t n, const float2* __restrict__ V, int64_t ld, int nv,
+                                                      const double2* __restrict__ c, float2* __restrict__ w,
                                                       double* __restrict__ norm_part, const int* __restrict__ skip) {
-  if (skip && *skip) return;  // selective reorthogonalisation: no update this step
-  __shared__ float4 sc[128];
+  if (skip && *skip) return;
+  __shared__ float4 sc[128];  // (re_hi, im_hi, re_lo, im_lo)
   for (int l = threadIdx.x; l < nv; l += blockDim.x) {
     float4 t;
     d_to_df(c[l].x, t.x, t.z);
@@ -443,25 +450,27 @@ __global__ void __launch_bounds__(kBS) k_df_multiaxpy(int64_t n, const float4* _
     sc[l] = t;
   }
   __syncthreads();
-  float nh = 0.f, nl = 0.f;
+  float s = 0.f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    float4 x = w[i];
+    const float2 x = w[i];
+    float xr = x.x, xi = x.y;
     for (int l = 0; l < nv; ++l) {
-      const float4 v = V[(size_t)l * ld + i];
+      const float2 v = V[(size_t)l * ld + i];
       const float4 cc = sc[l];
-      df_mac(x.x, x.z, -cc.x, -cc.z, v.x, v.z);
-      df_mac(x.x, x.z, cc.y, cc.w, v.y, v.w);
-      df_mac(x.y, x.w, -cc.x, -cc.z, v.y, v.w);
-      df_mac(x.y, x.w, -cc.y, -cc.w, v.x, v.z);
+      xr = __fmaf_rn(-cc.x, v.x, xr);
+      xr = __fmaf_rn(cc.y, v.y, xr);
+      xi = __fmaf_rn(-cc.x, v.y, xi);
+      xi = __fmaf_rn(-cc.y, v.x, xi);
+      xr = __fmaf_rn(-cc.z, v.x, xr);
+      xr = __fmaf_rn(cc.w, v.y, xr);
+      xi = __fmaf_rn(-cc.z, v.y, xi);
+      xi = __fmaf_rn(-cc.w, v.x, xi);
     }
-    df_renorm(x.x, x.z);
-    df_renorm(x.y, x.w);
-    w[i] = x;
-    df_mac(nh, nl, x.x, x.z, x.x, x.z);
-    df_mac(nh, nl, x.y, x.w, x.y, x.w);
+    w[i] = make_float2(xr, xi);
+    s = __fmaf_rn(xr, xr, __fmaf_rn(xi, xi, s));
   }
   if (norm_part) {
-    const double2 r = block_sum2(df_to_d(nh, nl), 0.0);
+    const double2 r = block_sum2((double)s, 0.0);
     if (threadIdx.x == 0) norm_part[blockIdx.x] = r.x;
   }
 }
@@ -476,9 +485,10 @@ __global__ void k_sel_flag(const double2* __restrict__ c, int nv, const double* 
   if (threadIdx.x == 0) *skip = m <= eta * sqrt(*w2) ? 1 : 0;
 }
 
-// v = w / sqrt(nrm2) (double-float); xs = sqrt(stab) v in complex64
-__global__ void k_df_normalize(int64_t n, const float4* __restrict__ w, const double* __restrict__ nrm2,
-                               float4* __restrict__ v, const uint8_t* __restrict__ stab, float2* __restrict__ xs) {
+// v = w / sqrt(nrm2) in complex64 (1/|w| as hi + lo floats, one rounding of
+// the product); xs = sqrt(stab) v, the matvec input
+__global__ void k_cf_normalize(int64_t n, const float2* __restrict__ w, const double* __restrict__ nrm2,
+                               float2* __restrict__ v, const uint8_t* __restrict__ stab, float2* __restrict__ xs) {
   __shared__ float s_sq[65];
   __shared__ float s_inv[2];
   for (int i = threadIdx.x; i < 65; i += blockDim.x) s_sq[i] = (float)sqrt((double)i);
@@ -486,35 +496,41 @@ __global__ void k_df_normalize(int64_t n, const float4* __restrict__ w, const do
   __syncthreads();
   const float ih = s_inv[0], il = s_inv[1];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float4 y = w[i];
-    float4 r;
-    r.x = __fmul_rn(y.x, ih);
-    r.z = __fmaf_rn(y.x, il, __fmaf_rn(y.z, ih, __fmaf_rn(y.x, ih, -r.x)));
-    r.y = __fmul_rn(y.y, ih);
-    r.w = __fmaf_rn(y.y, il, __fmaf_rn(y.w, ih, __fmaf_rn(y.y, ih, -r.y)));
-    df_renorm(r.x, r.z);
-    df_renorm(r.y, r.w);
-    if (v) v[i] = r;
+    const float2 y = w[i];
+    const float rx = __fmaf_rn(y.x, ih, __fmul_rn(y.x, il));
+    const float ry = __fmaf_rn(y.y, ih, __fmul_rn(y.y, il));
+    if (v) v[i] = make_float2(rx, ry);
     if (xs) {
       const float sq = s_sq[stab[i]];
-      xs[i] = make_float2(r.x * sq, r.y * sq);
+      xs[i] = make_float2(__fmul_rn(rx, sq), __fmul_rn(ry, sq));
     }
   }
 }
 
+// (h, l) += x (zh + zl) for a float x: TwoProd of the leading product, the
+// rest folded into the low word
+__device__ __forceinline__ void df_mac1(float& h, float& l, float x, float zh, float zl) {
+  const float p = __fmul_rn(x, zh);
+  const float pe = __fmaf_rn(x, zl, __fmaf_rn(x, zh, -p));
+  float sh, e;
+  df_two_sum(h, p, sh, e);
+  h = sh;
+  l = __fadd_rn(l, __fadd_rn(e, pe));
+}
+
 // Restart rotation out[c] = sum_l V[l] Z[l][c], Z real (the Ritz vectors of
-// the real projected matrix) as double-float pairs, row-major [l][keep].
-// Block row blockIdx.y takes outputs [c0, c0 + cs): up to kRotCh outputs per
-// pass, so the basis is read ceil(keep / kRotCh) times, and a complex-by-real
-// product costs two double-float multiply-adds.
+// the real projected matrix) as double-float pairs, row-major [l][keep],
+// accumulated in double-float and rounded once to complex64.
+// Block row blockIdx.y takes outputs [c0, c0 + CH): up to kRotCh outputs per
+// pass, so the basis is read ceil(keep / kRotCh) times.
 // The chunk width CH is a template parameter, chosen per launch as the exact
 // chunk size: an unrolled loop guarded by a runtime count would issue its
 // masked-off iterations too.
 static constexpr int kRotCh = 16;
 template <int CH>
-__global__ void __launch_bounds__(kBS) k_df_rotate_re(int64_t n, const float4* __restrict__ V, int64_t ld, int msz,
+__global__ void __launch_bounds__(kBS) k_cf_rotate_re(int64_t n, const float2* __restrict__ V, int64_t ld, int msz,
                                                       const float2* __restrict__ Z, int keep,
-                                                      float4* __restrict__ out) {
+                                                      float2* __restrict__ out) {
   __shared__ float2 sZ[121 * CH];
   const int c0 = blockIdx.y * CH;
   const int cn = min(CH, keep - c0);
@@ -524,37 +540,34 @@ __global__ void __launch_bounds__(kBS) k_df_rotate_re(int64_t n, const float4* _
   }
   __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    float4 acc[CH];
+    float4 acc[CH];  // (re_hi, im_hi, re_lo, im_lo)
 #pragma unroll
     for (int c = 0; c < CH; ++c) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int l = 0; l < msz; ++l) {
-      const float4 v = V[(size_t)l * ld + i];
+      const float2 v = V[(size_t)l * ld + i];
 #pragma unroll
       for (int c = 0; c < CH; ++c) {  // padding columns of the last chunk have z = 0
         const float2 z = sZ[l * CH + c];
-        df_mac(acc[c].x, acc[c].z, v.x, v.z, z.x, z.y);
-        df_mac(acc[c].y, acc[c].w, v.y, v.w, z.x, z.y);
+        df_mac1(acc[c].x, acc[c].z, v.x, z.x, z.y);
+        df_mac1(acc[c].y, acc[c].w, v.y, z.x, z.y);
       }
     }
 #pragma unroll
     for (int c = 0; c < CH; ++c)
-      if (c < cn) {
-        df_renorm(acc[c].x, acc[c].z);
-        df_renorm(acc[c].y, acc[c].w);
-        out[(size_t)(c0 + c) * ld + i] = acc[c];
-      }
+      if (c < cn) out[(size_t)(c0 + c) * ld + i] = make_float2(__fadd_rn(acc[c].x, acc[c].z),
+                                                               __fadd_rn(acc[c].y, acc[c].w));
   }
 }
 
 // out[0..keep) = V[0..msz) Z in ceil(keep / kRotCh) chunks of equal width
-static void df_rotate_re(int64_t n, const float4* V, int64_t ld, int msz, const float2* Z, int keep, float4* out,
+static void cf_rotate_re(int64_t n, const float2* V, int64_t ld, int msz, const float2* Z, int keep, float2* out,
                          int gblk, cudaStream_t s) {
   const int nch = (keep + kRotCh - 1) / kRotCh, cs = (keep + nch - 1) / nch;
   const dim3 g(gblk, nch);
   switch (cs) {
 #define SED_ROT(W) \
   case W:          \
-    k_df_rotate_re<W><<<g, kBS, 0, s>>>(n, V, ld, msz, Z, keep, out); \
+    k_cf_rotate_re<W><<<g, kBS, 0, s>>>(n, V, ld, msz, Z, keep, out); \
     break;
     SED_ROT(1) SED_ROT(2) SED_ROT(3) SED_ROT(4) SED_ROT(5) SED_ROT(6) SED_ROT(7) SED_ROT(8)
     SED_ROT(9) SED_ROT(10) SED_ROT(11) SED_ROT(12) SED_ROT(13) SED_ROT(14) SED_ROT(15) SED_ROT(16)
@@ -634,14 +647,12 @@ struct VecOps {
   cudaStream_t s;
   DevBuf part, part1, coef, scal, flag;  // partial sums, coefficients, scalars, skip flag
   double* host = nullptr;          // pinned scratch
-  bool df = false;                 // vectors are double-float (mixed precision)
-  VecOps(int64_t n_, cudaStream_t s_, bool df_) : n(n_), s(s_), df(df_) {
+  VecOps(int64_t n_, cudaStream_t s_) : n(n_), s(s_) {
     const int64_t sms = device_sm_count();
     nblk = (int)std::max<int64_t>(1, std::min<int64_t>((n + kBS * 4 - 1) / (kBS * 4), sms * 4));
-    // the double-float dot kernel holds 80 registers a thread, so fewer of
-    // its blocks are resident: its grid is one full wave of them
+    // the complex64 dot kernel's grid is one full wave of its resident blocks
     int per_sm = 1;
-    SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_df_multidot, kBS, 0));
+    SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cf_multidot, kBS, 0));
     nblk_dot = (int)std::max<int64_t>(1, std::min<int64_t>((n + kBS * 4 - 1) / (kBS * 4),
                                                             sms * std::max(per_sm, 1)));
     part.alloc((size_t)std::max(nblk, nblk_dot) * 130 * 16);
@@ -654,39 +665,34 @@ struct VecOps {
   ~VecOps() {
     if (host) cudaFreeHost(host);
   }
-  // scal[slot] = |v|^2 (fp64: the vector is FP64 whatever the basis format)
-  void norm2(const double2* v, int slot, bool fp64 = false) {
-    if (df && !fp64)
-      k_df_norm2_part<<<nblk, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(v), part1.as<double>());
-    else
-      k_norm2_part<<<nblk, kBS, 0, s>>>(n, v, part1.as<double>());
+  // scal[slot] = |v|^2
+  void norm2(const double2* v, int slot) {
+    k_norm2_part<<<nblk, kBS, 0, s>>>(n, v, part1.as<double>());
+    k_reduce_part1<<<1, kBS, 0, s>>>(part1.as<double>(), nblk, scal.as<double>() + slot);
+  }
+  void norm2(const float2* v, int slot) {
+    k_cf_norm2_part<<<nblk, kBS, 0, s>>>(n, v, part1.as<double>());
     k_reduce_part1<<<1, kBS, 0, s>>>(part1.as<double>(), nblk, scal.as<double>() + slot);
   }
   // coef[off .. off+nv) (=|+=) V[0..nv)^H w
-  void multidot(const double2* V, int64_t ld, int nv, const double2* w, int off, bool acc, bool fp64 = false) {
-    int nb = nblk;
-    if (df && !fp64) {
-      nb = nblk_dot;
-      dim3 g(nb, (nv + 7) / 8);
-      k_df_multidot<<<g, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(V), ld, nv,
-                                       reinterpret_cast<const float4*>(w), part.as<double2>());
-    } else {
-      dim3 g(nb, nv);
-      k_multidot<<<g, kBS, 0, s>>>(n, V, ld, w, part.as<double2>());
-    }
-    k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), nb, coef.as<double2>() + off, acc ? 1 : 0);
+  void multidot(const double2* V, int64_t ld, int nv, const double2* w, int off, bool acc) {
+    k_multidot<<<dim3(nblk, nv), kBS, 0, s>>>(n, V, ld, w, part.as<double2>());
+    k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), nblk, coef.as<double2>() + off, acc ? 1 : 0);
+  }
+  void multidot(const float2* V, int64_t ld, int nv, const float2* w, int off, bool acc) {
+    k_cf_multidot<<<dim3(nblk_dot, (nv + kDotCh - 1) / kDotCh), kBS, 0, s>>>(n, V, ld, nv, w, part.as<double2>());
+    k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), nblk_dot, coef.as<double2>() + off, acc ? 1 : 0);
   }
   // w -= V[0..nv) coef[off..], optionally scal[slot] = |w|^2
-  // (skip: device flag of the selective reorthogonalisation, double-float only)
-  void multiaxpy(const double2* V, int64_t ld, int nv, double2* w, int off, int norm_slot, bool fp64 = false,
-                 const int* skip = nullptr) {
-    if (df && !fp64)
-      k_df_multiaxpy<<<nblk, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(V), ld, nv, coef.as<double2>() + off,
-                                          reinterpret_cast<float4*>(w),
-                                          norm_slot >= 0 ? part1.as<double>() : nullptr, skip);
-    else
-      k_multiaxpy<<<nblk, kBS, 0, s>>>(n, V, ld, nv, coef.as<double2>() + off, w,
-                                       norm_slot >= 0 ? part1.as<double>() : nullptr);
+  // (skip: device flag of the selective reorthogonalisation, complex64 only)
+  void multiaxpy(const double2* V, int64_t ld, int nv, double2* w, int off, int norm_slot) {
+    k_multiaxpy<<<nblk, kBS, 0, s>>>(n, V, ld, nv, coef.as<double2>() + off, w,
+                                     norm_slot >= 0 ? part1.as<double>() : nullptr);
+    if (norm_slot >= 0) k_reduce_part1<<<1, kBS, 0, s>>>(part1.as<double>(), nblk, scal.as<double>() + norm_slot);
+  }
+  void multiaxpy(const float2* V, int64_t ld, int nv, float2* w, int off, int norm_slot, const int* skip = nullptr) {
+    k_cf_multiaxpy<<<nblk, kBS, 0, s>>>(n, V, ld, nv, coef.as<double2>() + off, w,
+                                        norm_slot >= 0 ? part1.as<double>() : nullptr, skip);
     if (norm_slot >= 0) k_reduce_part1<<<1, kBS, 0, s>>>(part1.as<double>(), nblk, scal.as<double>() + norm_slot);
   }
   void check() { SED_CUDA(cudaGetLastError()); }
@@ -726,29 +732,47 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
   const int m = (int)std::min<int64_t>(std::max(krylovdim, 2 * nev + 1), std::min<int64_t>(D, 120));
   cudaStream_t s = op.stream;
   const int nslots = std::max(m + 1, 3 * nev + 1);
-  const int64_t ld = n;
-  DevBuf Vb((size_t)nslots * ld * 16), Wb((size_t)ld * 16), Rb((size_t)std::max(m, 5 * nev) * ld * 16);
-  DevBuf xs((size_t)ld * 16), xs64((size_t)ld * 16), Sd((size_t)130 * 130 * 16);
+  const int64_t ld = n;          // FP64 vectors
+  const int64_t ldc = cf_ld(n);  // complex64 vectors
+  // FP64 precision: basis V, work vector W, restart buffer R.  Mixed: the
+  // complex64 basis Vc and restart buffer Rc (they trade places at every
+  // restart) and work vector Wc; R is then the FP64 scratch of the start
+  // vector, the gather fallback and the Rayleigh-Ritz check.
+  DevBuf Vb(mixed ? 0 : (size_t)nslots * ld * 16), Wb(mixed ? 0 : (size_t)ld * 16);
+  DevBuf Rb((size_t)(mixed ? 5 * nev : std::max(m, 5 * nev)) * ld * 16);
+  DevBuf Vcb(mixed ? (size_t)nslots * ldc * 8 : 0), Rcb(mixed ? (size_t)nslots * ldc * 8 : 0);
+  DevBuf Wcb(mixed ? (size_t)ldc * 8 : 0);
+  DevBuf xs((size_t)ldc * 16), xs64((size_t)ld * 16), Sd((size_t)130 * 130 * 16);
   double2* V = Vb.as<double2>();
   double2* W = Wb.as<double2>();
   double2* R = Rb.as<double2>();
-  VecOps ops(n, s, mixed);
+  float2* Vc = Vcb.as<float2>();
+  float2* Rc = Rcb.as<float2>();
+  float2* Wc = Wcb.as<float2>();
+  const double2* Vout = V;  // where the returned eigenvectors end up (FP64)
+  VecOps ops(n, s);
   auto vec = [&](int j) { return V + (size_t)j * ld; };
+  auto vecc = [&](int j) { return Vc + (size_t)j * ldc; };
   const int gblk = ops.nblk;
-  auto normalize = [&](const double2* w, int slot, double2* out, bool to_xs) {
+  // v_{j+1} = w / sqrt(scal[slot]) and the next matvec input xs
+  auto normalize = [&](int slot, int j1) {
     if (mixed)
-      k_df_normalize<<<gblk, kBS, 0, s>>>(n, reinterpret_cast<const float4*>(w), ops.scal.as<double>() + slot,
-                                          reinterpret_cast<float4*>(out), C.stab.as<uint8_t>(),
-                                          to_xs ? xs.as<float2>() : nullptr);
+      k_cf_normalize<<<gblk, kBS, 0, s>>>(n, Wc, ops.scal.as<double>() + slot, vecc(j1), C.stab.as<uint8_t>(),
+                                          xs.as<float2>());
     else
-      k_normalize<double2><<<gblk, kBS, 0, s>>>(n, w, ops.scal.as<double>() + slot, out, C.stab.as<uint8_t>(),
-                                                to_xs ? xs.as<double2>() : nullptr);
+      k_normalize<double2><<<gblk, kBS, 0, s>>>(n, W, ops.scal.as<double>() + slot, vec(j1), C.stab.as<uint8_t>(),
+                                                xs.as<double2>());
   };
   // start vector
-  k_start<<<gblk, kBS, 0, s>>>(n, S.rowflag.as<uint8_t>(), seed, W);
-  if (mixed) k_df_from_d<<<gblk, kBS, 0, s>>>(n, W);
-  ops.norm2(W, 0);
-  normalize(W, 0, vec(0), true);
+  if (mixed) {
+    k_start<<<gblk, kBS, 0, s>>>(n, S.rowflag.as<uint8_t>(), seed, R);
+    k_d_to_cf<<<gblk, kBS, 0, s>>>(n, R, Wc);
+    ops.norm2(Wc, 0);
+  } else {
+    k_start<<<gblk, kBS, 0, s>>>(n, S.rowflag.as<uint8_t>(), seed, W);
+    ops.norm2(W, 0);
+  }
+  normalize(0, 0);
   ops.check();
 
   std::vector<double> T((size_t)m * m, 0.0), theta, Z;
@@ -759,24 +783,31 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
   for (;;) {
     int jend = m;
     for (int j = k; j < m; ++j) {
-      if (!mixed)
-        op_apply_orbit(op, xs.p, (double*)W, s);
-      else if (!op_apply_orbit_df(op, xs.p, (double*)W, s))
-        k_df_from_d<<<gblk, kBS, 0, s>>>(n, W);
       // local step: CGS against the two newest basis vectors (they carry the
       // large alpha_j and beta_{j-1} components), then one full CGS pass
       // against the whole basis; a second full pass only when the first one
       // removed more than half of the norm (Daniel-Gragg-Kaufman-Stewart).
       const int l0 = j > 0 ? j - 1 : 0;
-      ops.multidot(vec(l0), ld, j + 1 - l0, W, 0, false);
-      ops.multiaxpy(vec(l0), ld, j + 1 - l0, W, 0, 5);
-      ops.multidot(V, ld, j + 1, W, 128, false);
-      // mixed precision: the update only when the measured loss of
-      // orthogonality exceeds kSelReorth (decided on the device)
-      if (mixed)
+      if (mixed) {
+        if (!op_apply_orbit_cf(op, xs.p, Wc, s)) {  // no hop table: the FP64-output gather
+          op_apply_orbit(op, xs.p, (double*)R, s);
+          k_d_to_cf<<<gblk, kBS, 0, s>>>(n, R, Wc);
+        }
+        ops.multidot(vecc(l0), ldc, j + 1 - l0, Wc, 0, false);
+        ops.multiaxpy(vecc(l0), ldc, j + 1 - l0, Wc, 0, 5);
+        ops.multidot(Vc, ldc, j + 1, Wc, 128, false);
+        // the update only when the measured loss of orthogonality exceeds
+        // kSelReorth (decided on the device)
         k_sel_flag<<<1, 32, 0, s>>>(ops.coef.as<double2>() + 128, j + 1, ops.scal.as<double>() + 5, kSelReorth,
                                     ops.flag.as<int>());
-      ops.multiaxpy(V, ld, j + 1, W, 128, 1, false, mixed ? ops.flag.as<int>() : nullptr);
+        ops.multiaxpy(Vc, ldc, j + 1, Wc, 128, 1, ops.flag.as<int>());
+      } else {
+        op_apply_orbit(op, xs.p, (double*)W, s);
+        ops.multidot(vec(l0), ld, j + 1 - l0, W, 0, false);
+        ops.multiaxpy(vec(l0), ld, j + 1 - l0, W, 0, 5);
+        ops.multidot(V, ld, j + 1, W, 128, false);
+        ops.multiaxpy(V, ld, j + 1, W, 128, 1);
+      }
       ops.check();
       SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.as<double2>() + (j - l0), 16, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaMemcpyAsync(ops.host + 2, ops.coef.as<double2>() + 128 + j, 16, cudaMemcpyDeviceToHost, s));
@@ -790,8 +821,13 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
       double alpha = ops.host[0] + (skipped ? 0.0 : ops.host[2]);
       double nrm2 = skipped ? ops.host[5] : ops.host[4];
       if (!skipped && nrm2 < 0.5 * ops.host[5]) {
-        ops.multidot(V, ld, j + 1, W, 128, false);
-        ops.multiaxpy(V, ld, j + 1, W, 128, 1);
+        if (mixed) {
+          ops.multidot(Vc, ldc, j + 1, Wc, 128, false);
+          ops.multiaxpy(Vc, ldc, j + 1, Wc, 128, 1);
+        } else {
+          ops.multidot(V, ld, j + 1, W, 128, false);
+          ops.multiaxpy(V, ld, j + 1, W, 128, 1);
+        }
         ops.check();
         SED_CUDA(cudaMemcpyAsync(ops.host + 2, ops.coef.as<double2>() + 128 + j, 16, cudaMemcpyDeviceToHost, s));
         SED_CUDA(cudaMemcpyAsync(ops.host + 4, ops.scal.as<double>() + 1, 8, cudaMemcpyDeviceToHost, s));
@@ -806,7 +842,7 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
         jend = j + 1;
         break;
       }
-      normalize(W, 1, vec(j + 1), true);
+      normalize(1, j + 1);
     }
     const int msz = jend;
     std::vector<double> A((size_t)msz * msz);
@@ -847,19 +883,21 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
           Zf[((size_t)l * keep + c) * 2 + 1] = (float)(z - (double)h);
         }
       SED_CUDA(cudaMemcpyAsync(Sd.p, Zf.data(), Zf.size() * 4, cudaMemcpyHostToDevice, s));
-      df_rotate_re(n, reinterpret_cast<const float4*>(V), ld, msz, Sd.as<float2>(), keep,
-                   reinterpret_cast<float4*>(R), gblk, s);
+      cf_rotate_re(n, Vc, ldc, msz, Sd.as<float2>(), keep, Rc, gblk, s);
+      if (!final_rot)  // the last normalised residual direction (slot m) continues the basis
+        SED_CUDA(cudaMemcpyAsync(Rc + (size_t)keep * ldc, vecc(m), (size_t)ldc * 8, cudaMemcpyDeviceToDevice, s));
+      std::swap(Vc, Rc);  // the rotated vectors become the basis; no copy back
     } else {
       std::vector<double> Sc((size_t)msz * keep * 2, 0.0);
       for (int l = 0; l < msz; ++l)
         for (int c = 0; c < keep; ++c) Sc[((size_t)l * keep + c) * 2] = Z[(size_t)l * msz + c];
       SED_CUDA(cudaMemcpyAsync(Sd.p, Sc.data(), Sc.size() * 8, cudaMemcpyHostToDevice, s));
       k_rotate<<<dim3(gblk, (keep + 7) / 8), kBS, 0, s>>>(n, V, ld, msz, Sd.as<double2>(), keep, R);
+      SED_CUDA(cudaMemcpyAsync(V, R, (size_t)keep * ld * 16, cudaMemcpyDeviceToDevice, s));
+      if (!final_rot)  // the last normalised residual direction (slot m) continues the basis
+        SED_CUDA(cudaMemcpyAsync(vec(keep), vec(m), (size_t)ld * 16, cudaMemcpyDeviceToDevice, s));
     }
-    SED_CUDA(cudaMemcpyAsync(V, R, (size_t)keep * ld * 16, cudaMemcpyDeviceToDevice, s));
     ops.check();
-    if (!final_rot)  // the last normalised residual direction (slot m) continues the basis
-      SED_CUDA(cudaMemcpyAsync(vec(keep), vec(m), (size_t)ld * 16, cudaMemcpyDeviceToDevice, s));
     if (done && !mixed) {
       res.converged = nconv;
       res.max_residual = maxr;
@@ -880,7 +918,8 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
       double2* Yr = R + (size_t)nw * ld;
       double2* HYr = R + (size_t)(2 * nw) * ld;
       double2* B64 = R + (size_t)(3 * nw) * ld;  // FP64 copies of the Ritz vectors
-      k_df_to_d<<<gblk, kBS, 0, s>>>(n * nw, reinterpret_cast<const float4*>(V), B64);
+      double2* Wr = R + (size_t)(4 * nw) * ld;   // residual scratch
+      k_cf_to_d<<<dim3(gblk, nw), kBS, 0, s>>>(n, Vc, ldc, B64, ld);
       for (int i = 0; i < nw; ++i) {
         op_scale_to_xs_prec(op, (const double*)(B64 + (size_t)i * ld), xs64.p, false, s);
         op_apply_orbit64(op, xs64.p, (double*)(HB + (size_t)i * ld), s);
@@ -888,7 +927,7 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
       }
       std::vector<double> M((size_t)nw * nw * 2), lam, U;
       for (int bcol = 0; bcol < nw; ++bcol) {
-        ops.multidot(B64, ld, nw, HB + (size_t)bcol * ld, 0, false, true);
+        ops.multidot(B64, ld, nw, HB + (size_t)bcol * ld, 0, false);
         ops.check();
         SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.p, (size_t)nw * 16, cudaMemcpyDeviceToHost, s));
         SED_CUDA(cudaStreamSynchronize(s));
@@ -901,7 +940,7 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
       // G = B^H B = L L^H, B L^-H is orthonormal and projects H to L^-1 M L^-H
       std::vector<double> Gm((size_t)nw * nw * 2);
       for (int bcol = 0; bcol < nw; ++bcol) {
-        ops.multidot(B64, ld, nw, B64 + (size_t)bcol * ld, 0, false, true);
+        ops.multidot(B64, ld, nw, B64 + (size_t)bcol * ld, 0, false);
         ops.check();
         SED_CUDA(cudaMemcpyAsync(ops.host, ops.coef.p, (size_t)nw * 16, cudaMemcpyDeviceToHost, s));
         SED_CUDA(cudaStreamSynchronize(s));
@@ -927,8 +966,8 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
       k_rotate<<<dim3(gblk, (nw + 7) / 8), kBS, 0, s>>>(n, B64, ld, nw, Sd.as<double2>(), nw, Yr);
       k_rotate<<<dim3(gblk, (nw + 7) / 8), kBS, 0, s>>>(n, HB, ld, nw, Sd.as<double2>(), nw, HYr);
       for (int i = 0; i < nev_out; ++i) {
-        k_residual<<<gblk, kBS, 0, s>>>(n, HYr + (size_t)i * ld, Yr + (size_t)i * ld, lam[i], W);
-        ops.norm2(W, 4, true);
+        k_residual<<<gblk, kBS, 0, s>>>(n, HYr + (size_t)i * ld, Yr + (size_t)i * ld, lam[i], Wr);
+        ops.norm2(Wr, 4);
         SED_CUDA(cudaMemcpyAsync(ops.host + i, ops.scal.as<double>() + 4, 8, cudaMemcpyDeviceToHost, s));
       }
       ops.check();
@@ -948,7 +987,7 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
         res.max_delta = maxd;
         res.status = 0;
         for (int i = 0; i < nw; ++i) evals[i] = lam[i];
-        SED_CUDA(cudaMemcpyAsync(V, Yr, (size_t)nw * ld * 16, cudaMemcpyDeviceToDevice, s));
+        Vout = Yr;
         break;
       }
       if (invariant || stagnated || res.restarts >= maxiter || tau <= 1e-9) {
@@ -988,7 +1027,7 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
   if (evecs) {
     DevBuf ys((size_t)std::max<int64_t>(D, 1) * 16);
     for (int i = 0; i < nev_out; ++i) {
-      compress_vec(S, (const double*)(V + (size_t)i * ld), ys.as<double>(), s);
+      compress_vec(S, (const double*)(Vout + (size_t)i * ld), ys.as<double>(), s);
       SED_CUDA(cudaMemcpyAsync(evecs + (size_t)i * D * 2, ys.p, (size_t)D * 16, cudaMemcpyDeviceToHost, s));
       SED_CUDA(cudaStreamSynchronize(s));
     }

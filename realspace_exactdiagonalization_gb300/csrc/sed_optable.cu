@@ -28,7 +28,6 @@
 #include <complex>
 #include <vector>
 
-#include "sed_dfloat.cuh"
 #include "sed_internal.cuh"
 #include "sed_rowgather.cuh"
 
@@ -102,9 +101,9 @@ __global__ void k_optab_fill(int64_t n_orb, const uint64_t* __restrict__ reps, c
   }
 }
 
-// DF: the row is stored as a double-float complex (re_hi, im_hi, re_lo,
-// im_lo), the form the mixed-precision Lanczos keeps its vectors in
-template <class P, bool DF = false>
+// CF: the row is stored as complex64, the form the mixed-precision Lanczos
+// keeps its vectors in (y is then read as float2)
+template <class P, bool CF = false>
 __global__ void __launch_bounds__(kTabBS) k_apply_tab(int64_t n_orb, const uint64_t* __restrict__ hop,
                                                       const int64_t* __restrict__ sl_off,
                                                       const int32_t* __restrict__ sl_w,
@@ -125,7 +124,10 @@ __global__ void __launch_bounds__(kTabBS) k_apply_tab(int64_t n_orb, const uint6
   const int lane = threadIdx.x & 31;
   for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_orb; o += (int64_t)gridDim.x * blockDim.x) {
     if (!rowflag[o]) {
-      y[o] = make_double2(0.0, 0.0);
+      if (CF)
+        reinterpret_cast<float2*>(y)[o] = make_float2(0.f, 0.f);
+      else
+        y[o] = make_double2(0.0, 0.0);
       continue;
     }
     const int64_t sl = o >> 5;
@@ -147,11 +149,8 @@ __global__ void __launch_bounds__(kTabBS) k_apply_tab(int64_t n_orb, const uint6
     }
     const double is = s_isr[stab[o]];
     const double yr = (double)ar * is, yi = (double)ai * is;
-    if (DF) {
-      float4 d;
-      d_to_df(yr, d.x, d.z);
-      d_to_df(yi, d.y, d.w);
-      reinterpret_cast<float4*>(y)[o] = d;
+    if (CF) {
+      reinterpret_cast<float2*>(y)[o] = make_float2((float)yr, (float)yi);
     } else {
       y[o] = make_double2(yr, yi);
     }
@@ -269,7 +268,7 @@ void op_drop_table(OpImpl& op) {
   op.tab_records = op.tab_coefs = 0;
 }
 
-void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s, bool df_out) {
+void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s, bool cf_out) {
   const SectorImpl& S = *op.sec;
   const CatalogImpl& C = *S.cat;
   const int64_t n = C.n_orbits;
@@ -282,7 +281,7 @@ void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream
   // its record and gather loads, so every resident warp helps
   const int64_t want = (n + kTabBS - 1) / kTabBS;
   int per_sm = 1;
-  if (fp32 && df_out)
+  if (fp32 && cf_out)
     SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_tab<P32, true>, kTabBS, smem));
   else if (fp32)
     SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_tab<P32>, kTabBS, smem));
@@ -290,7 +289,7 @@ void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream
     SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_tab<P64>, kTabBS, smem));
   const int grid =
       (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * std::max(per_sm, 1)));
-  if (fp32 && df_out)
+  if (fp32 && cf_out)
     k_apply_tab<P32, true><<<grid, kTabBS, smem, s>>>(n, op.tab_hop.as<uint64_t>(), op.tab_off.as<int64_t>(),
                                                       op.tab_w.as<int32_t>(), op.tab_coef32.as<float2>(), smem_coef,
                                                       (const float2*)xs, op.diag.as<double2>(),

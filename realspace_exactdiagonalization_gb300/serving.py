@@ -118,12 +118,16 @@ def random_requests(families: Dict[str, L.ModelSpec], n: int, rate: float, seed:
 
 
 def solver_footprint(n_orbits: int, nev: int, krylovdim: int = 30) -> int:
-    """Device bytes one device-wide mixed solve holds (Lanczos basis, work
-    vectors, polish basis and operator tables)."""
+    """Device bytes one device-wide mixed solve holds: the complex64 Lanczos
+    basis, restart buffer and work vector (8 B per element, padded to 64
+    elements), the FP64 polish block and matvec inputs (16 B per element),
+    and the operator's per-orbit tables."""
     nw = nev + 2
     m = max(krylovdim, 2 * nw + 1)
-    slots = max(m + 1, 3 * nw + 1) + max(m, 5 * nw) + 4
-    return int(slots * n_orbits * 16 + n_orbits * 17 + (64 << 20))
+    slots8 = 2 * max(m + 1, 3 * nw + 1) + 1
+    slots16 = 5 * nw + 2
+    padded = (n_orbits + 63) // 64 * 64
+    return int(slots8 * padded * 8 + slots16 * padded * 16 + n_orbits * 17 + (64 << 20))
 
 
 class SectorServer:
