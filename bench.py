@@ -56,10 +56,11 @@ def config(n_req, extra=None, grid=8):
     return c
 
 
-def lanczos_bytes(nmv: int, dim: int, m: int = 24, keep: int = 15, n_polish: int = 6) -> float:
+def lanczos_bytes(nmv: int, dim: int, m: int = 24, keep: int = 15, n_polish: int = 6, elem: int = 8) -> float:
     """Algorithmic bytes of the Lanczos vector work of one batched solve with
-    ``nmv`` matvecs on a sector of dimension ``dim``, double-float vectors
-    (16 B per element): each iteration streams three vectors (the matvec's
+    ``nmv`` matvecs on a sector of dimension ``dim``, ``elem`` bytes per vector
+    element (8: the mixed kernel's complex64 basis; 16: the FP64 kernel's
+    double-float basis): each iteration streams three vectors (the matvec's
     output, and the normalisation's read of it and write of the new basis
     vector) and reads the k basis vectors the reorthogonalisation's dot
     products sweep; each restart rotates m vectors into ``keep``.  k follows the
@@ -74,7 +75,7 @@ def lanczos_bytes(nmv: int, dim: int, m: int = 24, keep: int = 15, n_polish: int
     full, part = divmod(rest, cyc)
     ksum += full * sum(range(keep + 1, m + 1)) + sum(range(keep + 1, keep + 1 + part))
     restarts = full + (1 if part else 0) + (1 if steps >= m else 0)
-    return float((3 * steps + ksum + restarts * (m + keep)) * dim * 16)
+    return float((3 * steps + ksum + restarts * (m + keep)) * dim * elem)
 
 
 def profiled_traffic_per_sector():
@@ -309,7 +310,7 @@ def run_ours(args, rank, world):
     s = 8  # complex64 matvec input
     b_mv = dims * (8 + 4 + 2 * s) + stats["hops"] * (4 + 1 + 4 + s)
     bytes_mv = float((nmv * b_mv).sum())
-    bytes_lz = float(sum(lanczos_bytes(int(k), int(d)) for k, d in zip(nmv, dims)))
+    bytes_lz = float(sum(lanczos_bytes(int(k), int(d), elem=8) for k, d in zip(nmv, dims)))
     bytes_launch = bytes_mv + bytes_lz
     t_launch = tot_ms / args.steps / 1e3
     achieved = bytes_launch / t_launch / 1e9

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <mutex>
 #include <thread>
+#include <type_traits>
 #include <unordered_map>
 
 #include "../../include/sed_capi.h"
@@ -217,6 +218,7 @@ __device__ __forceinline__ void block_sum_df16(float (&h)[16], float (&l)[16], d
 }
 
 // store one matvec output row: double-float from an FP32 or FP64 accumulator
+// (the FP64 kernel's work vector), or FP64 (the FP64 polish)
 __device__ __forceinline__ void store_row(float4* w, int64_t o, float yr, float yi) {
   w[o] = make_float4(yr, yi, 0.f, 0.f);
 }
@@ -232,6 +234,12 @@ __device__ __forceinline__ void store_row(double2* w, int64_t o, float yr, float
 }
 __device__ __forceinline__ void zero_row(float4* w, int64_t o) { w[o] = make_float4(0.f, 0.f, 0.f, 0.f); }
 __device__ __forceinline__ void zero_row(double2* w, int64_t o) { w[o] = make_double2(0.0, 0.0); }
+// complex64 rows (the mixed kernel's work vector)
+__device__ __forceinline__ void store_row(float2* w, int64_t o, float yr, float yi) { w[o] = make_float2(yr, yi); }
+__device__ __forceinline__ void store_row(float2* w, int64_t o, double yr, double yi) {
+  w[o] = make_float2((float)yr, (float)yi);
+}
+__device__ __forceinline__ void zero_row(float2* w, int64_t o) { w[o] = make_float2(0.f, 0.f); }
 
 // Jacobi rotation (c, s) for the 2x2 block [[app, apq], [apq, aqq]].  The
 // angle only has to shrink apq, not zero it exactly, so it is computed in
@@ -1043,6 +1051,261 @@ __device__ __forceinline__ void block_normalize(const BatchArgs& a, const double
   }
 }
 
+// ------------------------------------------- complex64 vectors (mixed)
+// In mixed precision the Lanczos basis, restart buffer and work vector are
+// complex64: 8 bytes per element, half the traffic of the double-float
+// vectors the FP64 kernel keeps.  Each stored value is rounded once to FP32
+// from an accurately computed one:
+// * dot products accumulate FP32 products per thread (a thread sums
+//   n_orb / 512 elements) and add the thread partials in double-float, then
+//   FP64, over the block;
+// * updates w -= sum_q c_q v_q apply each coefficient as hi + lo floats, so
+//   the large local coefficients (alpha, beta) cancel without losing bits,
+//   and |w|^2 is summed in double-float;
+// * restart rotations accumulate in double-float (TwoProd, TwoSum);
+// * the normalisation multiplies by 1/|w| as hi + lo floats.
+// The storage rounding (2^-24) is the size of the complex64 matvec's own
+// rounding, which already perturbs the recurrence at that level; the
+// FP64-class Rayleigh-Ritz check bounds the eigenvalues.  The check itself
+// runs on double-float copies of the Ritz block.
+
+// the prefetch distance in chunks for complex64 sweeps: the byte volume in
+// flight of the double-float sweeps, at half the bytes per chunk
+__device__ __forceinline__ int cf_prefetch_dist(int nv) { return 2 * prefetch_dist(nv); }
+
+// as prefetch_chunks, for vectors of 8-byte elements (the byte count rounded
+// up to 16 inside the vector's padding: ld is a multiple of 32)
+__device__ __forceinline__ void prefetch_chunks(const BatchArgs& a, const float2* V, int nv, int64_t c0, int nch,
+                                                int span, int t) {
+  if (nch > 0 && t < nv * nch) {
+    const int64_t p0 = (c0 + t / nv) * span;
+    if (p0 < a.n_orb)
+      l2_prefetch_bulk(V + (size_t)(t % nv) * a.ld + p0,
+                       ((uint32_t)min((int64_t)span, a.n_orb - p0) * 8u + 15u) & ~15u);
+  }
+}
+
+// coef[0..nv) = V[0..nv)^H w for complex64 vectors, in chunks of 8
+__device__ void cf_dots(const BatchArgs& a, const float2* V, int nv, const float2* w, double* red, double2* coef) {
+  for (int l0 = 0; l0 < nv; l0 += 8) {
+    float h[16], l[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) h[c] = l[c] = 0.f;
+    const int cn = min(8, nv - l0);
+    const int span = blockDim.x, pd = cf_prefetch_dist(cn);
+    const float2* Vl = V + (size_t)l0 * a.ld;
+    prefetch_chunks(a, Vl, cn, 0, pd, span, threadIdx.x);
+    for (int64_t o0 = 0, ch = 0; o0 < a.n_orb; o0 += span, ++ch) {
+      if (pd) prefetch_chunks(a, Vl, cn, ch + pd, 1, span, threadIdx.x);
+      const int64_t o = o0 + threadIdx.x;
+      if (o >= a.n_orb) continue;
+      const float2 x = w[o];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn) {
+          const float2 v = Vl[(size_t)c * a.ld + o];
+          // conj(v) x = (vr xr + vi xi) + i (vr xi - vi xr)
+          h[2 * c] = __fmaf_rn(v.x, x.x, __fmaf_rn(v.y, x.y, h[2 * c]));
+          h[2 * c + 1] = __fmaf_rn(v.x, x.y, __fmaf_rn(-v.y, x.x, h[2 * c + 1]));
+        }
+    }
+    block_sum_df16(h, l, red, reinterpret_cast<double*>(coef + l0));
+  }
+}
+
+// x -= c v for one complex64 element, c as (re_hi, im_hi, re_lo, im_lo)
+__device__ __forceinline__ void cf_sub(float& xr, float& xi, float4 c, float2 v) {
+  xr = __fmaf_rn(-c.x, v.x, xr);
+  xr = __fmaf_rn(c.y, v.y, xr);
+  xi = __fmaf_rn(-c.x, v.y, xi);
+  xi = __fmaf_rn(-c.y, v.x, xi);
+  xr = __fmaf_rn(-c.z, v.x, xr);
+  xr = __fmaf_rn(c.w, v.y, xr);
+  xi = __fmaf_rn(-c.z, v.y, xi);
+  xi = __fmaf_rn(-c.w, v.x, xi);
+}
+
+// The local step's update folded into the first chunk of the full pass
+// (complex64 counterpart of df_dots_local): w -= Vl[0..nl) cl, then
+// coef[0..cn) = V[0..cn)^H w (cn <= 7) and |w|^2 (slot 14, double-float) in
+// the same sweep and block reduction.  Returns |w|^2.
+__device__ __noinline__ double cf_dots_local(const BatchArgs& a, const float2* V, int cn, const float2* Vl, int nl,
+                                             const float4* cl, float2* w, double* red, double2* coef) {
+  float h[16], l[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) h[c] = l[c] = 0.f;
+  const int span = blockDim.x, pd = cf_prefetch_dist(cn);
+  prefetch_chunks(a, V, cn, 0, pd, span, threadIdx.x);
+  for (int64_t o0 = 0, ch = 0; o0 < a.n_orb; o0 += span, ++ch) {
+    if (pd) prefetch_chunks(a, V, cn, ch + pd, 1, span, threadIdx.x);
+    const int64_t o = o0 + threadIdx.x;
+    if (o >= a.n_orb) continue;
+    const float2 x0 = w[o];
+    float xr = x0.x, xi = x0.y;
+    for (int q = 0; q < nl; ++q) cf_sub(xr, xi, cl[q], Vl[(size_t)q * a.ld + o]);
+    w[o] = make_float2(xr, xi);
+    df_mac(h[14], l[14], xr, 0.f, xr, 0.f);
+    df_mac(h[14], l[14], xi, 0.f, xi, 0.f);
+#pragma unroll
+    for (int c = 0; c < 7; ++c)
+      if (c < cn) {
+        const float2 v = V[(size_t)c * a.ld + o];
+        h[2 * c] = __fmaf_rn(v.x, xr, __fmaf_rn(v.y, xi, h[2 * c]));
+        h[2 * c + 1] = __fmaf_rn(v.x, xi, __fmaf_rn(-v.y, xr, h[2 * c + 1]));
+      }
+  }
+  double* out = reinterpret_cast<double*>(coef);
+  block_sum_df16(h, l, red, out);
+  return out[14];
+}
+
+// w -= V[0..nv) c (c as hi + lo floats in shared memory); returns this
+// thread's partial |w|^2 (double-float, then FP64).  Loads are issued in
+// groups of eight vectors before the arithmetic; out of line like df_axpy.
+__device__ __noinline__ double cf_axpy(const BatchArgs& a, const float2* V, int nv, const float4* cdf, float2* w) {
+  float nh = 0.f, nl = 0.f;
+  const int span = blockDim.x, pd = cf_prefetch_dist(nv);
+  prefetch_chunks(a, V, nv, 0, pd, span, threadIdx.x);
+  for (int64_t o0 = 0, ch = 0; o0 < a.n_orb; o0 += span, ++ch) {
+    if (pd) prefetch_chunks(a, V, nv, ch + pd, 1, span, threadIdx.x);
+    const int64_t o = o0 + threadIdx.x;
+    if (o >= a.n_orb) continue;
+    const float2 x0 = w[o];
+    float xr = x0.x, xi = x0.y;
+    for (int q0 = 0; q0 < nv; q0 += 8) {
+      const int cn = min(8, nv - q0);
+      float2 v[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn) v[c] = V[(size_t)(q0 + c) * a.ld + o];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn) cf_sub(xr, xi, cdf[q0 + c], v[c]);
+    }
+    w[o] = make_float2(xr, xi);
+    df_mac(nh, nl, xr, 0.f, xr, 0.f);
+    df_mac(nh, nl, xi, 0.f, xi, 0.f);
+  }
+  return df_to_d(nh, nl);
+}
+
+// v = w * inv (inv as hi + lo floats, one rounding of the product) and the
+// complex64 matvec input x = sqrt(stab) v
+__device__ __forceinline__ void cf_normalize(const BatchArgs& a, const float2* w, double inv, float2* v, float2* x,
+                                             const float* s_sqrtf) {
+  float ih, il;
+  d_to_df(inv, ih, il);
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    const float2 y = w[o];
+    const float rx = __fmaf_rn(y.x, ih, __fmul_rn(y.x, il));
+    const float ry = __fmaf_rn(y.y, ih, __fmul_rn(y.y, il));
+    if (v) v[o] = make_float2(rx, ry);
+    if (x) {
+      const float sq = s_sqrtf[a.stab[o]];
+      x[o] = make_float2(__fmul_rn(rx, sq), __fmul_rn(ry, sq));
+    }
+  }
+}
+
+// (h, l) += x (zh + zl) for a float x: TwoProd of the leading product, the
+// rest folded into the low word
+__device__ __forceinline__ void df_mac1(float& h, float& l, float x, float zh, float zl) {
+  const float p = __fmul_rn(x, zh);
+  const float pe = __fmaf_rn(x, zl, __fmaf_rn(x, zh, -p));
+  float sh, e;
+  df_two_sum(h, p, sh, e);
+  h = sh;
+  l = __fadd_rn(l, __fadd_rn(e, pe));
+}
+
+// out[c] = sum_l V[l] Z[l][c] for c < keep (complex64 counterpart of
+// df_rotate: same chunking and half-block split), accumulated in
+// double-float and rounded once to complex64
+__device__ void cf_rotate(const BatchArgs& a, const float2* V, int msz, const float2* Z, int keep, float2* out) {
+  const int nch = (keep + 7) / 8;
+  const int ng = nch > 1 ? 2 : 1;
+  const int gsz = blockDim.x / ng, grp = threadIdx.x / gsz, t = threadIdx.x - grp * gsz;
+  for (int ch = grp; ch < nch; ch += ng) {
+    const int c0 = ch * 8, cn = min(8, keep - c0);
+    for (int64_t o = t; o < a.n_orb; o += gsz) {
+      float4 acc[8];  // (re_hi, im_hi, re_lo, im_lo)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int q0 = 0; q0 < msz; q0 += 4) {
+        const int qn = min(4, msz - q0);
+        float2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (u < qn) v[u] = V[(size_t)(q0 + u) * a.ld + o];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (u < qn) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+              if (c < cn) {
+                const float2 z = Z[(q0 + u) * kMaxM + c0 + c];
+                df_mac1(acc[c].x, acc[c].z, v[u].x, z.x, z.y);
+                df_mac1(acc[c].y, acc[c].w, v[u].y, z.x, z.y);
+              }
+          }
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < cn)
+          out[(size_t)(c0 + c) * a.ld + o] = make_float2(__fadd_rn(acc[c].x, acc[c].z), __fadd_rn(acc[c].y, acc[c].w));
+    }
+  }
+}
+
+// The Lanczos vector operations of k_batch, by basis type: double-float
+// (float4, FP64 kernel) or complex64 (float2, mixed kernel).
+__device__ __forceinline__ void lz_dots(const BatchArgs& a, const float4* V, int nv, const float4* w, double* red,
+                                        double2* coef) {
+  df_dots(a, V, nv, w, red, coef);
+}
+__device__ __forceinline__ void lz_dots(const BatchArgs& a, const float2* V, int nv, const float2* w, double* red,
+                                        double2* coef) {
+  cf_dots(a, V, nv, w, red, coef);
+}
+__device__ __forceinline__ double lz_dots_local(const BatchArgs& a, const float4* V, int cn, const float4* Vl, int nl,
+                                                const float4* cl, float4* w, double* red, double2* coef) {
+  return df_dots_local(a, V, cn, Vl, nl, cl, w, red, coef);
+}
+__device__ __forceinline__ double lz_dots_local(const BatchArgs& a, const float2* V, int cn, const float2* Vl, int nl,
+                                                const float4* cl, float2* w, double* red, double2* coef) {
+  return cf_dots_local(a, V, cn, Vl, nl, cl, w, red, coef);
+}
+__device__ __forceinline__ double lz_axpy(const BatchArgs& a, const float4* V, int nv, const float4* cdf, float4* w) {
+  return df_axpy(a, V, nv, cdf, w);
+}
+__device__ __forceinline__ double lz_axpy(const BatchArgs& a, const float2* V, int nv, const float4* cdf, float2* w) {
+  return cf_axpy(a, V, nv, cdf, w);
+}
+template <class VT>
+__device__ __forceinline__ void lz_normalize(const BatchArgs& a, const float4* w, double inv, float4* v, VT* x,
+                                             const float* s_sqrtf, const double* s_sqrt) {
+  df_normalize<VT>(a, w, inv, v, x, s_sqrtf, s_sqrt);
+}
+template <class VT>
+__device__ __forceinline__ void lz_normalize(const BatchArgs& a, const float2* w, double inv, float2* v, VT* x,
+                                             const float* s_sqrtf, const double*) {
+  static_assert(sizeof(VT) == 8, "the complex64 basis feeds the complex64 matvec");
+  cf_normalize(a, w, inv, v, reinterpret_cast<float2*>(x), s_sqrtf);
+}
+__device__ __forceinline__ void lz_rotate(const BatchArgs& a, const float4* V, int msz, const float2* Z, int keep,
+                                          float4* out) {
+  df_rotate(a, V, msz, Z, keep, out);
+}
+__device__ __forceinline__ void lz_rotate(const BatchArgs& a, const float2* V, int msz, const float2* Z, int keep,
+                                          float2* out) {
+  cf_rotate(a, V, msz, Z, keep, out);
+}
+// one basis element as double-float and as FP64
+__device__ __forceinline__ float4 lz_to_df(float4 v) { return v; }
+__device__ __forceinline__ float4 lz_to_df(float2 v) { return make_float4(v.x, v.y, 0.f, 0.f); }
+__device__ __forceinline__ double2 lz_to_d(float4 v) { return make_double2(df_to_d(v.x, v.z), df_to_d(v.y, v.w)); }
+__device__ __forceinline__ double2 lz_to_d(float2 v) { return make_double2(v.x, v.y); }
+
 // ---------------------------------------------------------------- the kernel
 // Rayleigh-Ritz on a block B that is only semi-orthogonal (kSelReorth): with
 // G = B^H B = L L^H (Cholesky), B L^-H is orthonormal and its projected matrix
@@ -1181,13 +1444,16 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
     d_to_df(s_isr[i], s_isr_df[i].x, s_isr_df[i].y);
   }
 
-  // Lanczos basis, restart buffer and work vector: double-float complex.  The
-  // basis and restart buffers have the same capacity and trade places at
-  // every restart, so the rotated vectors are never copied back.
+  // Lanczos basis, restart buffer and work vector: complex64 in the mixed
+  // kernel, double-float in the FP64 kernel (each buffer holds 16 bytes per
+  // element either way).  The basis and restart buffers have the same
+  // capacity and trade places at every restart, so the rotated vectors are
+  // never copied back.
+  using BV = typename std::conditional<sizeof(typename P::S) == 4, float2, float4>::type;
   const size_t slots = (size_t)max(a.m + 1, 5 * (a.nev + 2));
-  float4* Vb = reinterpret_cast<float4*>(a.V + (size_t)blockIdx.x * slots * a.ld);
-  float4* Rb = reinterpret_cast<float4*>(a.R + (size_t)blockIdx.x * slots * a.ld);
-  float4* W = reinterpret_cast<float4*>(a.W + (size_t)blockIdx.x * a.ld);
+  BV* Vb = reinterpret_cast<BV*>(a.V + (size_t)blockIdx.x * slots * a.ld);
+  BV* Rb = reinterpret_cast<BV*>(a.R + (size_t)blockIdx.x * slots * a.ld);
+  BV* W = reinterpret_cast<BV*>(a.W + (size_t)blockIdx.x * a.ld);
   double2* X64 = a.X64 + (size_t)blockIdx.x * a.ld;
   double2* tchi64 = a.tchi64 + (size_t)blockIdx.x * a.n_bil * a.G;
   uint8_t* rowflag = a.rowflag + (size_t)blockIdx.x * a.ld;
@@ -1399,7 +1665,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       nrm += v.x * v.x + v.y * v.y;
     }
     nrm = block_sum1(nrm, s_red, s_misc);
-    df_normalize<V>(a, W, 1.0 / sqrt(nrm), Vb, x, s_sqrtf, s_sqrt);
+    lz_normalize<V>(a, W, 1.0 / sqrt(nrm), Vb, x, s_sqrtf, s_sqrt);
     for (int i = threadIdx.x; i < kMaxM * kMaxM; i += blockDim.x) s_T[i] = 0.0;
     __syncthreads();
 
@@ -1410,7 +1676,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
     for (;;) {
       int jend = m;
       for (int j = k; j < m; ++j) {
-        float4* vj = Vb + (size_t)j * a.ld;
+        BV* vj = Vb + (size_t)j * a.ld;
         if (a.use_tab)
           block_matvec_tab<P>(a, x, s_tchi, s_pwc, s_isr, s_isrf, rowflag, W);
         else
@@ -1423,14 +1689,14 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         // a second full pass only when the first removed more than half of
         // the norm (Daniel-Gragg-Kaufman-Stewart).
         const int l0 = j > 0 ? j - 1 : 0;
-        df_dots(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, W, s_red, s_coef);
+        lz_dots(a, Vb + (size_t)l0 * a.ld, j + 1 - l0, W, s_red, s_coef);
         df_coefs(s_coef, j + 1 - l0, s_cdf);
         double alpha = s_coef[j - l0].x;
         // the local update rides on the first chunk of the full pass's dots
         const int c0n = min(7, j + 1);
-        const double n0 = df_dots_local(a, Vb, c0n, Vb + (size_t)l0 * a.ld, j + 1 - l0, s_cdf, W, s_red,
+        const double n0 = lz_dots_local(a, Vb, c0n, Vb + (size_t)l0 * a.ld, j + 1 - l0, s_cdf, W, s_red,
                                         s_coef + kMaxM + 8);
-        if (j + 1 > c0n) df_dots(a, Vb + (size_t)c0n * a.ld, j + 1 - c0n, W, s_red, s_coef + kMaxM + 8 + c0n);
+        if (j + 1 > c0n) lz_dots(a, Vb + (size_t)c0n * a.ld, j + 1 - c0n, W, s_red, s_coef + kMaxM + 8 + c0n);
         // mixed precision: update only when the measured loss of orthogonality
         // exceeds kSelReorth (the test is uniform over the block)
         double cmax = 0.0;
@@ -1442,15 +1708,15 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         double nf = n0;
         if (!mixed || cmax > kSelReorth * sqrt(n0)) {
           df_coefs(s_coef + kMaxM + 8, j + 1, s_cdf);
-          double n1 = df_axpy(a, Vb, j + 1, s_cdf, W);
+          double n1 = lz_axpy(a, Vb, j + 1, s_cdf, W);
           alpha += s_coef[kMaxM + 8 + j].x;
           __syncthreads();
           n1 = block_sum1(n1, s_red, s_misc + 1);
           nf = n1;
           if (n1 < 0.5 * n0) {
-            df_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
+            lz_dots(a, Vb, j + 1, W, s_red, s_coef + kMaxM + 8);
             df_coefs(s_coef + kMaxM + 8, j + 1, s_cdf);
-            double n2 = df_axpy(a, Vb, j + 1, s_cdf, W);
+            double n2 = lz_axpy(a, Vb, j + 1, s_cdf, W);
             alpha += s_coef[kMaxM + 8 + j].x;
             __syncthreads();
             nf = block_sum1(n2, s_red, s_misc + 2);
@@ -1465,7 +1731,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           jend = j + 1;
           break;
         }
-        df_normalize<V>(a, W, 1.0 / beta, vj + a.ld, x, s_sqrtf, s_sqrt);
+        lz_normalize<V>(a, W, 1.0 / beta, vj + a.ld, x, s_sqrtf, s_sqrt);
         __syncthreads();
         (void)vj;
       }
@@ -1505,13 +1771,13 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         s_zdf[q * kMaxM + c] = z;
       }
       __syncthreads();
-      df_rotate(a, Vb, msz, s_zdf, keep, Rb);
+      lz_rotate(a, Vb, msz, s_zdf, keep, Rb);
       if (!final_rot)  // the last normalised residual direction continues the basis
         for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
           Rb[(size_t)keep * a.ld + o] = Vb[(size_t)m * a.ld + o];
       __syncthreads();
       {
-        float4* t = Vb;
+        BV* t = Vb;
         Vb = Rb;
         Rb = t;
       }
@@ -1537,15 +1803,23 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
 #pragma unroll
         for (int i = 0; i < kMaxNev; ++i) rr[i] = 0.0;
         if (a.use_tab) {
-          // double-float polish: B = Vb[0..nw) as stored, H B through the
-          // hop table with double-float coefficients, Rayleigh-Ritz and the
-          // FP64-class residuals of the rotated pairs
-          float4* HB = Rb;
-          float4* Yr = Rb + (size_t)nw * a.ld;
-          float4* HYr = Rb + (size_t)(2 * nw) * a.ld;
+          // double-float polish: B = the Ritz block Vb[0..nw) in
+          // double-float (Bd), H B through the hop table with double-float
+          // coefficients, Rayleigh-Ritz and the FP64-class residuals of the
+          // rotated pairs.  The free restart buffer holds HB, Yr, HYr and Bd
+          // (4 nw <= slots double-float vectors).
+          float4* R4 = reinterpret_cast<float4*>(Rb);
+          float4* HB = R4;
+          float4* Yr = R4 + (size_t)nw * a.ld;
+          float4* HYr = R4 + (size_t)(2 * nw) * a.ld;
+          float4* Bd = R4 + (size_t)(3 * nw) * a.ld;
           float4* Xd = reinterpret_cast<float4*>(X64);
+          for (int i = 0; i < nw; ++i)
+            for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x)
+              Bd[(size_t)i * a.ld + o] = lz_to_df(Vb[(size_t)i * a.ld + o]);
+          __syncthreads();
           for (int i = 0; i < nw; ++i) {
-            df_scale_xs(a, Vb + (size_t)i * a.ld, Xd, s_sq_df);
+            df_scale_xs(a, Bd + (size_t)i * a.ld, Xd, s_sq_df);
             __syncthreads();
             block_matvec_tab_df(a, Xd, reinterpret_cast<const float4*>(tchi64),
                                 reinterpret_cast<const float4*>(pwc64), s_isr_df, rowflag, HB + (size_t)i * a.ld);
@@ -1553,10 +1827,10 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           }
           n64 += nw;
           for (int bcol = 0; bcol < nw; ++bcol) {
-            df_dots(a, Vb, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
+            df_dots(a, Bd, nw, HB + (size_t)bcol * a.ld, s_red, s_coef);
             if (threadIdx.x < nw) M[threadIdx.x * kPolCap + bcol] = s_coef[threadIdx.x];
             __syncthreads();
-            df_dots(a, Vb, nw, Vb + (size_t)bcol * a.ld, s_red, s_coef);
+            df_dots(a, Bd, nw, Bd + (size_t)bcol * a.ld, s_red, s_coef);
             if (threadIdx.x < nw) Gm[threadIdx.x * kMaxNev + bcol] = s_coef[threadIdx.x];
             __syncthreads();
           }
@@ -1582,7 +1856,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
             s_zc[l * kMaxNev + c] = t;
           }
           __syncthreads();
-          df_rotate_c(a, Vb, nw, s_zc, nw, Yr);
+          df_rotate_c(a, Bd, nw, s_zc, nw, Yr);
           df_rotate_c(a, HB, nw, s_zc, nw, HYr);
           __syncthreads();
           float2 lam[kMaxNev];
@@ -1608,8 +1882,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           double2* B64 = Rb64 + (size_t)(3 * nw) * a.ld;  // the Ritz vectors in FP64
           for (int i = 0; i < nw; ++i)
             for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
-              const float4 v = Vb[(size_t)i * a.ld + o];
-              B64[(size_t)i * a.ld + o] = make_double2(df_to_d(v.x, v.z), df_to_d(v.y, v.w));
+              B64[(size_t)i * a.ld + o] = lz_to_d(Vb[(size_t)i * a.ld + o]);
             }
           __syncthreads();
           for (int i = 0; i < nw; ++i) {
@@ -1675,15 +1948,16 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
           // the check used x's global buffer for its FP64-class vectors: the
           // Lanczos resumes from the continuation vector (slot keep), so its
           // scaled copy, as df_normalize wrote it, goes back into x
-          const float4* vk = Vb + (size_t)keep * a.ld;
+          const BV* vk = Vb + (size_t)keep * a.ld;
           for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
-            const float4 v = vk[o];
+            const BV v = vk[o];
             if (sizeof(V) == 8) {
               const float sq = s_sqrtf[a.stab[o]];
-              reinterpret_cast<float2*>(x)[o] = make_float2(v.x * sq, v.y * sq);
+              reinterpret_cast<float2*>(x)[o] = make_float2(__fmul_rn(v.x, sq), __fmul_rn(v.y, sq));
             } else {
               const double sq = s_sqrt[a.stab[o]];
-              reinterpret_cast<double2*>(x)[o] = make_double2(df_to_d(v.x, v.z) * sq, df_to_d(v.y, v.w) * sq);
+              const double2 d = lz_to_d(v);
+              reinterpret_cast<double2*>(x)[o] = make_double2(d.x * sq, d.y * sq);
             }
           }
           __syncthreads();
