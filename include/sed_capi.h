@@ -198,6 +198,14 @@ int sed_op_info(const sed_op* op, int64_t* dim, int64_t* n_orbits, int64_t* hops
 int sed_op_set_hop_table(sed_op* op, int mode);
 int sed_op_hop_table_info(const sed_op* op, int32_t* built, int64_t* records, int64_t* bytes);
 int sed_op_set_stream(sed_op* op, void* cuda_stream);
+/* Scheduling priority of the operator's own stream (no counterpart in the
+ * reference, which runs one sector at a time): 1 = the device's greatest
+ * stream priority, 0 = its least (the default).  The operator gets a new
+ * stream of that priority, ordered after its previous work; when several
+ * solves share the GPU, the kernels of a high-priority solve are scheduled
+ * before the queued kernels of low-priority ones.  Replaces a stream set by
+ * sed_op_set_stream. */
+int sed_op_set_priority(sed_op* op, int high);
 /* Orbit-indexed matvec for benchmarking the kernel alone: xs_dev holds
  * sqrt(stab)*x in the op's precision (complex64 or complex128, length
  * n_orbits), y_dev receives complex128 H x (length n_orbits).  Asynchronous. */

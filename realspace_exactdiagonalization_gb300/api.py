@@ -385,6 +385,12 @@ class MatrixFreeHamiltonian(_Handle):
         check(_lib.load().sed_op_apply_shape(self._h, int(bool(complex64)), C.byref(t), C.byref(b)))
         return t.value, b.value
 
+    def set_priority(self, high: bool) -> None:
+        """Scheduling priority of this operator's stream when several solves
+        share the GPU (sed_op_set_priority): high-priority kernels are
+        scheduled before the queued kernels of low-priority solves."""
+        check(_lib.load().sed_op_set_priority(self._h, 1 if high else 0))
+
     def set_hop_table(self, mode: int) -> None:
         """The stored form of this operator's matvec (8 bytes per hop): 0 off,
         1 built at the first solve when it fits (default), 2 built now."""

@@ -248,6 +248,26 @@ int sed_op_set_stream(sed_op* op, void* stream) {
     op->p->stream = (cudaStream_t)stream;
   });
 }
+int sed_op_set_priority(sed_op* op, int high) {
+  return guarded([&] {
+    REQ(op, "NULL operator");
+    REQ(high == 0 || high == 1, "priority must be 0 or 1");
+    int least = 0, greatest = 0;
+    SED_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    cudaStream_t s = nullptr;
+    SED_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, high ? greatest : least));
+    if (op->p->stream) {  // the new stream starts after the operator's earlier work
+      const cudaError_t e = cudaStreamSynchronize(op->p->stream);
+      if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        SED_CUDA(e);
+      }
+      if (op->p->own_stream) cudaStreamDestroy(op->p->stream);
+    }
+    op->p->stream = s;
+    op->p->own_stream = true;
+  });
+}
 int sed_op_apply_orbit(sed_op* op, const void* xs_dev, double* y_dev) {
   return guarded([&] {
     REQ(op && xs_dev && y_dev, "NULL argument");

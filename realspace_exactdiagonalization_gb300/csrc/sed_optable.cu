@@ -62,27 +62,75 @@ __global__ void k_optab_count(int64_t n_orb, const uint64_t* __restrict__ reps, 
   }
 }
 
+// The rank table, the term records, the site offsets and the class masks
+// are staged in shared memory (dynamic: rank | rec | mask | off), like the
+// gather matvec's: every hop looks up one rank-table entry per byte of the
+// target state, at addresses that differ across the warp.
+struct FillSmem {
+  size_t rank, rec, mask, off, total;
+};
+static FillSmem fill_layout(int rank_total, int n_terms, int n_mask, int n_site) {
+  FillSmem L{};
+  auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
+  L.rank = 0;
+  L.rec = al((size_t)rank_total * 4);
+  L.mask = al(L.rec + (size_t)n_terms * 4);
+  L.off = al(L.mask + (size_t)n_mask * 8);
+  L.total = al(L.off + (size_t)(n_site + 1) * 2);
+  return L;
+}
+
 template <bool FERMI>
 __global__ void k_optab_fill(int64_t n_orb, const uint64_t* __restrict__ reps, const uint8_t* __restrict__ rowflag,
                              const uint64_t* __restrict__ state, const uint32_t* __restrict__ rank_tab, RankParams rp,
-                             const uint16_t* __restrict__ off, const uint32_t* __restrict__ rec,
-                             const uint64_t* __restrict__ mask, int K, int kp1, int P, int64_t n_phi,
-                             uint64_t zero_cid, const int64_t* __restrict__ sl_off,
+                             const uint16_t* __restrict__ off_g, int n_site, const uint32_t* __restrict__ rec_g,
+                             int n_terms, const uint64_t* __restrict__ mask_g, int n_mask, FillSmem L, int K, int kp1,
+                             int P, int64_t n_phi, uint64_t zero_cid, const int64_t* __restrict__ sl_off,
                              const int32_t* __restrict__ sl_w, uint64_t* __restrict__ out) {
-  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_orb; o += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t base = sl_off[o >> 5] + (o & 31);
-    const int wdt = sl_w[o >> 5];
-    int k = 0;
-    if (rowflag[o]) {
-      const uint64_t m = reps[o];
-      HopIter it;
-      it.init(m, off);
-      uint32_t r;
-      int from;
-      while (k < wdt && it.next(off, rec, r, from)) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* s_rank = reinterpret_cast<uint32_t*>(smem + L.rank);
+  uint32_t* rec = reinterpret_cast<uint32_t*>(smem + L.rec);
+  uint64_t* mask = reinterpret_cast<uint64_t*>(smem + L.mask);
+  uint16_t* off = reinterpret_cast<uint16_t*>(smem + L.off);
+  for (int i = threadIdx.x; i < rp.total; i += blockDim.x) s_rank[i] = rank_tab[i];
+  for (int i = threadIdx.x; i < n_terms; i += blockDim.x) rec[i] = rec_g[i];
+  for (int i = threadIdx.x; i < n_mask; i += blockDim.x) mask[i] = mask_g[i];
+  for (int i = threadIdx.x; i <= n_site; i += blockDim.x) off[i] = off_g[i];
+  __syncthreads();
+  // one warp per slice, its 32 lanes the slice's rows, in lockstep over the
+  // slice's record positions: each position is stored by the whole warp at
+  // once (256 contiguous bytes), and the next hop's state word is loaded one
+  // hop ahead.  Lanes past the last row write padding records.
+  const int lane = threadIdx.x & 31;
+  const int64_t n_sl = (n_orb + 31) / 32;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t sl = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); sl < n_sl; sl += warps) {
+    const int64_t o = sl * 32 + lane;
+    uint64_t* dst = out + sl_off[sl] + lane;
+    const int wdt = sl_w[sl];
+    const uint64_t m = o < n_orb ? reps[o] : 0;
+    HopIter it;
+    it.init(m, off);
+    uint32_t r_n = 0;
+    int from_n = 0;
+    uint64_t nw_n = 0, wd_n = 0;
+    bool have = o < n_orb && rowflag[o] && it.next(off, rec, r_n, from_n);
+    if (have) {
+      nw_n = m ^ ((1ULL << from_n) | (1ULL << (r_n & 0xFF)));
+      wd_n = __ldg(state + dev::rank_of(nw_n, s_rank, rp));
+    }
+    for (int k = 0; k < wdt; ++k) {
+      uint64_t word = zero_cid << kCBits;
+      if (have) {
+        const uint32_t r = r_n;
+        const int from = from_n;
+        const uint64_t nw = nw_n, wd = wd_n;
+        have = it.next(off, rec, r_n, from_n);
+        if (have) {
+          nw_n = m ^ ((1ULL << from_n) | (1ULL << (r_n & 0xFF)));
+          wd_n = __ldg(state + dev::rank_of(nw_n, s_rank, rp));
+        }
         const int j = r & 0xFF;
-        const uint64_t nw = m ^ ((1ULL << from) | (1ULL << j));
-        const uint64_t wd = state[dev::rank_of(nw, rank_tab, rp)];
         int neg = (int)((wd >> 40) & 1);
         if (FERMI) neg ^= __popcll(m & dev::bits_between(from, j)) & 1;
         const int h = (int)((wd >> 48) & 0xFF);
@@ -93,11 +141,11 @@ __global__ void k_optab_fill(int64_t n_orb, const uint64_t* __restrict__ reps, c
         }
         const uint64_t phi = ((uint64_t)(h * P + pidx) << 1) | (uint64_t)neg;
         const uint64_t cid = (uint64_t)(r >> 8) * (uint64_t)n_phi + phi;
-        out[base + 32 * (int64_t)k] = ((uint64_t)(uint32_t)wd & kCMask) | (cid << kCBits);
-        ++k;
+        word = ((uint64_t)(uint32_t)wd & kCMask) | (cid << kCBits);
       }
+      __syncwarp();
+      dst[32 * (int64_t)k] = word;
     }
-    for (; k < wdt; ++k) out[base + 32 * (int64_t)k] = zero_cid << kCBits;
   }
 }
 
@@ -240,16 +288,19 @@ bool op_build_table(OpImpl& op) {
   upload(op.tab_off, off, s);
   upload(op.tab_w, w, s);
   op.tab_hop.alloc((size_t)std::max<int64_t>(tot, 1) * 8);
-  if (G.stats == 1)
-    k_optab_fill<true><<<grid1(n, 256), 256, 0, s>>>(
-        n, C.reps.as<uint64_t>(), S.rowflag.as<uint8_t>(), C.state.as<uint64_t>(), C.rank.dev.as<uint32_t>(),
-        C.rank.rp, op.site_off.as<uint16_t>(), op.rec.as<uint32_t>(), op.cls_mask.as<uint64_t>(), K, kp1, (int)P,
-        n_phi, (uint64_t)(n_coef - 1), op.tab_off.as<int64_t>(), op.tab_w.as<int32_t>(), op.tab_hop.as<uint64_t>());
-  else
-    k_optab_fill<false><<<grid1(n, 256), 256, 0, s>>>(
-        n, C.reps.as<uint64_t>(), S.rowflag.as<uint8_t>(), C.state.as<uint64_t>(), C.rank.dev.as<uint32_t>(),
-        C.rank.rp, op.site_off.as<uint16_t>(), op.rec.as<uint32_t>(), op.cls_mask.as<uint64_t>(), K, kp1, (int)P,
-        n_phi, (uint64_t)(n_coef - 1), op.tab_off.as<int64_t>(), op.tab_w.as<int32_t>(), op.tab_hop.as<uint64_t>());
+  const int n_terms = tt.n_terms, n_mask = nG * kMaxCls;
+  const FillSmem L = fill_layout(C.rank.rp.total, n_terms, n_mask, G.n_site);
+  auto fill = G.stats == 1 ? k_optab_fill<true> : k_optab_fill<false>;
+  SED_CUDA(cudaFuncSetAttribute(fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
+  int per_sm = 1;
+  SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill, 512, L.total));
+  const int fgrid = (int)std::max<int64_t>(
+      1, std::min<int64_t>((n_sl + 15) / 16, (int64_t)device_sm_count() * std::max(per_sm, 1)));
+  fill<<<fgrid, 512, L.total, s>>>(n, C.reps.as<uint64_t>(), S.rowflag.as<uint8_t>(), C.state.as<uint64_t>(),
+                                   C.rank.dev.as<uint32_t>(), C.rank.rp, op.site_off.as<uint16_t>(), G.n_site,
+                                   op.rec.as<uint32_t>(), n_terms, op.cls_mask.as<uint64_t>(), n_mask, L, K, kp1,
+                                   (int)P, n_phi, (uint64_t)(n_coef - 1), op.tab_off.as<int64_t>(),
+                                   op.tab_w.as<int32_t>(), op.tab_hop.as<uint64_t>());
   SED_CUDA(cudaGetLastError());
   SED_CUDA(cudaStreamSynchronize(s));
   op.tab_records = tot;

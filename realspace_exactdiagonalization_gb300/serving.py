@@ -12,6 +12,9 @@ Here a scheduler keeps the GPU busy with many requests at once:
 * small sectors go to the persistent batched kernel (``sed_batch_run``); two
   lanes alternate, so requests that arrive while one batch runs start in the
   next launch as soon as a lane frees, overlapping the batch in flight;
+* mid-size sectors go to the same batched kernel with its matvec input in
+  global memory, on a lane of their own, so they neither wait behind the
+  device-wide solves' kernels nor delay the small sectors' lanes;
 * large sectors go to device-wide solves (``sed_solve``), several at once on
   their own streams, each admitted only while the reserved device memory of
   the solves in flight plus its own footprint stays within the budget;
@@ -36,17 +39,22 @@ from . import lattice as L
 from .batched import BatchedSectorSolver
 from .groups import statistics_from_name
 
-# sectors whose catalog has at most this many orbits are solved by the batched
-# kernel, one thread block each (its complex64 matvec input fits in shared
-# memory); larger sectors take concurrent device-wide solves.  The batched
-# kernel also runs larger sectors with that input in global memory, but in
-# the served mix routing 1e5-3e5-orbit families there measured slower: the
-# shared batch lanes then delay the small families, while the large route
-# stays bound by its biggest sectors.  small_max_orbits raises the limit.
+# sectors whose catalog has at most SMALL_MAX_ORBITS orbits are solved by the
+# batched kernel, one thread block each (its complex64 matvec input fits in
+# shared memory), on the shared batch lanes; larger sectors take concurrent
+# device-wide solves.  Sectors up to medium_max_orbits can instead take the
+# batched kernel with that input in global memory, on lanes of their own.
+# That route is off by default (MEDIUM_MAX_ORBITS = 0): in the served mix its
+# thread blocks, each holding an SM for about a second per batch, slowed the
+# other routes more than they relieved the device-wide one.
 SMALL_MAX_ORBITS = 16384
-# catalogs above this size keep their batch workspace (the per-block Lanczos
-# basis) to MEDIUM_MAX_BATCH concurrent requests per lane
-MEDIUM_ORBITS = 16384
+MEDIUM_MAX_ORBITS = 0
+# device-wide solves of catalogs below this size run on high-priority streams:
+# their short host-synchronised steps then go ahead of the larger solves'
+# queued kernels instead of waiting behind them
+PRIORITY_MAX_ORBITS = 2_000_000
+# mid-size catalogs keep their batch workspace (the per-block Lanczos basis)
+# to MEDIUM_MAX_BATCH concurrent requests per lane
 MEDIUM_MAX_BATCH = 48
 
 
@@ -56,7 +64,7 @@ class Family:
     spec: L.ModelSpec
     catalog: A.Symmetry_Orbit_Catalog
     pairs: List[tuple]
-    route: str  # "batch" | "large"
+    route: str  # "batch" | "medium" | "large"
     solvers: List[BatchedSectorSolver] = field(default_factory=list)
 
     @property
@@ -133,8 +141,11 @@ def solver_footprint(n_orbits: int, nev: int, krylovdim: int = 30) -> int:
 class SectorServer:
     def __init__(self, families: Dict[str, L.ModelSpec], budget_bytes: float = 160e9, batch_lanes: int = 2,
                  large_workers: int = 3, max_batch: int = 512, small_max_orbits: int = SMALL_MAX_ORBITS,
-                 precision: str = "mixed", tol: float = 1e-10, nev: int = 1):
+                 precision: str = "mixed", tol: float = 1e-10, nev: int = 1,
+                 medium_max_orbits: int = MEDIUM_MAX_ORBITS, medium_lanes: int = 1,
+                 priority_max_orbits: int = PRIORITY_MAX_ORBITS):
         self.budget = float(budget_bytes)
+        self.priority_max_orbits = priority_max_orbits
         self.precision = precision
         self.tol = tol
         self.max_batch = max_batch
@@ -145,12 +156,17 @@ class SectorServer:
             cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G,
                                                  particle_statistics=statistics_from_name(spec.statistics))
             pairs = [(i, j) for (i, j, _) in spec.bilinear_terms()]
-            route = "batch" if cat.n_orbits <= small_max_orbits else "large"
+            if cat.n_orbits <= small_max_orbits:
+                route = "batch"
+            elif cat.n_orbits <= medium_max_orbits and medium_lanes > 0:
+                route = "medium"
+            else:
+                route = "large"
             fam = Family(name, spec, cat, pairs, route)
             self.resident += cat.n_states * 8 + cat.n_orbits * 9
-            if route == "batch":
-                cap = max_batch if cat.n_orbits <= MEDIUM_ORBITS else min(max_batch, MEDIUM_MAX_BATCH)
-                for _ in range(batch_lanes):
+            if route != "large":
+                cap = max_batch if route == "batch" else min(max_batch, MEDIUM_MAX_BATCH)
+                for _ in range(batch_lanes if route == "batch" else medium_lanes):
                     s = BatchedSectorSolver(cat, pairs, spec.density_terms, precision=precision, nev=nev,
                                             max_requests=cap)
                     fam.solvers.append(s)
@@ -159,10 +175,10 @@ class SectorServer:
         if self.resident > self.budget:
             raise MemoryError(f"resident catalogs and batch workspaces ({self.resident / 1e9:.1f} GB) exceed the budget")
         self.n_lanes = batch_lanes
+        self.n_medium = medium_lanes if any(f.route == "medium" for f in self.families.values()) else 0
         self.n_large = large_workers
         self._lock = threading.Condition()
-        self._pending_batch: List[Request] = []
-        self._pending_large: List[Request] = []
+        self._pending: Dict[str, List[Request]] = {"batch": [], "medium": [], "large": []}
         self._reserved = 0.0
         self._done: List[Request] = []
         self._closed = False
@@ -185,18 +201,19 @@ class SectorServer:
             srs.append(SectorRequest(irr, G, amps, r.seed))
         return srs
 
-    def _batch_lane(self, lane: int):
+    def _batch_lane(self, route: str, lane: int):
+        pending = self._pending[route]
         while True:
             with self._lock:
-                while not self._pending_batch and not self._closed:
+                while not pending and not self._closed:
                     self._lock.wait()
-                if not self._pending_batch and self._closed:
+                if not pending and self._closed:
                     return
-                fam_name = self._pending_batch[0].family  # oldest request decides the family
+                fam_name = pending[0].family  # oldest request decides the family
                 cap = self.families[fam_name].solvers[lane % len(self.families[fam_name].solvers)].max_requests
-                take = [r for r in self._pending_batch if r.family == fam_name][:cap]
+                take = [r for r in pending if r.family == fam_name][:cap]
                 for r in take:
-                    self._pending_batch.remove(r)
+                    pending.remove(r)
             fam = self.families[fam_name]
             t_start = self._now()
             solver = fam.solvers[lane % len(fam.solvers)]
@@ -208,19 +225,20 @@ class SectorServer:
                     r.status = int(out["status"][i])
                     r.dim = int(out["dims"][i])
                     r.delta_polish = float(out["delta_polish"][i])
-                    r.t_start, r.t_end, r.route = t_start, t_end, "batch"
+                    r.t_start, r.t_end, r.route = t_start, t_end, route
                     self._done.append(r)
                 self._lock.notify_all()
 
     def _large_worker(self):
+        pending = self._pending["large"]
         while True:
             with self._lock:
                 while True:
-                    if self._pending_large:
-                        r = self._pending_large[0]
+                    if pending:
+                        r = pending[0]
                         need = solver_footprint(self.families[r.family].n_orbits, r.nev)
                         if self._reserved + need <= self.budget - self.resident or self._reserved == 0:
-                            self._pending_large.pop(0)
+                            pending.pop(0)
                             self._reserved += need
                             self.peak_reserved = max(self.peak_reserved, self._reserved)
                             break
@@ -238,6 +256,8 @@ class SectorServer:
                 else:
                     H = A.MatrixFreeHamiltonian(basis, fam.spec.bilinear_terms(r.twist), fam.spec.density_terms,
                                                 precision=self.precision)
+                    if fam.n_orbits <= self.priority_max_orbits:
+                        H.set_priority(True)
                     vals, _, info = H.solve(r.nev, tol=self.tol, seed=r.seed, want_vectors=False)
                     status, delta = 0, info.max_delta_polish
                     del H
@@ -254,7 +274,10 @@ class SectorServer:
     def start(self):
         self._t0 = time.perf_counter()
         self._closed = False
-        self._threads = [threading.Thread(target=self._batch_lane, args=(i,), daemon=True) for i in range(self.n_lanes)]
+        self._threads = [threading.Thread(target=self._batch_lane, args=("batch", i), daemon=True)
+                         for i in range(self.n_lanes)]
+        self._threads += [threading.Thread(target=self._batch_lane, args=("medium", i), daemon=True)
+                          for i in range(self.n_medium)]
         self._threads += [threading.Thread(target=self._large_worker, daemon=True) for _ in range(self.n_large)]
         for t in self._threads:
             t.start()
@@ -263,7 +286,7 @@ class SectorServer:
         fam = self.families[r.family]
         with self._lock:
             r.arrival = self._now()
-            (self._pending_batch if fam.route == "batch" else self._pending_large).append(r)
+            self._pending[fam.route].append(r)
             self._lock.notify_all()
 
     def close(self) -> List[Request]:

@@ -1,7 +1,7 @@
 """The served path: a mixed request stream through the continuous-batching
-scheduler (batched kernel lanes + concurrent device-wide solves) against the
-oracle's dense spectra, and each request alone against its result in the mix
-(within the mixed path's |dE|/|E| <= 1e-9)."""
+scheduler (batched kernel lanes, a mid-size lane, concurrent device-wide
+solves) against the oracle's dense spectra, and each request alone against
+its result in the mix (within the mixed path's |dE|/|E| <= 1e-9)."""
 import numpy as np
 import pytest
 
@@ -17,14 +17,19 @@ def _families():
             "ring16": L.ring_xxz(16, 1.0, 2.0)}
 
 
-def test_served_mix_matches_oracle_and_alone(oracle):
+@pytest.mark.parametrize("ring_route", ["large", "medium"])
+def test_served_mix_matches_oracle_and_alone(oracle, ring_route):
     from realspace_exactdiagonalization_gb300.serving import SectorServer, random_requests
 
     fams = _families()
     reqs = random_requests(fams, 36, rate=0.0, seed=7, nev=1)
-    # ring16 (810 orbits) takes the device-wide route, the others the batched kernel
-    srv = SectorServer(fams, budget_bytes=8e9, batch_lanes=2, large_workers=2, small_max_orbits=300)
-    assert srv.families["ring16"].route == "large" and srv.families["haldane2x4"].route == "batch"
+    # ring16 (810 orbits) takes the device-wide route, or the batched kernel's
+    # mid-size lane with its matvec input in global memory; the others take
+    # the batched kernel's shared lanes
+    medium = 1000 if ring_route == "medium" else 0
+    srv = SectorServer(fams, budget_bytes=8e9, batch_lanes=2, large_workers=2, small_max_orbits=300,
+                       medium_max_orbits=medium)
+    assert srv.families["ring16"].route == ring_route and srv.families["haldane2x4"].route == "batch"
     done = sorted(srv.serve(reqs), key=lambda r: r.rid)
     assert len(done) == len(reqs) and all(r.status == 0 for r in done)
     for r in done:
@@ -38,10 +43,34 @@ def test_served_mix_matches_oracle_and_alone(oracle):
     # alone: a fresh server answers each of a few requests on its own
     for r in done[:: 7]:
         srv1 = SectorServer({r.family: fams[r.family]}, budget_bytes=8e9, batch_lanes=1, large_workers=1,
-                            small_max_orbits=300)
+                            small_max_orbits=300, medium_max_orbits=medium)
         q = random_requests(fams, 36, rate=0.0, seed=7, nev=1)[r.rid]
         alone = srv1.serve([q])[0]
         assert alone.dim == r.dim
         # the mixed path's stated tolerance, |dE|/|E| <= 1e-9
         assert np.all(np.abs(alone.evals - r.evals) <= 1e-9 * np.maximum(1.0, np.abs(r.evals))), \
             (r.rid, r.family, alone.evals, r.evals)
+
+
+def test_op_priority_keeps_results():
+    """sed_op_set_priority moves the operator to a stream of the device's
+    greatest (or least) priority; the solve gives the same bits, and a
+    priority other than 0 or 1 is refused."""
+    import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300 import _lib
+
+    spec = L.ring_xxz(16, 1.0, 2.0)
+    G = L.build_translation_group(spec.lattice, (0.2, 0.0))
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G,
+                                         particle_statistics=A.Bosonic())
+    basis = A.build_symmetry_sector_basis(cat, L.build_translation_irrep_list(G, spec.lattice)[3], group=G)
+    H = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms((0.2, 0.0)), spec.density_terms, precision="mixed")
+    a, _, _ = H.solve(2, want_vectors=False)
+    H.set_priority(True)
+    b, _, _ = H.solve(2, want_vectors=False)
+    H.set_priority(False)
+    c, _, _ = H.solve(2, want_vectors=False)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, c)
+    with pytest.raises(_lib.SEDError):
+        _lib.check(_lib.load().sed_op_set_priority(H.handle, 2))
