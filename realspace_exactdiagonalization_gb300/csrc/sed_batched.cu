@@ -1069,21 +1069,9 @@ __device__ __forceinline__ void block_normalize(const BatchArgs& a, const double
 // FP64-class Rayleigh-Ritz check bounds the eigenvalues.  The check itself
 // runs on double-float copies of the Ritz block.
 
-// the prefetch distance in chunks for complex64 sweeps: the byte volume in
-// flight of the double-float sweeps, at half the bytes per chunk
-__device__ __forceinline__ int cf_prefetch_dist(int nv) { return 2 * prefetch_dist(nv); }
-
-// as prefetch_chunks, for vectors of 8-byte elements (the byte count rounded
-// up to 16 inside the vector's padding: ld is a multiple of 32)
-__device__ __forceinline__ void prefetch_chunks(const BatchArgs& a, const float2* V, int nv, int64_t c0, int nch,
-                                                int span, int t) {
-  if (nch > 0 && t < nv * nch) {
-    const int64_t p0 = (c0 + t / nv) * span;
-    if (p0 < a.n_orb)
-      l2_prefetch_bulk(V + (size_t)(t % nv) * a.ld + p0,
-                       ((uint32_t)min((int64_t)span, a.n_orb - p0) * 8u + 15u) & ~15u);
-  }
-}
+// The complex64 sweeps rely on the threads' own loads: with half the bytes
+// per element, the bulk L2 prefetch of the double-float sweeps measured
+// slower here (1929 against 1971 sector solves/s on the flux-scan batch).
 
 // coef[0..nv) = V[0..nv)^H w for complex64 vectors, in chunks of 8
 __device__ void cf_dots(const BatchArgs& a, const float2* V, int nv, const float2* w, double* red, double2* coef) {
@@ -1092,13 +1080,8 @@ __device__ void cf_dots(const BatchArgs& a, const float2* V, int nv, const float
 #pragma unroll
     for (int c = 0; c < 16; ++c) h[c] = l[c] = 0.f;
     const int cn = min(8, nv - l0);
-    const int span = blockDim.x, pd = cf_prefetch_dist(cn);
     const float2* Vl = V + (size_t)l0 * a.ld;
-    prefetch_chunks(a, Vl, cn, 0, pd, span, threadIdx.x);
-    for (int64_t o0 = 0, ch = 0; o0 < a.n_orb; o0 += span, ++ch) {
-      if (pd) prefetch_chunks(a, Vl, cn, ch + pd, 1, span, threadIdx.x);
-      const int64_t o = o0 + threadIdx.x;
-      if (o >= a.n_orb) continue;
+    for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
       const float2 x = w[o];
 #pragma unroll
       for (int c = 0; c < 8; ++c)
@@ -1134,12 +1117,7 @@ __device__ __noinline__ double cf_dots_local(const BatchArgs& a, const float2* V
   float h[16], l[16];
 #pragma unroll
   for (int c = 0; c < 16; ++c) h[c] = l[c] = 0.f;
-  const int span = blockDim.x, pd = cf_prefetch_dist(cn);
-  prefetch_chunks(a, V, cn, 0, pd, span, threadIdx.x);
-  for (int64_t o0 = 0, ch = 0; o0 < a.n_orb; o0 += span, ++ch) {
-    if (pd) prefetch_chunks(a, V, cn, ch + pd, 1, span, threadIdx.x);
-    const int64_t o = o0 + threadIdx.x;
-    if (o >= a.n_orb) continue;
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
     const float2 x0 = w[o];
     float xr = x0.x, xi = x0.y;
     for (int q = 0; q < nl; ++q) cf_sub(xr, xi, cl[q], Vl[(size_t)q * a.ld + o]);
@@ -1164,12 +1142,7 @@ __device__ __noinline__ double cf_dots_local(const BatchArgs& a, const float2* V
 // groups of eight vectors before the arithmetic; out of line like df_axpy.
 __device__ __noinline__ double cf_axpy(const BatchArgs& a, const float2* V, int nv, const float4* cdf, float2* w) {
   float nh = 0.f, nl = 0.f;
-  const int span = blockDim.x, pd = cf_prefetch_dist(nv);
-  prefetch_chunks(a, V, nv, 0, pd, span, threadIdx.x);
-  for (int64_t o0 = 0, ch = 0; o0 < a.n_orb; o0 += span, ++ch) {
-    if (pd) prefetch_chunks(a, V, nv, ch + pd, 1, span, threadIdx.x);
-    const int64_t o = o0 + threadIdx.x;
-    if (o >= a.n_orb) continue;
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
     const float2 x0 = w[o];
     float xr = x0.x, xi = x0.y;
     for (int q0 = 0; q0 < nv; q0 += 8) {
