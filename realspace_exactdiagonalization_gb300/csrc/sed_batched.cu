@@ -1072,6 +1072,10 @@ __device__ __forceinline__ void block_normalize(const BatchArgs& a, const double
 // The complex64 sweeps rely on the threads' own loads: with half the bytes
 // per element, the bulk L2 prefetch of the double-float sweeps measured
 // slower here (1929 against 1971 sector solves/s on the flux-scan batch).
+// Their loops step over the block's rows in block-wide chunks, a trip count
+// uniform over the block, with the threads past the end skipping their row:
+// the per-thread strided form of the same loops measured 10 % slower (1790
+// sector solves/s).
 
 // coef[0..nv) = V[0..nv)^H w for complex64 vectors, in chunks of 8
 __device__ void cf_dots(const BatchArgs& a, const float2* V, int nv, const float2* w, double* red, double2* coef) {
@@ -1081,7 +1085,9 @@ __device__ void cf_dots(const BatchArgs& a, const float2* V, int nv, const float
     for (int c = 0; c < 16; ++c) h[c] = l[c] = 0.f;
     const int cn = min(8, nv - l0);
     const float2* Vl = V + (size_t)l0 * a.ld;
-    for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    for (int64_t o0 = 0; o0 < a.n_orb; o0 += blockDim.x) {
+      const int64_t o = o0 + threadIdx.x;
+      if (o >= a.n_orb) continue;
       const float2 x = w[o];
 #pragma unroll
       for (int c = 0; c < 8; ++c)
@@ -1117,7 +1123,9 @@ __device__ __noinline__ double cf_dots_local(const BatchArgs& a, const float2* V
   float h[16], l[16];
 #pragma unroll
   for (int c = 0; c < 16; ++c) h[c] = l[c] = 0.f;
-  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+  for (int64_t o0 = 0; o0 < a.n_orb; o0 += blockDim.x) {
+    const int64_t o = o0 + threadIdx.x;
+    if (o >= a.n_orb) continue;
     const float2 x0 = w[o];
     float xr = x0.x, xi = x0.y;
     for (int q = 0; q < nl; ++q) cf_sub(xr, xi, cl[q], Vl[(size_t)q * a.ld + o]);
@@ -1142,7 +1150,9 @@ __device__ __noinline__ double cf_dots_local(const BatchArgs& a, const float2* V
 // groups of eight vectors before the arithmetic; out of line like df_axpy.
 __device__ __noinline__ double cf_axpy(const BatchArgs& a, const float2* V, int nv, const float4* cdf, float2* w) {
   float nh = 0.f, nl = 0.f;
-  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+  for (int64_t o0 = 0; o0 < a.n_orb; o0 += blockDim.x) {
+    const int64_t o = o0 + threadIdx.x;
+    if (o >= a.n_orb) continue;
     const float2 x0 = w[o];
     float xr = x0.x, xi = x0.y;
     for (int q0 = 0; q0 < nv; q0 += 8) {
