@@ -374,9 +374,9 @@ def run_ours(args, rank, world):
                      "bytes_per_launch": bytes_launch, "matvec_bytes_per_launch": bytes_mv,
                      "lanczos_bytes_per_launch": bytes_lz, "frac_matvec_bytes_only": bytes_mv / t_launch / 1e9 / peak,
                      "note": "algorithmic bytes of one launch: every matvec D*(8+4+2s)+hops*(4+1+4+s) (s=8), plus "
-                             "every Lanczos iteration's (3+k)*D*16 (three double-float vector streams and the "
+                             "every Lanczos iteration's (3+k)*D*8 (three complex64 vector streams and the "
                              "reorthogonalisation's read of the k basis vectors) and every restart's "
-                             "(m+keep)*D*16 rotation, k following the thick-restart schedule m=24, keep=15"},
+                             "(m+keep)*D*8 rotation, k following the thick-restart schedule m=24, keep=15"},
         "cpu_baseline": cpu,
         # one k_batch launch per step, plus the FP64 re-solve launch when a
         # request's polish missed its target (inputs are identical every step)
