@@ -524,6 +524,7 @@ def run_served(args):
     done = sorted(srv.serve(reqs), key=lambda r: r.rid)
     st = latency_stats(done)
     bad = [r.rid for r in done if r.status != 0]
+    errors = {r.rid: f"{r.family}: {r.error or r.status}" for r in done if r.status != 0}
     # the plain FP64 drop-in, one request at a time, on a per-family sample
     per_fam = {}
     plain_ev = {}
@@ -561,7 +562,7 @@ def run_served(args):
     mix_s = np.mean([per_fam[r.family]["plain_fp64_s"] for r in done])
     rel = [abs(done[i].evals[0] - e) / abs(e) for i, e in plain_ev.items()]
     line = {"workload": "served_config5", "requests": len(done), "rate_per_s": args.served_rate,
-            "served": st, "unconverged": bad, "setup_s": t_setup, "peak_reserved_gb": srv.peak_reserved / 1e9,
+            "served": st, "unconverged": bad, "errors": errors, "setup_s": t_setup, "peak_reserved_gb": srv.peak_reserved / 1e9,
             "resident_gb": srv.resident / 1e9,
             "plain_fp64_one_at_a_time_solves_per_s": 1.0 / mix_s,
             "speedup_vs_plain_fp64": st["solves_per_s"] * mix_s,

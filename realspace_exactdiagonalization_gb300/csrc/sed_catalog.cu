@@ -381,15 +381,27 @@ std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> gp, int n_
   c->reps.alloc((size_t)c->n_orbits * 8);
   c->stab.alloc((size_t)c->n_orbits);
   const size_t smem = (size_t)c->rank.rp.total * 4;
-  // the opt-in covers the dynamic part; the kernel also holds 4 KB of static shared memory
-  SED_CUDA(cudaFuncSetAttribute(k_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_expand<<<grid_for(nw, 256), 256, smem, s>>>(n_states, G.n_site, n_filled, G.n_ops, G.stats,
-                                                c->perm_u8.as<uint8_t>(), c->binom.as<uint64_t>(),
-                                                flags.as<uint32_t>(), offs.as<uint32_t>(),
-                                                c->rank.dev.as<uint32_t>(), c->rank.rp, c->inv_u8.as<uint8_t>(),
-                                                c->state.as<uint64_t>(), c->reps.as<uint64_t>(),
-                                                c->stab.as<uint8_t>());
-  SED_CUDA(cudaGetLastError());
+  {
+    // the opt-in covers the dynamic part (the kernel also holds 4 KB of static
+    // shared memory); it is a property of the kernel, shared by every catalog
+    // and host thread, so it is only raised, and raised-and-launched under
+    // one lock: a concurrent build with a smaller rank table cannot undercut
+    // this launch
+    static std::mutex mu;
+    static size_t configured = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (smem > configured) {
+      SED_CUDA(cudaFuncSetAttribute(k_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      configured = smem;
+    }
+    k_expand<<<grid_for(nw, 256), 256, smem, s>>>(n_states, G.n_site, n_filled, G.n_ops, G.stats,
+                                                  c->perm_u8.as<uint8_t>(), c->binom.as<uint64_t>(),
+                                                  flags.as<uint32_t>(), offs.as<uint32_t>(),
+                                                  c->rank.dev.as<uint32_t>(), c->rank.rp, c->inv_u8.as<uint8_t>(),
+                                                  c->state.as<uint64_t>(), c->reps.as<uint64_t>(),
+                                                  c->stab.as<uint8_t>());
+    SED_CUDA(cudaGetLastError());
+  }
   c->stab_host.resize(c->n_orbits);
   if (c->n_orbits)
     SED_CUDA(cudaMemcpyAsync(c->stab_host.data(), c->stab.p, c->n_orbits, cudaMemcpyDeviceToHost, s));

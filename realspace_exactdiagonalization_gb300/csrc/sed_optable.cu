@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <mutex>
 #include <vector>
 
 #include "sed_internal.cuh"
@@ -291,17 +292,30 @@ bool op_build_table(OpImpl& op) {
   const int n_terms = tt.n_terms, n_mask = nG * kMaxCls;
   const FillSmem L = fill_layout(C.rank.rp.total, n_terms, n_mask, G.n_site);
   auto fill = G.stats == 1 ? k_optab_fill<true> : k_optab_fill<false>;
-  SED_CUDA(cudaFuncSetAttribute(fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
-  int per_sm = 1;
-  SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill, 512, L.total));
-  const int fgrid = (int)std::max<int64_t>(
-      1, std::min<int64_t>((n_sl + 15) / 16, (int64_t)device_sm_count() * std::max(per_sm, 1)));
-  fill<<<fgrid, 512, L.total, s>>>(n, C.reps.as<uint64_t>(), S.rowflag.as<uint8_t>(), C.state.as<uint64_t>(),
-                                   C.rank.dev.as<uint32_t>(), C.rank.rp, op.site_off.as<uint16_t>(), G.n_site,
-                                   op.rec.as<uint32_t>(), n_terms, op.cls_mask.as<uint64_t>(), n_mask, L, K, kp1,
-                                   (int)P, n_phi, (uint64_t)(n_coef - 1), op.tab_off.as<int64_t>(),
-                                   op.tab_w.as<int32_t>(), op.tab_hop.as<uint64_t>());
-  SED_CUDA(cudaGetLastError());
+  {
+    // the shared-memory opt-in is a property of the kernel, shared by every
+    // operator and host thread: raise it (never lower it) and launch under
+    // one lock, so a concurrent build with a smaller rank table cannot
+    // undercut this launch
+    static std::mutex mu;
+    static size_t configured[2] = {0, 0};
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cfg = configured[G.stats == 1 ? 1 : 0];
+    if (L.total > cfg) {
+      SED_CUDA(cudaFuncSetAttribute(fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
+      cfg = L.total;
+    }
+    int per_sm = 1;
+    SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill, 512, L.total));
+    const int fgrid = (int)std::max<int64_t>(
+        1, std::min<int64_t>((n_sl + 15) / 16, (int64_t)device_sm_count() * std::max(per_sm, 1)));
+    fill<<<fgrid, 512, L.total, s>>>(n, C.reps.as<uint64_t>(), S.rowflag.as<uint8_t>(), C.state.as<uint64_t>(),
+                                     C.rank.dev.as<uint32_t>(), C.rank.rp, op.site_off.as<uint16_t>(), G.n_site,
+                                     op.rec.as<uint32_t>(), n_terms, op.cls_mask.as<uint64_t>(), n_mask, L, K, kp1,
+                                     (int)P, n_phi, (uint64_t)(n_coef - 1), op.tab_off.as<int64_t>(),
+                                     op.tab_w.as<int32_t>(), op.tab_hop.as<uint64_t>());
+    SED_CUDA(cudaGetLastError());
+  }
   SED_CUDA(cudaStreamSynchronize(s));
   op.tab_records = tot;
   op.tab_coefs = n_coef;

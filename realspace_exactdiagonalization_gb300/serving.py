@@ -89,6 +89,7 @@ class Request:
     t_end: float = 0.0
     delta_polish: float = 0.0
     route: str = ""
+    error: str = ""  # the library's message when status != 0
 
 
 def config5_families() -> Dict[str, L.ModelSpec]:
@@ -263,7 +264,7 @@ class SectorServer:
                     del H
                 r.evals, r.status, r.dim, r.delta_polish = np.asarray(vals), status, basis.dim, delta
             except A._lib.SEDError as e:  # reported per request, never silently dropped
-                r.status, r.evals = e.code, np.full(r.nev, np.nan)
+                r.status, r.evals, r.error = e.code, np.full(r.nev, np.nan), str(e)
             r.t_start, r.t_end, r.route = t_start, self._now(), "large"
             with self._lock:
                 self._reserved -= need

@@ -74,3 +74,42 @@ def test_op_priority_keeps_results():
     np.testing.assert_array_equal(a, c)
     with pytest.raises(_lib.SEDError):
         _lib.check(_lib.load().sed_op_set_priority(H.handle, 2))
+
+
+def test_concurrent_table_builds_from_two_threads():
+    """Catalog expansions and operator hop tables stage per-catalog rank
+    tables of different sizes in shared memory; their kernels' shared-memory
+    opt-in is shared by every host thread.  Two threads building catalogs,
+    sectors and hop tables of two fillings (different rank-table sizes) over
+    and over must all succeed and give the same ground energies each time."""
+    import threading
+
+    import realspace_exactdiagonalization_gb300.api as A
+
+    def work(n_filled, out, errs):
+        try:
+            spec = L.hubbard_square(2, 4, n_filled=n_filled)
+            G = L.build_translation_group(spec.lattice, (0.3, 0.1))
+            irr = L.build_translation_irrep_list(G, spec.lattice)[1]
+            for _ in range(12):
+                cat = A.build_symmetry_orbit_catalog(n_filled=n_filled, symmetry_group=G,
+                                                     particle_statistics=A.Fermionic())
+                basis = A.build_symmetry_sector_basis(cat, irr, group=G)
+                H = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms((0.3, 0.1)), spec.density_terms,
+                                            precision="mixed")
+                H.set_hop_table(2)
+                vals, _, _ = H.solve(1, want_vectors=False)
+                out.append(float(vals[0]))
+                del H
+        except Exception as e:  # reported to the main thread
+            errs.append(repr(e))
+
+    outs, errs = {5: [], 8: []}, []
+    ts = [threading.Thread(target=work, args=(nf, outs[nf], errs)) for nf in (5, 8)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errs, errs
+    for nf, vals in outs.items():
+        assert len(vals) == 12 and len(set(vals)) == 1, (nf, vals)
