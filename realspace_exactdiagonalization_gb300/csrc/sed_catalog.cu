@@ -76,12 +76,14 @@ void build_rank_table(int N, int k, RankTable& rt, cudaStream_t s) {
 }
 
 int device_sm_count() {
-  static int sms = 0;
-  if (!sms) {
-    int d = 0;
+  // initialised once, thread-safely, by the first caller of any thread (a
+  // failed query throws and leaves it for the next call)
+  static const int sms = [] {
+    int d = 0, n = 0;
     SED_CUDA(cudaGetDevice(&d));
-    SED_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d));
-  }
+    SED_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d));
+    return n;
+  }();
   return sms;
 }
 
