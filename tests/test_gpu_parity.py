@@ -144,6 +144,28 @@ def test_eigenvalues_match_dense(oracle, name):
                 assert np.linalg.norm(r) < bound * max(1.0, abs(vals[i])), (name, k, precision, i)
 
 
+def test_lanczos_odd_orbit_count(oracle):
+    """A catalog with an odd orbit count: a ring of 16 sites with 7 particles
+    at a twist, 715 orbits, every sector above the dense branch's 500 rows.
+    The mixed solve's vector kernels take element pairs plus the last element
+    alone; both precisions give the oracle's lowest eigenvalues."""
+    from cases import Case
+    from realspace_exactdiagonalization_gb300 import lattice as L
+
+    case = Case("ring16_7", L.ring_xxz(16, 1.0, 2.0, n_filled=7), theta=(0.21, 0.0))
+    for k in (0, 3):
+        _, _, op = oracle_objects(oracle, case, k)
+        ref = np.linalg.eigvalsh(op.dense())
+        for precision in ("fp64", "mixed"):
+            cat, basis, H = _device(case, k, precision)
+            assert cat.n_orbits == 715 and basis.dim > 500
+            vals, vecs, _ = H.solve(3, tol=1e-10)
+            assert_lanczos_spectrum(vals, ref, 1e-9 * max(1.0, abs(ref[0])), f"k={k} {precision}")
+            for i in range(len(vals)):
+                r = op.dense() @ vecs[:, i] - vals[i] * vecs[:, i]
+                assert np.linalg.norm(r) < (1e-7 if precision == "fp64" else 1e-4) * max(1.0, abs(vals[i]))
+
+
 def test_sector_union_equals_full_spectrum(oracle):
     """flux_regression.jl:46 on the device: the union of the device sector
     spectra equals the identity-group (full Fock) spectrum at a twisted flux."""
