@@ -1119,17 +1119,6 @@ __device__ void cf_dots(const BatchArgs& a, const float2* V, int nv, const float
   }
 }
 
-// x -= c v for one complex64 element, c as (re_hi, im_hi, re_lo, im_lo)
-__device__ __forceinline__ void cf_sub(float& xr, float& xi, float4 c, float2 v) {
-  xr = __fmaf_rn(-c.x, v.x, xr);
-  xr = __fmaf_rn(c.y, v.y, xr);
-  xi = __fmaf_rn(-c.x, v.y, xi);
-  xi = __fmaf_rn(-c.y, v.x, xi);
-  xr = __fmaf_rn(-c.z, v.x, xr);
-  xr = __fmaf_rn(c.w, v.y, xr);
-  xi = __fmaf_rn(-c.z, v.y, xi);
-  xi = __fmaf_rn(-c.w, v.x, xi);
-}
 
 // The local step's update folded into the first chunk of the full pass
 // (complex64 counterpart of df_dots_local): w -= Vl[0..nl) cl, then
@@ -1246,16 +1235,6 @@ __device__ __forceinline__ void cf_normalize(const BatchArgs& a, const float2* w
   }
 }
 
-// (h, l) += x (zh + zl) for a float x: TwoProd of the leading product, the
-// rest folded into the low word
-__device__ __forceinline__ void df_mac1(float& h, float& l, float x, float zh, float zl) {
-  const float p = __fmul_rn(x, zh);
-  const float pe = __fmaf_rn(x, zl, __fmaf_rn(x, zh, -p));
-  float sh, e;
-  df_two_sum(h, p, sh, e);
-  h = sh;
-  l = __fadd_rn(l, __fadd_rn(e, pe));
-}
 
 // out[c] = sum_l V[l] Z[l][c] for c < keep (complex64 counterpart of
 // df_rotate: same chunking and half-block split), accumulated in

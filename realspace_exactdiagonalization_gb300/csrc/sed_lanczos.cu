@@ -10,11 +10,13 @@
 // complex128; the projected matrix and its eigen-decomposition stay on the host.
 //
 // Mixed precision (SED_PREC_MIXED): the matvec reads complex64 inputs and
-// accumulates in FP32, everything else stays FP64-class (double-float
-// vectors), and the full reorthogonalisation is selective (kSelReorth).  Once the Ritz estimates of
-// the requested pairs fall below 1e-6 |E|, one Rayleigh-Ritz step with FP64
-// matvecs over the nev + 2 Ritz vectors polishes the eigenvalues, and the
-// result is accepted by the quadratic bound |dE| <= |r|^2 / gap (see solve).
+// accumulates in FP32; the Lanczos basis, restart buffer and work vector are
+// complex64, each value rounded once from an accurately computed one (see the
+// complex64 kernels below); the full reorthogonalisation is selective
+// (kSelReorth).  Once the Ritz estimates of the requested pairs fall below
+// 1e-6 |E|, one Rayleigh-Ritz step with FP64 matvecs over the nev + 2 Ritz
+// vectors polishes the eigenvalues, and the result is accepted by the
+// quadratic bound |dE| <= |r|^2 / gap (see solve).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -430,18 +432,6 @@ __global__ void __launch_bounds__(kBS) k_cf_multidot(int64_t n, const float2* __
     }
 }
 
-// x -= c v for one complex64 element, c as (re_hi, im_hi, re_lo, im_lo): the
-// hi parts first, then the lo parts
-__device__ __forceinline__ void cf_sub(float& xr, float& xi, float4 c, float2 v) {
-  xr = __fmaf_rn(-c.x, v.x, xr);
-  xr = __fmaf_rn(c.y, v.y, xr);
-  xi = __fmaf_rn(-c.x, v.y, xi);
-  xi = __fmaf_rn(-c.y, v.x, xi);
-  xr = __fmaf_rn(-c.z, v.x, xr);
-  xr = __fmaf_rn(c.w, v.y, xr);
-  xi = __fmaf_rn(-c.z, v.y, xi);
-  xi = __fmaf_rn(-c.w, v.x, xi);
-}
 
 // w -= sum_l c_l V_l, each FP64 coefficient applied as hi + lo floats;
 // optionally the block partial of |w|^2.  skip: the device flag of the
@@ -519,16 +509,6 @@ __global__ void k_cf_normalize(int64_t n, const float2* __restrict__ w, const do
   }
 }
 
-// (h, l) += x (zh + zl) for a float x: TwoProd of the leading product, the
-// rest folded into the low word
-__device__ __forceinline__ void df_mac1(float& h, float& l, float x, float zh, float zl) {
-  const float p = __fmul_rn(x, zh);
-  const float pe = __fmaf_rn(x, zl, __fmaf_rn(x, zh, -p));
-  float sh, e;
-  df_two_sum(h, p, sh, e);
-  h = sh;
-  l = __fadd_rn(l, __fadd_rn(e, pe));
-}
 
 // Restart rotation out[c] = sum_l V[l] Z[l][c], Z real (the Ritz vectors of
 // the real projected matrix) as double-float pairs, row-major [l][keep],
