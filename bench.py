@@ -74,7 +74,8 @@ def lanczos_bytes(nmv: int, dim: int, m: int = 24, keep: int = 8, n_polish: int 
     cyc = m - keep
     full, part = divmod(rest, cyc)
     ksum += full * sum(range(keep + 1, m + 1)) + sum(range(keep + 1, keep + 1 + part))
-    restarts = full + (1 if part else 0) + (1 if steps >= m else 0)
+    # every cycle ends in a rotation, a partial one (first or last) included
+    restarts = (1 if steps > 0 else 0) + full + (1 if part else 0)
     return float((3 * steps + ksum + restarts * (m + keep)) * dim * elem)
 
 
