@@ -166,6 +166,24 @@ def test_lanczos_odd_orbit_count(oracle):
                 assert np.linalg.norm(r) < (1e-7 if precision == "fp64" else 1e-4) * max(1.0, abs(vals[i]))
 
 
+def test_mixed_solve_without_hop_table(oracle):
+    """The mixed solve with the operator's hop table switched off: each
+    matvec is the on-the-fly gather with an FP64 output, converted to the
+    complex64 work vector.  Same lowest eigenvalues as the oracle."""
+    from cases import Case
+    from realspace_exactdiagonalization_gb300 import lattice as L
+
+    case = Case("ring16_7", L.ring_xxz(16, 1.0, 2.0, n_filled=7), theta=(0.21, 0.0))
+    for k in (1, 5):
+        _, _, op = oracle_objects(oracle, case, k)
+        ref = np.linalg.eigvalsh(op.dense())
+        _, basis, H = _device(case, k, "mixed")
+        H.set_hop_table(H.HOP_TABLE_OFF)
+        vals, _, _ = H.solve(3, tol=1e-10)
+        assert not H.hop_table_info()["built"]
+        assert_lanczos_spectrum(vals, ref, 1e-9 * max(1.0, abs(ref[0])), f"k={k}")
+
+
 def test_sector_union_equals_full_spectrum(oracle):
     """flux_regression.jl:46 on the device: the union of the device sector
     spectra equals the identity-group (full Fock) spectrum at a twisted flux."""
