@@ -92,9 +92,32 @@ void sed_group_destroy(sed_group* g);
  * over |G| permutations held in shared memory, orbit expansion into the
  * representative tables.  Limit: binomial(n_site, n_filled) < 2^32. */
 int sed_catalog_build(const sed_group* g, int n_filled, sed_catalog** out);
+/* The same catalog restricted to two separately conserved species (no
+ * counterpart in the reference, which fixes only the total particle number,
+ * SRE:1460-1466): n_lo particles on modes [0, n_split) and n_hi on
+ * [n_split, n_site), e.g. spin-up at bit i and spin-down at bit i + n_site/2 of
+ * a Hubbard model (benchmark/benchmark.jl:155-219) in one S^z sector.  Every
+ * group element must map each species onto itself, and operators built on it
+ * may not move particles between species (SED_ERR_ARG).  The basis states are
+ * ranked rank_hi(m >> n_split) * binomial(n_split, n_lo) + rank_lo(low bits),
+ * which is ascending-mask order, so the representatives, stabilizers and
+ * rep_sym/rep_amp tables equal the total-particle catalog's entries for the
+ * masks of this block, in the same order; REP_RANK numbers the orbits of the
+ * block.  Limit: binomial(n_split, n_lo) * binomial(n_site - n_split, n_hi)
+ * < 2^32. */
+int sed_catalog_build_species(const sed_group* g, int n_split, int n_lo, int n_hi, sed_catalog** out);
+/* n_split (0 for a one-species catalog) and the particle numbers of each
+ * species (n_lo = n_filled and n_hi = 0 for one species). */
+int sed_catalog_species(const sed_catalog* c, int* n_split, int* n_lo, int* n_hi);
 int sed_catalog_info(const sed_catalog* c, int64_t* n_states, int64_t* n_orbits, int64_t* n_stab_total);
 /* Read one table back to the host in the reference's layout (bit-exact). */
 int sed_catalog_get(const sed_catalog* c, int field, void* out, int64_t out_bytes);
+/* The three per-state tables of SED_FIELD_REP_RANK / REP_SYM / REP_AMP
+ * (SRE:305-327, in the same 1-based layout) at n given masks, each holding the
+ * catalog's particle number(s): the readback for catalogs whose tables are too
+ * large to copy whole (SRE:584-594 get_canonical reads the same entries). */
+int sed_catalog_lookup(const sed_catalog* c, int64_t n, const uint64_t* masks, int32_t* rep_rank, int32_t* rep_sym,
+                       double* rep_amp_reim);
 /* update_orbit_stabilizer_phases! (SRE:338-369): same permutations, new
  * per-site phases (a flux-twisted group); no re-enumeration. */
 int sed_catalog_update_phases(sed_catalog* c, const sed_group* new_group);
@@ -219,23 +242,40 @@ int sed_op_apply_orbit(sed_op* op, const void* xs_dev, double* y_dev);
  * which every GPU that loads it keeps until exit; sectors whose catalog has
  * more than 1048576 orbits are rejected with SED_ERR_LIMIT.  The first call on
  * a device looks up that array's device address; make it before any stream
- * capture.  All calls share the array, so calls that overlap on the GPU race:
- * serialise them.  Asynchronous on the operator's stream. */
+ * capture.  The call never runs the gather's launch-shape autotuner: it uses
+ * the operator's chosen or pinned shape, else the one remembered for the same
+ * catalog shape, else one thread per row and 512 threads per block.  All
+ * calls share the array, so calls that overlap on the GPU race: serialise
+ * them.  Asynchronous on the operator's stream. */
 int sed_op_apply_noalloc(sed_op* op, const double* x_dev, double* y_dev, int64_t n);
 void sed_op_destroy(sed_op* op);
 
 /* -------------------------------------------------------------------- solve */
-/* diagonalize_block_matrixfree (SRE:998-1030): lowest nev eigenpairs by
- * thick-restart Lanczos with full reorthogonalisation on the device.  tol is
- * the absolute Ritz-residual bound (the reference passes 1e-10), maxiter the
- * restart budget (300), krylovdim the basis size (0 = 30).  seed selects the
- * complex Gaussian start vector.  evecs_reim (nullable) receives nev
- * sector-ordered complex128 vectors, vector-major.  Mixed-precision operators
- * converge with the complex64 matvec (with two spare Ritz pairs), then run an
- * FP64 block-Davidson polish (Rayleigh-Ritz over the Ritz vectors and their
- * diagonally preconditioned FP64 residuals, at most 16 expansions); if that
- * misses max(tol, 1e-7 |E|) the sector is solved again entirely in FP64, so
- * the returned pairs always meet the FP64 residual bound. */
+/* diagonalize_block_matrixfree (SRE:998-1030): lowest nev eigenpairs.
+ * Sectors of dimension <= 500 take the reference's dense branch (every
+ * column from a device FP64 matvec, then a Hermitian eigensolve on the host);
+ * larger ones a thick-restart Lanczos with full reorthogonalisation on the
+ * device.  tol is the absolute Ritz-residual bound (the reference passes
+ * 1e-10), maxiter the restart budget (300), krylovdim the basis size (0 = 30).
+ * seed selects the complex Gaussian start vector.  evecs_reim (nullable)
+ * receives nev sector-ordered complex128 vectors, vector-major.
+ * Mixed-precision operators (SED_PREC_MIXED) run the Lanczos with complex64
+ * vectors and matvec until the Ritz estimates of the requested pairs fall
+ * below 1e-6 |E|, carrying two spare Ritz pairs; then one Rayleigh-Ritz step
+ * with FP64 matvecs over those nev + 2 Ritz vectors, orthonormalised through
+ * their Gram matrix, gives the eigenvalues and their FP64 residuals r.  A pair
+ * is accepted when r <= tol, or when it is isolated (gap > 2 r) and
+ * r^2 / gap <= 1e-10 |E|, gap being its distance to the lower end (Ritz value
+ * minus its residual) of the first Lanczos Ritz interval above the block;
+ * otherwise the Lanczos resumes with a 10x tighter threshold.  A run that
+ * stagnates at the complex64 noise floor is solved again entirely in FP64.
+ * Levels closer together than the complex64 run's residuals (about 1e-6 |E|)
+ * that it never separates into distinct Ritz values cannot be told apart by
+ * any residual test: such a cluster comes back as one level inside it (error
+ * at most its width); request SED_PREC_FP64 for spectra with such clusters.
+ * The first gather matvec of an operator (when it has no hop table) times
+ * eight launch shapes and waits on the host for them; later solves of the same
+ * catalog shape reuse the choice (see sed_op_set_apply_shape). */
 int sed_solve(sed_op* op, int nev, double tol, int maxiter, int krylovdim, uint64_t seed, double* evals,
               double* evecs_reim, sed_solve_info* info);
 
@@ -250,11 +290,14 @@ int sed_solve(sed_op* op, int nev, double tol, int maxiter, int krylovdim, uint6
  * build_translation_group, SRE:1374-1405), its bilinear amplitudes (n_bil
  * complex, same (i, j) list for every request) and its start-vector seed, so
  * its result does not depend on which other requests share the launch.
- * precision: SED_PREC_MIXED (complex64 matvec + FP64 block-Davidson polish;
- * a request whose polish misses its target is re-solved by the FP64 kernel in
- * a second launch) or SED_PREC_FP64.  Outputs per request: nev eigenvalues (ascending), status
- * (0 ok, SED_ERR_NOT_CONVERGED), sector dimension, |E_polished - E_c64| and
- * the matvec count. */
+ * precision: SED_PREC_MIXED or SED_PREC_FP64.  The mixed kernel follows the
+ * mixed sed_solve (complex64 Lanczos to 1e-6 |E|, then one FP64-class
+ * Rayleigh-Ritz step over the nev + 2 Ritz vectors, orthonormalised through
+ * their Gram matrix, with the same acceptance test, else continued); a
+ * request that stagnates at the complex64 noise floor is re-solved by the
+ * FP64 kernel in a second launch.  Outputs per request: nev
+ * eigenvalues (ascending), status (0 ok, SED_ERR_NOT_CONVERGED), sector
+ * dimension, |E_polished - E_c64| and the matvec count. */
 typedef struct sed_batch sed_batch;
 int sed_batch_create(const sed_catalog* c, int n_bil, const int32_t* bil_ij, int n_den, const int32_t* den_ij,
                      const double* den_v_reim, int precision, int nev, int krylovdim, int max_requests,

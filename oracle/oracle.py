@@ -85,6 +85,14 @@ def lib():
         L.or_op_solve.restype = i32
         L.or_op_solve.argtypes = [p, i32, dbl, i32, i32, u64, i32, p, p, p, p, p]
         L.or_max_threads.restype = i32
+        L.or_group_create.restype = p
+        L.or_group_create.argtypes = [i32, i32, p, p, i32, i32]
+        L.or_group_free.argtypes = [p]
+        L.or_group_state_entry.argtypes = [p, u64, p, p, p, p]
+        L.or_group_compatible.restype = i32
+        L.or_group_compatible.argtypes = [p, p, u64, dbl]
+        L.or_group_column.restype = i64
+        L.or_group_column.argtypes = [p, p, i32, p, p, i32, p, p, u64, dbl, p, p, p, i64]
         _lib = L
     return _lib
 
@@ -287,6 +295,55 @@ class Op:
                                _ptr(vecs) if vecs is not None else None, _ptr(nr), _ptr(nm), _ptr(res))
         return {"status": int(st), "evals": ev, "evecs": vecs, "restarts": int(nr[0]), "matvecs": int(nm[0]),
                 "residuals": res}
+
+
+class Group:
+    """Catalog-free oracle for sectors too large for an in-memory catalog:
+    table entries, compatibility and matrix columns for single masks, computed
+    straight from the group (SRE:371-487, 534-542, 627-632, 843-866)."""
+
+    def __init__(self, perm0: np.ndarray, phase: np.ndarray, identity0: int, stats: int):
+        self.perm0 = np.ascontiguousarray(perm0, dtype=np.int32)
+        self.phase = np.ascontiguousarray(phase, dtype=np.complex128)
+        n_ops, n_site = self.perm0.shape
+        self.h = lib().or_group_create(n_site, n_ops, _ptr(self.perm0), _ptr(self.phase), identity0, stats)
+        if not self.h:
+            raise ValueError(_err())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_group_free(self.h)
+            self.h = None
+
+    def state_entry(self, m: int):
+        """(representative, stabilizer order, rep_sym (1-based), rep_amp) of basis state m."""
+        r = np.zeros(1, dtype=np.uint64)
+        st = np.zeros(1, dtype=np.int32)
+        sym = np.zeros(1, dtype=np.int32)
+        amp = np.zeros(1, dtype=np.complex128)
+        lib().or_group_state_entry(self.h, C.c_uint64(int(m)), _ptr(r), _ptr(st), _ptr(sym), _ptr(amp))
+        return int(r[0]), int(st[0]), int(sym[0]), complex(amp[0])
+
+    def compatible(self, chi: np.ndarray, rep: int, atol: float = 1e-12) -> bool:
+        chi = np.ascontiguousarray(chi, dtype=np.complex128)
+        return bool(lib().or_group_compatible(self.h, _ptr(chi), C.c_uint64(int(rep)), atol))
+
+    def column(self, chi: np.ndarray, bilinear, density, rep_c: int, atol: float = 1e-12):
+        """Column rep_c of the sector matrix: (diagonal, [(target rep, element), ...])."""
+        chi = np.ascontiguousarray(chi, dtype=np.complex128)
+        bij = np.ascontiguousarray([[i, j] for (i, j, _) in bilinear], dtype=np.int32).reshape(-1, 2)
+        bt = np.ascontiguousarray([t for (_, _, t) in bilinear], dtype=np.complex128)
+        dij = np.ascontiguousarray([[i, j] for (i, j, _) in density], dtype=np.int32).reshape(-1, 2)
+        dv = np.ascontiguousarray([v for (_, _, v) in density], dtype=np.complex128)
+        cap = max(len(bt), 1)
+        tr = np.zeros(cap, dtype=np.uint64)
+        el = np.zeros(cap, dtype=np.complex128)
+        dg = np.zeros(1, dtype=np.complex128)
+        n = lib().or_group_column(self.h, _ptr(chi), len(bt), _ptr(bij), _ptr(bt), len(dv), _ptr(dij), _ptr(dv),
+                                  C.c_uint64(int(rep_c)), atol, _ptr(dg), _ptr(tr), _ptr(el), cap)
+        if n < 0:
+            raise RuntimeError("column buffer too small")
+        return complex(dg[0]), list(zip(tr[:n].tolist(), el[:n].tolist()))
 
 
 def max_threads() -> int:

@@ -905,6 +905,117 @@ void or_canonical(void* cat, uint64_t m, uint64_t* repr, int* g, double* amp) {
   amp[1] = a.im;
 }
 
+// ------------------------------------------------- catalog-free, one mask at a time
+// For sectors too large for an in-memory catalog (sampled parity checks): the
+// same table entries and matrix elements, evaluated for single masks straight
+// from the group.  Only the group is held.
+void* or_group_create(int n_site, int n_ops, const int32_t* perm, const double* phase, int identity, int stats) {
+  init_binom();
+  Group* G = new Group();
+  if (!make_group(*G, n_site, n_ops, perm, phase, identity, stats)) {
+    delete G;
+    return nullptr;
+  }
+  return G;
+}
+void or_group_free(void* g) { delete (Group*)g; }
+
+// The catalog entries of one basis state m (SRE:371-487): its orbit's
+// representative (the orbit minimum, SRE:442-453), the representative's
+// stabilizer order, and rep_sym / rep_amp as the reference's orbit expansion
+// leaves them -- the last g in 1..|G| with g(rep) = m wins (SRE:458-477):
+// sym = inverse(g) (1-based), amp = conj(alpha_g(rep)).
+void or_group_state_entry(void* gp, uint64_t m, uint64_t* rep_out, int32_t* stab_out, int32_t* sym_out,
+                          double* amp_out) {
+  const Group& G = *(Group*)gp;
+  uint64_t rep = m;
+  for (int g = 0; g < G.n_ops; ++g) {
+    uint64_t s;
+    cd a;
+    apply_op(G, g, m, &s, &a);
+    if (s < rep) rep = s;
+  }
+  int32_t order = 0, sym = 0;
+  cd amp{0.0, 0.0};
+  for (int g = 0; g < G.n_ops; ++g) {
+    uint64_t s;
+    cd a;
+    apply_op(G, g, rep, &s, &a);
+    if (s == rep) ++order;
+    if (s == m) {
+      sym = G.inv[g] + 1;
+      amp = cconj(a);
+    }
+  }
+  *rep_out = rep;
+  *stab_out = order;
+  *sym_out = sym;
+  amp_out[0] = amp.re;
+  amp_out[1] = amp.im;
+}
+
+// SRE:534-542 _is_orbit_compatible for one representative.
+static bool group_compatible(const Group& G, const cd* chi, uint64_t rep, double atol) {
+  for (int g = 0; g < G.n_ops; ++g) {
+    uint64_t s;
+    cd a;
+    apply_op(G, g, rep, &s, &a);
+    if (s == rep && !capprox(chi[g], a, atol)) return false;
+  }
+  return true;
+}
+int or_group_compatible(void* gp, const double* chi_reim, uint64_t rep, double atol) {
+  const Group& G = *(Group*)gp;
+  return group_compatible(G, (const cd*)chi_reim, rep, atol) ? 1 : 0;
+}
+
+// Column rep_c of the sector matrix by apply_hamiltonian!'s element formula
+// (SRE:843-866): the diagonal, then for every bilinear term valid on rep_c
+// (gate (m & hop) == from, XOR hop) the projected target (SRE:627-632, with the
+// table entries of or_group_state_entry) and, when its orbit belongs to the
+// sector, H[target, c] = t * s_JW * coeff * sqrt(stab_target) * (1/sqrt(stab_c)).
+// Writes at most max_out entries (target representative, element); returns
+// their number, or -1 when max_out is too small.
+int64_t or_group_column(void* gp, const double* chi_reim, int n_bil, const int32_t* bil_ij, const double* bil_t,
+                        int n_den, const int32_t* den_ij, const double* den_v, uint64_t rep_c, double atol,
+                        double* diag_out, uint64_t* target_rep, double* elem, int64_t max_out) {
+  const Group& G = *(Group*)gp;
+  const cd* chi = (const cd*)chi_reim;
+  cd d{0.0, 0.0};
+  for (int t = 0; t < n_den; ++t)
+    if (((rep_c >> den_ij[2 * t]) & 1ULL) && ((rep_c >> den_ij[2 * t + 1]) & 1ULL))
+      d = cadd(d, cd{den_v[2 * t], den_v[2 * t + 1]});
+  diag_out[0] = d.re;
+  diag_out[1] = d.im;
+  uint64_t r0;
+  int32_t stab_c, sym0;
+  double amp0[2];
+  or_group_state_entry(gp, rep_c, &r0, &stab_c, &sym0, amp0);
+  const double inv_sqrt_stab_col = 1.0 / std::sqrt((double)stab_c);
+  int64_t n = 0;
+  for (int t = 0; t < n_bil; ++t) {
+    const int i = bil_ij[2 * t], j = bil_ij[2 * t + 1];
+    const uint64_t from = 1ULL << i;
+    const uint64_t hop = from | (1ULL << j);
+    if ((rep_c & hop) != from) continue;
+    const uint64_t nm = rep_c ^ hop;
+    uint64_t rep;
+    int32_t stab_r, sym;
+    double amp[2];
+    or_group_state_entry(gp, nm, &rep, &stab_r, &sym, amp);
+    if (!group_compatible(G, chi, rep, atol)) continue;
+    const cd coeff = cmul(cd{amp[0], amp[1]}, cconj(chi[sym - 1]));
+    cd e = cmul(cmul(cd{bil_t[2 * t], bil_t[2 * t + 1]}, hopping_phase(G.stats, rep_c, i, j)), coeff);
+    e = cscale(cscale(e, std::sqrt((double)stab_r)), inv_sqrt_stab_col);
+    if (n >= max_out) return -1;
+    target_rep[n] = rep;
+    elem[2 * n] = e.re;
+    elem[2 * n + 1] = e.im;
+    ++n;
+  }
+  return n;
+}
+
 // Bilinear terms (i, j, t): a particle hops from site i to site j (0-based).
 void* or_op_create(void* s, int n_bil, const int32_t* bil_ij, const double* bil_t, int n_den, const int32_t* den_ij,
                    const double* den_v) {

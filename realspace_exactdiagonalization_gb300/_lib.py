@@ -51,6 +51,9 @@ SIGNATURES = [
     ("sed_group_inverse", _i32, [_p, _p]),
     ("sed_group_destroy", None, [_p]),
     ("sed_catalog_build", _i32, [_p, _i32, _p]),
+    ("sed_catalog_build_species", _i32, [_p, _i32, _i32, _i32, _p]),
+    ("sed_catalog_species", _i32, [_p, _p, _p, _p]),
+    ("sed_catalog_lookup", _i32, [_p, _i64, _p, _p, _p, _p]),
     ("sed_catalog_info", _i32, [_p, _p, _p, _p]),
     ("sed_catalog_get", _i32, [_p, _i32, _p, _i64]),
     ("sed_catalog_update_phases", _i32, [_p, _p]),

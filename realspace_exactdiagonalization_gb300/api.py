@@ -105,12 +105,14 @@ class Symmetry_Orbit_Catalog(_Handle):
 
     _destroy = "sed_catalog_destroy"
 
-    def __init__(self, h, dgroup: DeviceGroup, n_filled: int):
+    def __init__(self, h, dgroup: DeviceGroup, n_filled: int, species=None):
         super().__init__(h)
         self._dgroup = dgroup
         self.symmetry_group = dgroup.group
         self.particle_statistics = dgroup.stats
         self.n_filled = n_filled
+        # (n_split, n_lo, n_hi) for a two-species catalog, else None
+        self.species = tuple(species) if species else None
         ns, no, nst = C.c_int64(), C.c_int64(), C.c_int64()
         check(_lib.load().sed_catalog_info(h, C.byref(ns), C.byref(no), C.byref(nst)))
         self.n_states, self.n_orbits, self.n_stab_total = ns.value, no.value, nst.value
@@ -160,19 +162,42 @@ class Symmetry_Orbit_Catalog(_Handle):
     def rep_amp_table(self) -> np.ndarray:
         return self._get(_lib.FIELD_REP_AMP)
 
+    def lookup(self, masks) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(rep_rank, rep_sym, rep_amp) at the given masks, 1-based like the
+        whole tables, without reading the tables back."""
+        m = np.ascontiguousarray(masks, dtype=np.uint64)
+        rk = np.zeros(m.size, dtype=np.int32)
+        sy = np.zeros(m.size, dtype=np.int32)
+        am = np.zeros(m.size, dtype=np.complex128)
+        check(_lib.load().sed_catalog_lookup(self._h, m.size, ptr(m), ptr(rk), ptr(sy), ptr(am)))
+        return rk, sy, am
+
 
 def build_symmetry_orbit_catalog(*, second_quantized_model=None, n_filled: int,
                                  symmetry_group: Finite_Symmetry_Group,
-                                 particle_statistics: Particle_Statistics) -> Symmetry_Orbit_Catalog:
-    """SRE:371-487, on the device."""
+                                 particle_statistics: Particle_Statistics,
+                                 species=None) -> Symmetry_Orbit_Catalog:
+    """SRE:371-487, on the device.
+
+    ``species=(n_split, n_lo, n_hi)`` (an extension: the reference fixes only
+    the total particle number) restricts the catalog to n_lo particles on
+    sites 1..n_split and n_hi on the rest, e.g. one (N_up, N_down) block of a
+    Hubbard model whose up spins sit on the first half of the modes; n_filled
+    must then equal n_lo + n_hi."""
     if second_quantized_model is not None and second_quantized_model.lattice.n_site != symmetry_group.n_site:
         raise ValueError("the group and the model act on different numbers of sites")
     if not 0 <= n_filled <= symmetry_group.n_site:
         raise ValueError("n_filled must be in [0, n_site]")
     dg = DeviceGroup(symmetry_group, particle_statistics)
     h = C.c_void_p()
-    check(_lib.load().sed_catalog_build(dg.handle, n_filled, C.byref(h)))
-    return Symmetry_Orbit_Catalog(h, dg, n_filled)
+    if species:
+        n_split, n_lo, n_hi = species
+        if n_lo + n_hi != n_filled:
+            raise ValueError("n_filled must equal n_lo + n_hi of the species")
+        check(_lib.load().sed_catalog_build_species(dg.handle, n_split, n_lo, n_hi, C.byref(h)))
+    else:
+        check(_lib.load().sed_catalog_build(dg.handle, n_filled, C.byref(h)))
+    return Symmetry_Orbit_Catalog(h, dg, n_filled, species)
 
 
 def update_orbit_stabilizer_phases_(catalog: Symmetry_Orbit_Catalog, new_group: Finite_Symmetry_Group,
@@ -296,13 +321,28 @@ def colex_unrank(ranks: np.ndarray, n_site: int, n_filled: int) -> np.ndarray:
     return m
 
 
+def catalog_state_masks(catalog: "Symmetry_Orbit_Catalog", ranks: np.ndarray) -> np.ndarray:
+    """Masks of the catalog's basis states of the given ranks: colex k-subsets,
+    or for a two-species catalog rank = rank_hi * binom(n_split, n_lo) +
+    rank_lo (both ascending-mask orders)."""
+    from math import comb
+
+    n_site = catalog.symmetry_group.n_site
+    if not catalog.species:
+        return colex_unrank(ranks, n_site, catalog.n_filled)
+    n_split, n_lo, n_hi = catalog.species
+    r = np.asarray(ranks, dtype=np.int64)
+    lo = colex_unrank(r % comb(n_split, n_lo), n_split, n_lo)
+    hi = colex_unrank(r // comb(n_split, n_lo), n_site - n_split, n_hi)
+    return lo | np.left_shift(hi, np.uint64(n_split))
+
+
 def _expand_sector_state_to_fock_amplitudes(c: np.ndarray, basis: "Symmetry_Sector_Basis",
                                             particle_statistics=None, atol: float = 1e-12) -> Dict[int, complex]:
     """The reference's Dict{Mask, ComplexF64} form of expand_sector_state_to_fock."""
     dense = expand_sector_state_to_fock(c, basis, atol)
     nz = np.nonzero(dense)[0]
-    g = basis.catalog.symmetry_group
-    masks = colex_unrank(nz, g.n_site, basis.catalog.n_filled)
+    masks = catalog_state_masks(basis.catalog, nz)
     return {int(mk): complex(a) for mk, a in zip(masks, dense[nz])}
 
 

@@ -28,6 +28,7 @@
 #include <unordered_map>
 
 #include "../../include/sed_capi.h"
+#include "sed_handles.cuh"
 #include "sed_internal.cuh"
 
 #include "sed_dfloat.cuh"
@@ -1789,6 +1790,12 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       const int keep = final_rot ? min(nev, msz)
                                  : min(msz - 1, mixed ? nev + 2 : max(nev + (m - nev) / 2, nev + 1));
       if (threadIdx.x < keep) s_arrow[threadIdx.x] = beta * s_T[(msz - 1) * kMaxM + threadIdx.x];
+      // Lanczos residual of the first Ritz value after the polish block (the
+      // lower end of its inclusion interval bounds the gap in the check below)
+      if (threadIdx.x == 0) {
+        const int nwb = min(nev, msz);
+        s_misc[20] = (msz > nwb && !invariant) ? fabs(beta * s_T[(msz - 1) * kMaxM + nwb]) : 0.0;
+      }
       for (int i = threadIdx.x; i < msz * keep; i += blockDim.x) {
         const int q = i / keep, c = i % keep;
         float2 z;
@@ -1815,8 +1822,9 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         // FP64 matvecs over its nev + 2 Ritz vectors B = Vb[0..nw), the block
         // orthonormalised through its Gram matrix (rr_orthonormalise); accepted
         // when every requested pair meets the residual tolerance or the
-        // quadratic bound |dE| <= |r|^2 / gap (gap to the first Lanczos Ritz
-        // value outside the block) is below kMixedRelTarget |E|.  Otherwise
+        // quadratic bound |dE| <= |r|^2 / gap (gap to the lower end of the
+        // first Lanczos Ritz interval outside the block) is below
+        // kMixedRelTarget |E|.  Otherwise
         // the Lanczos resumes with a tighter threshold; a stagnated run is
         // re-solved by the FP64 kernel (status kPolishFailed).
         const int nw = min(nev, msz);
@@ -1949,14 +1957,15 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
             }
         }
         block_sum<kMaxNev>(rr, s_red, s_misc + 8);
-        const double thL = msz > nw ? s_theta[nw] : HUGE_VAL;
+        // every requested pair must pass mixed_pair_accepted: isolated, and
+        // the quadratic bound with the gap to the lower end theta_L - r_L of
+        // the first Lanczos Ritz interval above the block
+        const double thL = msz > nw ? s_theta[nw] - s_misc[20] : HUGE_VAL;
         bool ok = true;
         dmax = 0.0;
         for (int i = 0; i < nev_out; ++i) {
-          const double r2 = s_misc[8 + i], gap = thL - s_lam[i];
           dmax = fmax(dmax, fabs(s_lam[i] - s_theta[i]));
-          ok = ok && (sqrt(r2) <= a.tol ||
-                      (gap > 0.0 && r2 <= kMixedRelTarget * fmax(fabs(s_lam[i]), 1e-6 * scale) * gap));
+          ok = ok && mixed_pair_accepted(s_lam[i], s_misc[8 + i], thL, a.tol, scale);
         }
         __syncthreads();
         if (ok) {
@@ -2065,25 +2074,19 @@ struct BatchImpl {
   }
 };
 
-// The shared-memory opt-in is a property of each kernel instantiation,
-// shared by every batch object (and host thread) that launches it: it is only
-// ever raised, and raised-and-launched under one lock, so a concurrent batch
-// with a smaller footprint cannot undercut a launch in progress.
+// The shared-memory opt-in is a property of each kernel instantiation on each
+// device, shared by every batch object (and host thread) that launches it: it
+// is only ever raised, and raised-and-launched under one lock, so a concurrent
+// batch with a smaller footprint cannot undercut a launch in progress.
 template <class P, bool F, bool PH, bool XS>
 struct KernelSmem {
   static std::mutex& mu() {
     static std::mutex m;
     return m;
   }
-  static size_t& configured() {
-    static size_t c = 0;
-    return c;
-  }
   static void ensure(size_t bytes) {
-    if (bytes > configured()) {
-      SED_CUDA(cudaFuncSetAttribute(k_batch<P, F, PH, XS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-      configured() = bytes;
-    }
+    static SmemOptIn optin;
+    optin.ensure(k_batch<P, F, PH, XS>, bytes);
   }
 };
 
@@ -2489,6 +2492,7 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
     SED_REQUIRE(i != j, 1, "a bilinear term (i, i, t) changes the particle number; write it as a density term");
     by_site[i].push_back({j, k});
   }
+  check_species_terms(C, n_bil, bil_ij);
   B->tt.site_off.assign(G.n_site + 1, 0);
   for (int i = 0; i < G.n_site; ++i) {
     B->tt.site_off[i] = (uint16_t)B->tt.rec.size();
@@ -2744,12 +2748,6 @@ void batch_last_stats(const BatchImpl& B, int64_t* hops, int64_t* t0, int64_t* t
 }  // namespace sed
 
 // ------------------------------------------------------------------ C ABI
-struct sed_batch {
-  std::shared_ptr<sed::BatchImpl> p;
-};
-struct sed_catalog {
-  std::shared_ptr<sed::CatalogImpl> p;
-};
 
 template <class F>
 static int bguard(F&& f) {

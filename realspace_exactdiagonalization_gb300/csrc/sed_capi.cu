@@ -5,20 +5,8 @@
 #include <string>
 
 #include "../../include/sed_capi.h"
+#include "sed_handles.cuh"
 #include "sed_internal.cuh"
-
-struct sed_group {
-  std::shared_ptr<sed::GroupImpl> p;
-};
-struct sed_catalog {
-  std::shared_ptr<sed::CatalogImpl> p;
-};
-struct sed_sector {
-  std::shared_ptr<sed::SectorImpl> p;
-};
-struct sed_op {
-  std::shared_ptr<sed::OpImpl> p;
-};
 
 namespace sed {
 static thread_local std::string g_last_error;
@@ -85,6 +73,30 @@ int sed_catalog_build(const sed_group* g, int n_filled, sed_catalog** out) {
     *out = nullptr;
     auto c = sed::build_catalog(g->p, n_filled);
     *out = new sed_catalog{c};
+  });
+}
+int sed_catalog_build_species(const sed_group* g, int n_split, int n_lo, int n_hi, sed_catalog** out) {
+  return guarded([&] {
+    REQ(g && out, "NULL argument");
+    *out = nullptr;
+    REQ(n_split > 0, "n_split must be positive (sed_catalog_build serves one species)");
+    auto c = sed::build_catalog(g->p, n_lo + n_hi, n_split, n_lo, n_hi);
+    *out = new sed_catalog{c};
+  });
+}
+int sed_catalog_lookup(const sed_catalog* c, int64_t n, const uint64_t* masks, int32_t* rep_rank, int32_t* rep_sym,
+                       double* rep_amp_reim) {
+  return guarded([&] {
+    REQ(c, "NULL argument");
+    sed::catalog_lookup(*c->p, n, masks, rep_rank, rep_sym, rep_amp_reim);
+  });
+}
+int sed_catalog_species(const sed_catalog* c, int* n_split, int* n_lo, int* n_hi) {
+  return guarded([&] {
+    REQ(c, "NULL argument");
+    if (n_split) *n_split = c->p->split;
+    if (n_lo) *n_lo = c->p->split > 0 ? c->p->n_lo : c->p->n_filled;
+    if (n_hi) *n_hi = c->p->split > 0 ? c->p->n_hi : 0;
   });
 }
 int sed_catalog_info(const sed_catalog* c, int64_t* n_states, int64_t* n_orbits, int64_t* n_stab_total) {

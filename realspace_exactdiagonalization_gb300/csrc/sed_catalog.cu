@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 
+#include <atomic>
 #include <mutex>
 
 #include "sed_internal.cuh"
@@ -39,35 +40,67 @@ int64_t binom64(int n, int k) {
   return g_binom[n][k];
 }
 
-void build_rank_table(int N, int k, RankTable& rt, cudaStream_t s) {
+// Two conserved species (split L > 0): modes [0, L) hold klo particles and
+// modes [L, N) hold khi, and the rank of a state is
+//   rank_hi(m >> L) * binom(L, klo) + rank_lo(m & (2^L - 1)),
+// each part a colex rank of its own subset.  Rank order is then ascending-mask
+// order, the reference's catalog order restricted to the (klo, khi) block.
+// Every low particle lies below bit L, so p (the set bits below chunk c)
+// still determines each bit's index within its own species -- p itself below
+// L, p - klo above it -- and rank_of reads the split tables unchanged.
+// split = 0: one species of k = klo particles on all N modes.
+void build_rank_table(int N, int split, int klo, int khi, RankTable& rt, cudaStream_t s) {
   init_binom();
+  const int L = split > 0 ? split : N;
+  const int k = split > 0 ? klo + khi : klo;
+  if (split <= 0) khi = 0;
+  const uint64_t clo = (uint64_t)binom64(L, klo);
   RankParams rp{};
   rp.nchunk = (N + 7) / 8;
   int total = 0;
+  std::vector<int> pmaxs(rp.nchunk);
   for (int c = 0; c < rp.nchunk; ++c) {
-    const int pmin = std::max(0, k - (N - 8 * c));
-    const int pmax = std::min(k, 8 * c);
+    const int s0 = 8 * c;
+    int pmin, pmax;
+    if (s0 <= L) {  // every bit below the chunk is a low-species mode
+      pmin = std::max(0, klo - (L - s0));
+      pmax = std::min(klo, s0);
+    } else {        // all klo low particles lie below the chunk
+      pmin = klo + std::max(0, khi - (N - s0));
+      pmax = klo + std::min(khi, s0 - L);
+    }
+    if (split <= 0) {
+      pmin = std::max(0, k - (N - s0));
+      pmax = std::min(k, s0);
+    }
     rp.pmin[c] = pmin;
     rp.off[c] = total;
+    pmaxs[c] = pmax;
     total += (std::max(pmax - pmin + 1, 1)) * 256;
   }
   rp.total = total;
   rt.host.assign(total, 0u);
   for (int c = 0; c < rp.nchunk; ++c) {
-    const int pmin = rp.pmin[c], pmax = std::min(k, 8 * c);
+    const int s0 = 8 * c, pmin = rp.pmin[c], pmax = pmaxs[c];
     for (int p = pmin; p <= pmax; ++p)
       for (int v = 0; v < 256; ++v) {
         uint64_t sum = 0;
-        int t = 0;
+        int jl = s0 <= L ? p : klo, jh = s0 <= L ? 0 : p - klo;
         bool ok = true;
         for (int b = 0; b < 8; ++b)
           if ((v >> b) & 1) {
-            const int pos = 8 * c + b;
-            if (pos >= N) ok = false;
-            sum += (uint64_t)binom64(pos, p + t + 1);
-            ++t;
+            const int pos = s0 + b;
+            if (pos >= N) {
+              ok = false;
+            } else if (pos < L) {
+              sum += (uint64_t)binom64(pos, jl + 1);
+              ++jl;
+            } else {
+              sum += clo * (uint64_t)binom64(pos - L, jh + 1);
+              ++jh;
+            }
           }
-        if (!ok || p + t > k || sum > 0xFFFFFFFFull) sum = 0;
+        if (!ok || jl > (split > 0 ? klo : k) || jh > khi || sum > 0xFFFFFFFFull) sum = 0;
         rt.host[rp.off[c] + ((p - pmin) << 8) + v] = (uint32_t)sum;
       }
   }
@@ -75,16 +108,25 @@ void build_rank_table(int N, int k, RankTable& rt, cudaStream_t s) {
   upload(rt.dev, rt.host, s);
 }
 
+int current_device() {
+  int d = 0;
+  SED_CUDA(cudaGetDevice(&d));
+  SED_REQUIRE(d >= 0 && d < kMaxDevices, 5, "device ordinal above the library's limit of 64");
+  return d;
+}
+
 int device_sm_count() {
-  // initialised once, thread-safely, by the first caller of any thread (a
-  // failed query throws and leaves it for the next call)
-  static const int sms = [] {
-    int d = 0, n = 0;
-    SED_CUDA(cudaGetDevice(&d));
+  // one entry per device, filled by the first query on that device (a failed
+  // query throws and leaves it for the next call; concurrent first queries
+  // store the same value)
+  static std::atomic<int> sms[kMaxDevices];
+  const int d = current_device();
+  int n = sms[d].load(std::memory_order_relaxed);
+  if (n <= 0) {
     SED_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d));
-    return n;
-  }();
-  return sms;
+    sms[d].store(n, std::memory_order_relaxed);
+  }
+  return n;
 }
 
 // ---------------------------------------------------------------------- group
@@ -252,9 +294,35 @@ __device__ __forceinline__ uint64_t unrank_colex(uint64_t r, int N, int k, const
   return m;
 }
 
+// The enumeration of a catalog's basis states in rank order: colex k-subsets
+// of N modes, or (split L > 0) the two-species product with the high species
+// as the major index (see build_rank_table).
+struct EnumParams {
+  int N, k;        // one species: k particles on N modes
+  int L, klo, khi; // two species (L > 0): klo on [0, L), khi on [L, N)
+  uint64_t clo;    // binom(L, klo)
+};
+
+__device__ __forceinline__ uint64_t enum_unrank(uint64_t r, const EnumParams& e, const uint64_t* __restrict__ binom) {
+  if (e.L == 0) return unrank_colex(r, e.N, e.k, binom);
+  return unrank_colex(r % e.clo, e.L, e.klo, binom) | (unrank_colex(r / e.clo, e.N - e.L, e.khi, binom) << e.L);
+}
+
+// the state after m in rank order (called only when one exists)
+__device__ __forceinline__ uint64_t enum_next(uint64_t m, const EnumParams& e) {
+  if (e.L == 0) return dev::gosper_next(m);
+  const uint64_t lomask = (1ULL << e.L) - 1ULL;
+  if (e.klo > 0) {
+    const uint64_t nl = dev::gosper_next(m & lomask);
+    if (!(nl >> e.L)) return (m & ~lomask) | nl;
+  }
+  if (e.khi == 0) return m;  // unreachable: no state follows the last one
+  return ((1ULL << e.klo) - 1ULL) | (dev::gosper_next(m >> e.L) << e.L);
+}
+
 // SRE:434-455: a mask is a representative iff no group image is smaller
 // (early exit on the first smaller image).  One flag bit per colex rank.
-__global__ void __launch_bounds__(256) k_find_reps(int64_t n_states, int N, int k, int G,
+__global__ void __launch_bounds__(256) k_find_reps(int64_t n_states, EnumParams e, int G,
                                                    const uint8_t* __restrict__ perm_g,
                                                    const uint64_t* __restrict__ binom, uint32_t* __restrict__ flags) {
   __shared__ uint8_t sperm[SED_MAX_OPS * 64];
@@ -262,7 +330,7 @@ __global__ void __launch_bounds__(256) k_find_reps(int64_t n_states, int N, int 
   __syncthreads();
   const int64_t nw = (n_states + 31) / 32;
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
-    uint64_t m = unrank_colex((uint64_t)w * 32, N, k, binom);
+    uint64_t m = enum_unrank((uint64_t)w * 32, e, binom);
     const int cnt = (int)min((int64_t)32, n_states - w * 32);
     uint32_t f = 0;
     for (int b = 0; b < cnt; ++b) {
@@ -273,7 +341,7 @@ __global__ void __launch_bounds__(256) k_find_reps(int64_t n_states, int N, int 
           break;
         }
       if (rep) f |= 1u << b;
-      if (b + 1 < cnt) m = dev::gosper_next(m);
+      if (b + 1 < cnt) m = enum_next(m, e);
     }
     flags[w] = f;
   }
@@ -283,7 +351,7 @@ __global__ void __launch_bounds__(256) k_find_reps(int64_t n_states, int N, int 
 // writes the state word of g(rep) (the last g wins where the stabilizer is
 // non-trivial, exactly as the reference's loop overwrites), plus the
 // representative list and stabilizer order in catalog order.
-__global__ void __launch_bounds__(256) k_expand(int64_t n_states, int N, int k, int G, int fermi,
+__global__ void __launch_bounds__(256) k_expand(int64_t n_states, EnumParams e, int G, int fermi,
                                                 const uint8_t* __restrict__ perm_g,
                                                 const uint64_t* __restrict__ binom,
                                                 const uint32_t* __restrict__ flags,
@@ -302,14 +370,14 @@ __global__ void __launch_bounds__(256) k_expand(int64_t n_states, int N, int k, 
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
     uint32_t f = flags[w];
     if (!f) continue;
-    uint64_t m = unrank_colex((uint64_t)w * 32, N, k, binom);
+    uint64_t m = enum_unrank((uint64_t)w * 32, e, binom);
     int pos = 0;
     uint32_t o = offs[w];
     while (f) {
       const int b = __ffs(f) - 1;
       f &= f - 1;
       while (pos < b) {
-        m = dev::gosper_next(m);
+        m = enum_next(m, e);
         ++pos;
       }
       int so = 0;
@@ -344,19 +412,39 @@ static int grid_for(int64_t work, int block) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, sms * 16));
 }
 
-std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> gp, int n_filled) {
+std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> gp, int n_filled, int split, int n_lo,
+                                           int n_hi) {
   const GroupImpl& G = *gp;
-  SED_REQUIRE(n_filled >= 0 && n_filled <= G.n_site, 1, "n_filled must be in [0, n_site]");
-  const int64_t n_states = binom64(G.n_site, n_filled);
-  SED_REQUIRE(n_states < (int64_t)0xFFFFFFFFll, 5, "binomial(n_site, n_filled) must be below 2^32");
+  int64_t n_states = 0;
+  if (split > 0) {
+    SED_REQUIRE(split < G.n_site, 1, "the species split must lie inside the lattice: 0 < n_split < n_site");
+    SED_REQUIRE(n_lo >= 0 && n_lo <= split && n_hi >= 0 && n_hi <= G.n_site - split, 1,
+                "species particle numbers must be in [0, modes of the species]");
+    for (int g = 0; g < G.n_ops; ++g)
+      for (int i = 0; i < G.n_site; ++i)
+        SED_REQUIRE((G.perm[(size_t)g * G.n_site + i] < split) == (i < split), 1,
+                    "every symmetry operation must map each species onto itself");
+    n_filled = n_lo + n_hi;
+    n_states = binom64(split, n_lo) * binom64(G.n_site - split, n_hi);
+    SED_REQUIRE(n_states < (int64_t)0xFFFFFFFFll, 5,
+                "binomial(n_split, n_lo) * binomial(n_site - n_split, n_hi) must be below 2^32");
+  } else {
+    SED_REQUIRE(n_filled >= 0 && n_filled <= G.n_site, 1, "n_filled must be in [0, n_site]");
+    n_states = binom64(G.n_site, n_filled);
+    SED_REQUIRE(n_states < (int64_t)0xFFFFFFFFll, 5, "binomial(n_site, n_filled) must be below 2^32");
+    split = n_lo = n_hi = 0;
+  }
   auto c = std::make_shared<CatalogImpl>();
   c->group = gp;
   c->n_filled = n_filled;
+  c->split = split;
+  c->n_lo = n_lo;
+  c->n_hi = n_hi;
   c->n_states = n_states;
   SED_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   c->own_stream = true;
   cudaStream_t s = c->stream;
-  build_rank_table(G.n_site, n_filled, c->rank, s);
+  build_rank_table(G.n_site, split, split > 0 ? n_lo : n_filled, n_hi, c->rank, s);
   SED_REQUIRE((size_t)c->rank.rp.total * 4 <= 160 * 1024, 5, "rank table exceeds the shared-memory budget");
   std::vector<uint8_t> perm_u8((size_t)G.n_ops * 64, 0);
   for (int g = 0; g < G.n_ops; ++g)
@@ -376,7 +464,8 @@ std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> gp, int n_
   SED_CUDA(cudaMemsetAsync(c->state.p, 0xFF, (size_t)n_states * 8, s));
   const int64_t nw = (n_states + 31) / 32;
   DevBuf flags((size_t)nw * 4), offs((size_t)nw * 4);
-  k_find_reps<<<grid_for(nw, 256), 256, 0, s>>>(n_states, G.n_site, n_filled, G.n_ops, c->perm_u8.as<uint8_t>(),
+  EnumParams e{G.n_site, n_filled, split, n_lo, n_hi, split > 0 ? (uint64_t)binom64(split, n_lo) : 1};
+  k_find_reps<<<grid_for(nw, 256), 256, 0, s>>>(n_states, e, G.n_ops, c->perm_u8.as<uint8_t>(),
                                                 c->binom.as<uint64_t>(), flags.as<uint32_t>());
   SED_CUDA(cudaGetLastError());
   c->n_orbits = (int64_t)scan_popcount(flags.as<uint32_t>(), nw, offs.as<uint32_t>(), s);
@@ -385,18 +474,15 @@ std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> gp, int n_
   const size_t smem = (size_t)c->rank.rp.total * 4;
   {
     // the opt-in covers the dynamic part (the kernel also holds 4 KB of static
-    // shared memory); it is a property of the kernel, shared by every catalog
-    // and host thread, so it is only raised, and raised-and-launched under
-    // one lock: a concurrent build with a smaller rank table cannot undercut
-    // this launch
+    // shared memory); it is a property of the kernel on each device, shared
+    // by every catalog and host thread, so it is only raised, and
+    // raised-and-launched under one lock: a concurrent build with a smaller
+    // rank table cannot undercut this launch
     static std::mutex mu;
-    static size_t configured = 0;
+    static SmemOptIn optin;
     std::lock_guard<std::mutex> lock(mu);
-    if (smem > configured) {
-      SED_CUDA(cudaFuncSetAttribute(k_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      configured = smem;
-    }
-    k_expand<<<grid_for(nw, 256), 256, smem, s>>>(n_states, G.n_site, n_filled, G.n_ops, G.stats,
+    optin.ensure(k_expand, smem);
+    k_expand<<<grid_for(nw, 256), 256, smem, s>>>(n_states, e, G.n_ops, G.stats,
                                                   c->perm_u8.as<uint8_t>(), c->binom.as<uint64_t>(),
                                                   flags.as<uint32_t>(), offs.as<uint32_t>(),
                                                   c->rank.dev.as<uint32_t>(), c->rank.rp, c->inv_u8.as<uint8_t>(),
@@ -412,6 +498,13 @@ std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> gp, int n_
   for (uint8_t v : c->stab_host) tot += v;
   c->n_stab_total = tot;
   return c;
+}
+
+void check_species_terms(const CatalogImpl& c, int n_bil, const int32_t* bil_ij) {
+  if (c.split <= 0) return;
+  for (int k = 0; k < n_bil; ++k)
+    SED_REQUIRE((bil_ij[2 * k] < c.split) == (bil_ij[2 * k + 1] < c.split), 1,
+                "a bilinear term moves a particle between the two conserved species");
 }
 
 void catalog_update_phases(CatalogImpl& c, std::shared_ptr<GroupImpl> g) {
@@ -672,6 +765,58 @@ __global__ void k_sector_project(int64_t n, const uint64_t* __restrict__ masks, 
   }
 }
 
+// The reference's three tables at single masks (rank -> state word), for
+// sampled checks of catalogs too large to read back whole.
+__global__ void k_lookup(int64_t n, const uint64_t* __restrict__ masks, const uint64_t* __restrict__ state,
+                         const uint64_t* __restrict__ reps, int G, int N, int fermi, const uint8_t* __restrict__ perm_g,
+                         const uint8_t* __restrict__ inv, const double2* __restrict__ phase,
+                         const uint32_t* __restrict__ rank_tab, RankParams rp, int32_t* rank_out, int32_t* sym_out,
+                         double2* amp_out) {
+  __shared__ uint8_t sperm[SED_MAX_OPS * 64];
+  for (int i = threadIdx.x; i < G * 64; i += blockDim.x) sperm[i] = perm_g[i];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t w = state[dev::rank_of(masks[i], rank_tab, rp)];
+    const uint32_t o = (uint32_t)w;
+    if (o == SED_UNSET_ORBIT) {
+      rank_out[i] = 0;
+      sym_out[i] = 0;
+      amp_out[i] = make_double2(0.0, 0.0);
+      continue;
+    }
+    const int g = (int)((w >> 32) & 0xFF);
+    rank_out[i] = (int32_t)o + 1;
+    sym_out[i] = (int32_t)inv[g] + 1;
+    double2 a;
+    dev::apply_full(reps[o], sperm + g * 64, phase + (size_t)g * N, fermi, &a);
+    amp_out[i] = make_double2(a.x, -a.y);
+  }
+}
+
+void catalog_lookup(const CatalogImpl& c, int64_t n, const uint64_t* masks, int32_t* rank, int32_t* sym,
+                    double* amp) {
+  const GroupImpl& G = *c.group;
+  SED_REQUIRE(n >= 0 && (n == 0 || (masks && rank && sym && amp)), 1, "NULL argument");
+  const uint64_t valid = (1ULL << G.n_site) - 1ULL;
+  for (int64_t i = 0; i < n; ++i)
+    SED_REQUIRE((masks[i] & ~valid) == 0 && catalog_holds(c, masks[i]), 1,
+                c.split > 0 ? "every mask must hold n_lo particles below n_split and n_hi above it"
+                            : "every mask must hold n_filled particles on the lattice sites");
+  if (n == 0) return;
+  cudaStream_t s = c.stream;
+  DevBuf dm((size_t)n * 8), dr((size_t)n * 4), ds((size_t)n * 4), da((size_t)n * 16);
+  SED_CUDA(cudaMemcpyAsync(dm.p, masks, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+  k_lookup<<<grid_for(n, 256), 256, 0, s>>>(n, dm.as<uint64_t>(), c.state.as<uint64_t>(), c.reps.as<uint64_t>(),
+                                            G.n_ops, G.n_site, G.stats, c.perm_u8.as<uint8_t>(),
+                                            c.inv_u8.as<uint8_t>(), c.phase.as<double2>(), c.rank.dev.as<uint32_t>(),
+                                            c.rank.rp, dr.as<int32_t>(), ds.as<int32_t>(), da.as<double2>());
+  SED_CUDA(cudaGetLastError());
+  SED_CUDA(cudaMemcpyAsync(rank, dr.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+  SED_CUDA(cudaMemcpyAsync(sym, ds.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+  SED_CUDA(cudaMemcpyAsync(amp, da.p, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+  SED_CUDA(cudaStreamSynchronize(s));
+}
+
 __global__ void k_orbit_row(int64_t dim, const uint32_t* __restrict__ row_orbit, int32_t* __restrict__ orbit_row) {
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x)
     orbit_row[row_orbit[r]] = (int32_t)r;
@@ -683,8 +828,9 @@ void sector_project(const SectorImpl& S, int64_t n, const uint64_t* masks, int64
   SED_REQUIRE(n >= 0 && (n == 0 || (masks && rows && coeff)), 1, "NULL argument");
   const uint64_t valid = G.n_site == 64 ? ~0ULL : ((1ULL << G.n_site) - 1ULL);
   for (int64_t i = 0; i < n; ++i)
-    SED_REQUIRE((masks[i] & ~valid) == 0 && __builtin_popcountll(masks[i]) == c.n_filled, 1,
-                "every mask must hold n_filled particles on the lattice sites");
+    SED_REQUIRE((masks[i] & ~valid) == 0 && catalog_holds(c, masks[i]), 1,
+                c.split > 0 ? "every mask must hold n_lo particles below n_split and n_hi above it"
+                            : "every mask must hold n_filled particles on the lattice sites");
   if (n == 0) return;
   cudaStream_t s = c.stream;
   DevBuf orow((size_t)std::max<int64_t>(c.n_orbits, 1) * 4), dm((size_t)n * 8), dr((size_t)n * 8),

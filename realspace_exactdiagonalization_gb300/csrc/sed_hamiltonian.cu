@@ -419,6 +419,7 @@ std::shared_ptr<OpImpl> make_op(std::shared_ptr<SectorImpl> sp, int n_bil, const
   const CatalogImpl& C = *S.cat;
   const GroupImpl& G = *S.group;
   check_hermitian_symmetric(G, n_bil, bil_ij, bil_t);
+  check_species_terms(C, n_bil, bil_ij);
   for (int k = 0; k < n_den; ++k)
     SED_REQUIRE(den_ij[2 * k] >= 0 && den_ij[2 * k] < G.n_site && den_ij[2 * k + 1] >= 0 &&
                     den_ij[2 * k + 1] < G.n_site,
@@ -538,16 +539,14 @@ static void launch_apply_tpr(const ApplyArgs& a, const void* xs, double* y, cuda
   const SmemLayout<V> L = SmemLayout<V>::make(a, T);
   auto kern = k_apply<P, F, PH, T, TPR>;
   SED_REQUIRE(L.total <= 200 * 1024, 5, "operator tables exceed the shared-memory budget");
-  // the shared-memory opt-in is a property of the kernel, shared by every
-  // operator: raise it (never lower it) and launch under one lock, so a
-  // concurrent caller with a smaller footprint cannot undercut this launch
+  // the shared-memory opt-in is a property of the kernel on each device,
+  // shared by every operator: raise it (never lower it) and launch under one
+  // lock, so a concurrent caller with a smaller footprint cannot undercut this
+  // launch
   static std::mutex mu;
-  static size_t configured = 0;
+  static SmemOptIn optin;
   std::lock_guard<std::mutex> lock(mu);
-  if (L.total > configured) {
-    SED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
-    configured = L.total;
-  }
+  optin.ensure(kern, L.total);
   int blocks_per_sm = 0;
   SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, block, L.total));
   blocks_per_sm = std::max(blocks_per_sm, 1);
@@ -626,9 +625,13 @@ static bool env_shape(ApplyShape* out) {
   return false;
 }
 
+// allow_tune = false (the allocation-free matvec): no timing runs and no host
+// synchronisation; the shape is the operator's, the pinned one, the one
+// remembered for this catalog shape, or the default (1, 512), and nothing is
+// stored on the operator, so a later allocating matvec still tunes.
 template <class P>
 static ApplyShape apply_shape(OpImpl& op, const ApplyArgs& a, bool fp32, const void* xs, double* ypad,
-                              cudaStream_t s) {
+                              cudaStream_t s, bool allow_tune) {
   const int k = fp32 ? 1 : 0;
   if (op.apply_tpr[k] > 0) return ApplyShape{op.apply_tpr[k], op.apply_block[k]};
   ApplyShape best{1, 512};
@@ -644,6 +647,7 @@ static ApplyShape apply_shape(OpImpl& op, const ApplyArgs& a, bool fp32, const v
       found = true;
     }
   }
+  if (!found && !allow_tune) return best;
   if (!found) {
     cudaEvent_t e0, e1;
     SED_CUDA(cudaEventCreate(&e0));
@@ -684,7 +688,8 @@ void op_set_apply_shape(OpImpl& op, int tpr, int block) {
   op.apply_block[0] = op.apply_block[1] = block;
 }
 
-static void apply_impl(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s) {
+static void apply_impl(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream_t s,
+                       bool allow_tune = true) {
   const GroupImpl& G = *op.sec->group;
   if (op.sec->cat->n_orbits == 0) return;
   if (op.tab_built) {  // the stored form of the same matvec (sed_optable.cu)
@@ -694,14 +699,18 @@ static void apply_impl(OpImpl& op, bool fp32, const void* xs, double* ypad, cuda
   const ApplyArgs a = make_args(op, fp32);
   if (fp32)
     dispatch_apply<P32>(a, G.stats == 1, G.has_phases, op.tchi_in_smem, xs, ypad, s,
-                        apply_shape<P32>(op, a, true, xs, ypad, s));
+                        apply_shape<P32>(op, a, true, xs, ypad, s, allow_tune));
   else
     dispatch_apply<P64>(a, G.stats == 1, G.has_phases, op.tchi_in_smem, xs, ypad, s,
-                        apply_shape<P64>(op, a, false, xs, ypad, s));
+                        apply_shape<P64>(op, a, false, xs, ypad, s, allow_tune));
 }
 
 void op_apply_orbit(OpImpl& op, const void* xs, double* ypad, cudaStream_t s) {
   apply_impl(op, op.precision == 1, xs, ypad, s);
+}
+
+void op_apply_orbit_untuned(OpImpl& op, const void* xs, double* ypad, cudaStream_t s) {
+  apply_impl(op, op.precision == 1, xs, ypad, s, false);
 }
 
 bool op_apply_orbit_cf(OpImpl& op, const void* xs, float2* y, cudaStream_t s) {

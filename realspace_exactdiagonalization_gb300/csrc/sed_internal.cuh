@@ -102,7 +102,7 @@ struct RankTable {
   std::vector<uint32_t> host;
   DevBuf dev;
 };
-void build_rank_table(int n_site, int k, RankTable& rt, cudaStream_t s);
+void build_rank_table(int n_site, int split, int klo, int khi, RankTable& rt, cudaStream_t s);
 
 // host binomial table (exact int64)
 int64_t binom64(int n, int k);
@@ -119,6 +119,10 @@ struct GroupImpl {
 struct CatalogImpl {
   std::shared_ptr<GroupImpl> group;
   int n_filled = 0;
+  // two conserved species (split > 0): n_lo particles on modes [0, split),
+  // n_hi on [split, n_site), n_filled = n_lo + n_hi; states are ranked
+  // rank_hi * binom(split, n_lo) + rank_lo (build_rank_table)
+  int split = 0, n_lo = 0, n_hi = 0;
   int64_t n_states = 0, n_orbits = 0, n_stab_total = 0;
   RankTable rank;
   DevBuf state, reps, stab;            // see layout above
@@ -200,8 +204,18 @@ void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream
 // ----------------------------------------------------------- entry points
 std::shared_ptr<GroupImpl> make_group(int n_site, int n_ops, const int32_t* perm, const double* phase, int identity,
                                       int stats);
-std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> g, int n_filled);
+std::shared_ptr<CatalogImpl> build_catalog(std::shared_ptr<GroupImpl> g, int n_filled, int split = 0, int n_lo = 0,
+                                           int n_hi = 0);
+// the mask carries the catalog's particle numbers (per species when split)
+inline bool catalog_holds(const CatalogImpl& c, uint64_t m) {
+  if (c.split <= 0) return __builtin_popcountll(m) == c.n_filled;
+  const uint64_t lo = m & ((1ULL << c.split) - 1ULL);
+  return __builtin_popcountll(lo) == c.n_lo && __builtin_popcountll(m ^ lo) == c.n_hi;
+}
+// bilinear terms must keep every particle in its species (SED_ERR_ARG)
+void check_species_terms(const CatalogImpl& c, int n_bil, const int32_t* bil_ij);
 void catalog_readback(const CatalogImpl& c, int field, void* out, int64_t out_bytes);
+void catalog_lookup(const CatalogImpl& c, int64_t n, const uint64_t* masks, int32_t* rank, int32_t* sym, double* amp);
 void catalog_update_phases(CatalogImpl& c, std::shared_ptr<GroupImpl> g);
 std::shared_ptr<SectorImpl> build_sector(std::shared_ptr<CatalogImpl> c, const double* chi, double atol,
                                          std::shared_ptr<GroupImpl> g = nullptr);
@@ -220,6 +234,10 @@ void check_hermitian_symmetric(const GroupImpl& G, int n_bil, const int32_t* bil
 void op_apply_host(OpImpl& op, const double* x, double* y, int64_t n, bool device_ptrs);
 // y_pad (complex128, orbit-indexed) = H x given xs = sqrt(stab) * x in the op precision
 void op_apply_orbit(OpImpl& op, const void* xs, double* ypad, cudaStream_t s);
+// the same without the launch-shape autotuner's timing runs (no host
+// synchronisation): the shape pinned or remembered for the operator's catalog
+// shape, else the default
+void op_apply_orbit_untuned(OpImpl& op, const void* xs, double* ypad, cudaStream_t s);
 // the mixed-precision matvec streamed from the hop table with a complex64
 // output; false (nothing launched) when the operator has no hop table
 bool op_apply_orbit_cf(OpImpl& op, const void* xs, float2* y, cudaStream_t s);
@@ -242,6 +260,28 @@ static constexpr int64_t kDenseMaxDim = 500;
 // bound |r|^2 / gap is below this fraction of |E| (one tenth of the 1e-9
 // relative accuracy the mixed path promises).
 static constexpr double kMixedRelTarget = 1e-10;
+
+// The acceptance test of one pair (value lam, squared FP64 residual r2) of a
+// mixed-precision Rayleigh-Ritz block.  The Rayleigh-Ritz step removes the
+// coupling between the block's own vectors, so the quadratic bound
+// |dE| <= r^2 / gap needs the distance from lam to the eigenvalues outside
+// the block: gap = thL - lam, thL the lower end theta_L - r_L of the first
+// Lanczos Ritz interval above the block (an eigenvalue lies within r_L of
+// theta_L; theta_L alone would overestimate the gap, since Ritz values bound
+// eigenvalues from above).  The pair must also be isolated, gap > 2 r, for the
+// bound to apply.  A pair whose FP64 residual meets tol is accepted outright.
+// Levels the complex64 run has not separated into distinct Ritz values -- a
+// cluster narrower than its residuals, about 1e-6 |E| -- are invisible to any
+// residual-based test; wider clusters fail the test until the Lanczos
+// resolves them, or the run stagnates and the pair is solved in FP64.
+__host__ __device__ inline bool mixed_pair_accepted(double lam, double r2, double thL, double tol, double scale) {
+  const double r = sqrt(r2);
+  if (r <= tol) return true;
+  const double gap = thL - lam;
+  const double e = lam < 0 ? -lam : lam;
+  const double floor_e = 1e-6 * scale;
+  return gap > 2.0 * r && r2 <= kMixedRelTarget * (e > floor_e ? e : floor_e) * gap;
+}
 // Mixed precision reorthogonalises selectively: the full pass's dot products
 // are always taken (FP64-class), and the update is applied only when the
 // largest of them exceeds this fraction of |w|.  Between updates the basis
@@ -255,7 +295,27 @@ static constexpr double kSelReorth = 1e-7;
 void eigh_real_sym(int n, std::vector<double>& A, std::vector<double>& w, std::vector<double>& Z);
 void eigh_complex_herm(int n, const std::vector<double>& Hreim, std::vector<double>& w, std::vector<double>& Zreim);
 
-int device_sm_count();
+// Per-device facts.  A process may drive several GPUs (one host thread each):
+// the SM count and every kernel's shared-memory opt-in are properties of the
+// current device, so both are kept per device ordinal.
+static constexpr int kMaxDevices = 64;
+int current_device();  // cudaGetDevice, checked against kMaxDevices
+int device_sm_count(); // SM count of the current device
+// One kernel's dynamic shared-memory opt-in on every device.  ensure() raises
+// it to at least `bytes` on the current device and never lowers it; callers
+// hold their own lock from ensure() through the launch, so a concurrent caller
+// with a smaller footprint cannot undercut a launch in progress.
+struct SmemOptIn {
+  size_t bytes[kMaxDevices] = {};
+  template <class K>
+  void ensure(K* kern, size_t need) {
+    size_t& cfg = bytes[current_device()];
+    if (need > cfg) {
+      SED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+      cfg = need;
+    }
+  }
+};
 int grid1(int64_t work, int block);
 void compute_diag(int64_t n_orb, const uint64_t* reps, const uint8_t* rowflag, int n_den, const int32_t* den_ij,
                   const double2* den_v, double2* diag, cudaStream_t s);

@@ -908,9 +908,10 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
       // FP64 matvecs over its nev + 2 Ritz vectors B = V[0..nw).  Accepted
       // when every requested pair meets the residual tolerance or the
       // quadratic eigenvalue bound |dE| <= |r|^2 / gap is below
-      // kMixedRelTarget |E|, the gap measured to the first Lanczos Ritz value
-      // outside the block; otherwise the Lanczos resumes with a tighter
-      // threshold, and only a stagnated complex64 run falls back to FP64.
+      // kMixedRelTarget |E|, the gap measured to the lower end of the first
+      // Lanczos Ritz interval outside the block; otherwise the Lanczos
+      // resumes with a tighter threshold, and only a stagnated complex64 run
+      // falls back to FP64.
       const int nw = std::min(nev, msz);
       double2* HB = R;
       double2* Yr = R + (size_t)nw * ld;
@@ -970,14 +971,20 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
       }
       ops.check();
       SED_CUDA(cudaStreamSynchronize(s));
-      const double thL = msz > nw ? theta[nw] : HUGE_VAL;
+      // every requested pair must pass mixed_pair_accepted: isolated, and the
+      // quadratic bound with the gap to the lower end theta_L - r_L of the
+      // first Lanczos Ritz interval above the block (an eigenvalue lies within
+      // its Lanczos residual r_L of theta_L).  The bound holds as long as the
+      // Krylov space has not missed an eigenvalue between the block and
+      // theta_L, which the two spare pairs guard.
+      const double rL = (msz > nw && !invariant) ? std::fabs(beta * Z[(size_t)(msz - 1) * msz + nw]) : 0.0;
+      const double thL = msz > nw ? theta[nw] - rL : HUGE_VAL;
       bool ok = true;
       double maxr64 = 0.0, maxd = 0.0;
       for (int i = 0; i < nev_out; ++i) {
-        const double r = std::sqrt(ops.host[i]), gap = thL - lam[i];
-        maxr64 = std::max(maxr64, r);
+        maxr64 = std::max(maxr64, std::sqrt(ops.host[i]));
         maxd = std::max(maxd, std::fabs(lam[i] - theta[i]));
-        ok = ok && (r <= tol || (gap > 0.0 && r * r <= kMixedRelTarget * std::max(std::fabs(lam[i]), 1e-6 * scale) * gap));
+        ok = ok && mixed_pair_accepted(lam[i], ops.host[i], thL, tol, scale);
       }
       if (ok) {
         res.converged = nev_out;

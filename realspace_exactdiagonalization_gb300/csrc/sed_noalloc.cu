@@ -19,6 +19,10 @@
 //   * the first call on a device resolves the array's device address with
 //     cudaGetSymbolAddress (which may load the module); make that first call
 //     before any stream capture;
+//   * the call never runs the gather's launch-shape autotuner (whose timing
+//     runs wait on the host): it uses the operator's shape if one is chosen
+//     or pinned, else the shape remembered for the same catalog shape, else
+//     the default of one thread per row and 512 threads per block;
 //   * every call shares the one array: calls that overlap on the GPU (two
 //     streams, two threads, two operators) race and must be serialised by the
 //     caller.  Each call clears what it needs to start at zero, so a call
@@ -26,6 +30,7 @@
 #include <mutex>
 
 #include "../../include/sed_capi.h"
+#include "sed_handles.cuh"
 #include "sed_internal.cuh"
 
 namespace sed {
@@ -74,15 +79,11 @@ void op_apply_noalloc(OpImpl& op, const double* x, double* y, int64_t n) {
   cudaStream_t s = op.stream;
   expand_vec(S, x, pad, s);  // zeroes the n_orb entries, then scatters x
   op_scale_to_xs(op, pad, xs, s);
-  op_apply_orbit(op, xs, pad, s);
+  op_apply_orbit_untuned(op, xs, pad, s);
   compress_vec(S, pad, y, s);
 }
 
 }  // namespace sed
-
-struct sed_op {
-  std::shared_ptr<sed::OpImpl> p;
-};
 
 extern "C" int sed_op_apply_noalloc(sed_op* op, const double* x_dev, double* y_dev, int64_t n) {
   try {

@@ -293,18 +293,14 @@ bool op_build_table(OpImpl& op) {
   const FillSmem L = fill_layout(C.rank.rp.total, n_terms, n_mask, G.n_site);
   auto fill = G.stats == 1 ? k_optab_fill<true> : k_optab_fill<false>;
   {
-    // the shared-memory opt-in is a property of the kernel, shared by every
-    // operator and host thread: raise it (never lower it) and launch under
-    // one lock, so a concurrent build with a smaller rank table cannot
-    // undercut this launch
+    // the shared-memory opt-in is a property of the kernel on each device,
+    // shared by every operator and host thread: raise it (never lower it) and
+    // launch under one lock, so a concurrent build with a smaller rank table
+    // cannot undercut this launch
     static std::mutex mu;
-    static size_t configured[2] = {0, 0};
+    static SmemOptIn optin[2];
     std::lock_guard<std::mutex> lock(mu);
-    size_t& cfg = configured[G.stats == 1 ? 1 : 0];
-    if (L.total > cfg) {
-      SED_CUDA(cudaFuncSetAttribute(fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
-      cfg = L.total;
-    }
+    optin[G.stats == 1 ? 1 : 0].ensure(fill, L.total);
     int per_sm = 1;
     SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill, 512, L.total));
     const int fgrid = (int)std::max<int64_t>(

@@ -214,6 +214,10 @@ class ModelSpec:
     statistics: str  # "bosonic" | "fermionic"
     density_terms: List[Tuple[int, int, complex]]
     n_filled: int
+    # (n_split, n_lo, n_hi): two separately conserved species, n_lo particles
+    # on the first n_split modes and n_hi on the rest (None: only the total
+    # particle number is fixed, as in the reference)
+    species: Tuple[int, int, int] | None = None
 
     def bilinear_terms(self, theta: Sequence[float] = (0.0, 0.0)) -> List[Tuple[int, int, complex]]:
         return generate_bilinear_terms(self.tb, theta)
@@ -304,12 +308,14 @@ def checkerboard(L1: int, L2: int, t: float = 1.0, tp1: float = 0.3, tp2: float 
 
 
 def hubbard_square(L1: int, L2: int, t: float = 1.0, U: float = 8.0, n_filled: int | None = None,
-                   order: str = "sub_major") -> ModelSpec:
+                   order: str = "sub_major", n_up: int | None = None, n_dn: int | None = None) -> ModelSpec:
     """Spinful Fermi-Hubbard on an L1 x L2 square torus as 2*L1*L2 fermionic
     modes (sublattice 1 = up, 2 = down; reference benchmark/benchmark.jl:155-219).
     ``order="sub_major"`` puts the up spin of cell i at bit i and the down spin
     at bit i + L1*L2.  The particle number is fixed over all S^z, as in the
-    reference (its default is half filling, N = L1*L2)."""
+    reference (its default is half filling, N = L1*L2).  With ``n_up`` and
+    ``n_dn`` (sub_major order only) the model carries the two-species block
+    (N_up, N_down) instead: species = (L1*L2, n_up, n_dn)."""
     lat = initialize_real_space_lattice((L1, L2), 2, f"hubbard{L1}x{L2}", order=order)
     spinless = initialize_real_space_lattice((L1, L2), 1, "square")
     tb1 = TightBindingModel(spinless)
@@ -325,5 +331,14 @@ def hubbard_square(L1: int, L2: int, t: float = 1.0, U: float = 8.0, n_filled: i
     for y in range(L2):
         for x in range(L1):
             den.append((lat.site_to_index_map[((x, y), 1)], lat.site_to_index_map[((x, y), 2)], complex(U)))
+    if (n_up is None) != (n_dn is None):
+        raise ValueError("give both n_up and n_dn, or neither")
+    if n_up is not None:
+        if order != "sub_major":
+            raise ValueError("the (N_up, N_down) block needs the sub_major mode order")
+        if n_filled is not None and n_filled != n_up + n_dn:
+            raise ValueError("n_filled must equal n_up + n_dn")
+        return ModelSpec(f"hubbard{L1}x{L2}_{n_up}u{n_dn}d", lat, tb, "fermionic", den, n_up + n_dn,
+                         (L1 * L2, n_up, n_dn))
     nf = L1 * L2 if n_filled is None else n_filled
     return ModelSpec(f"hubbard{L1}x{L2}", lat, tb, "fermionic", den, nf)

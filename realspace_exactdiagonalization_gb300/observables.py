@@ -132,7 +132,7 @@ def flux_point_states(spec: L.ModelSpec, flux: Sequence[float], manifold_size: i
     flux = tuple(float(f) for f in flux)
     G = L.build_translation_group(spec.lattice, flux)
     if catalog is None:
-        catalog = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G,
+        catalog = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G,
                                                  particle_statistics=statistics_from_name(spec.statistics))
     terms = spec.bilinear_terms(flux)
     cands = []
@@ -184,7 +184,7 @@ def many_body_chern_number(spec: L.ModelSpec, manifold_size: int, flux_grid_size
     if manifold_size <= 0:
         raise ValueError("manifold_size must be positive.")
     G0 = L.build_translation_group(spec.lattice)
-    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G0,
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G0,
                                          particle_statistics=statistics_from_name(spec.statistics))
     fx = [ix / nx for ix in range(nx)]
     fy = [iy / ny for iy in range(ny)]
@@ -283,7 +283,7 @@ def flux_charge_pump(spec: L.ModelSpec, manifold_size: int, flux_direction: int 
     fluxes = list(twisted_phases_over_2pi_list) if twisted_phases_over_2pi_list is not None else \
         list(np.linspace(0.0, 1.0, 9))
     G0 = L.build_translation_group(lat)
-    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G0,
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G0,
                                          particle_statistics=statistics_from_name(spec.statistics))
     site_phases = many_body_position_phases(lat, polarization_direction, include_sublattice)
     gaps, min_sv, selected = [], [], []

@@ -92,11 +92,13 @@ class Request:
     error: str = ""  # the library's message when status != 0
 
 
-def config5_families() -> Dict[str, L.ModelSpec]:
+def config5_families(hubbard_blocks: bool = True) -> Dict[str, L.ModelSpec]:
     """The served mix: hard-core boson rings (t=1, V=2) at half filling, checkerboard
     fermions at 1/3 lower-band filling (4x4: Np=5, since 16/3 is not an integer),
-    and spinful Hubbard (t=1, U=8) with N_up = N_down = 5 or 6 as the reference
-    encodes it: a fixed total particle number over 2 L1 L2 modes."""
+    and spinful Hubbard (t=1, U=8) with N_up = N_down = 5 or 6: by default in its
+    (N_up, N_down) block (a two-species catalog); with hubbard_blocks=False as
+    the reference encodes it, a fixed total particle number 2 N_up over all
+    S^z."""
     fam = {}
     for n in (20, 24, 28):
         fam[f"ring{n}"] = L.ring_xxz(n, 1.0, 2.0)
@@ -104,7 +106,8 @@ def config5_families() -> Dict[str, L.ModelSpec]:
     fam["checkerboard4x4"] = L.checkerboard(4, 4, n_filled=5)
     for (l1, l2) in ((3, 4), (4, 4)):
         for nh in (5, 6):
-            fam[f"hubbard{l1}x{l2}_{nh}+{nh}"] = L.hubbard_square(l1, l2, n_filled=2 * nh)
+            fam[f"hubbard{l1}x{l2}_{nh}+{nh}"] = (L.hubbard_square(l1, l2, n_up=nh, n_dn=nh) if hubbard_blocks
+                                                  else L.hubbard_square(l1, l2, n_filled=2 * nh))
     return fam
 
 
@@ -154,7 +157,7 @@ class SectorServer:
         self.resident = 0
         for name, spec in families.items():
             G = L.build_translation_group(spec.lattice)
-            cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G,
+            cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G,
                                                  particle_statistics=statistics_from_name(spec.statistics))
             pairs = [(i, j) for (i, j, _) in spec.bilinear_terms()]
             if cat.n_orbits <= small_max_orbits:

@@ -112,3 +112,70 @@ def assert_lanczos_spectrum(vals, ref, tol, msg=""):
     assert sorted(set(got)) == list(range(len(set(got)))), (msg, got)
     for i in set(got):
         assert got.count(i) <= mult[i], (msg, got, mult[:6])
+
+
+def _cycles(perm0_row):
+    seen, cycles = set(), []
+    for s in range(len(perm0_row)):
+        if s in seen:
+            continue
+        c, t = [], s
+        while t not in seen:
+            seen.add(t)
+            c.append(t)
+            t = int(perm0_row[t])
+        cycles.append(c)
+    return cycles
+
+
+def fixed_masks(perm0_row, n_filled, species=None):
+    """Masks with the catalog's particle numbers that the permutation maps to
+    themselves: unions of whole cycles (each cycle stays inside one species
+    when the group preserves the species)."""
+    cycles = _cycles(perm0_row)
+    if species:
+        n_split, n_lo, n_hi = species
+        want = (n_lo, n_hi)
+        weight = [(len(c) if c[0] < n_split else 0, len(c) if c[0] >= n_split else 0) for c in cycles]
+    else:
+        want = (n_filled, 0)
+        weight = [(len(c), 0) for c in cycles]
+    out = []
+
+    def rec(i, a, b, m):
+        if a == want[0] and b == want[1]:
+            out.append(m)
+            return
+        if i == len(cycles) or a > want[0] or b > want[1]:
+            return
+        rec(i + 1, a, b, m)
+        bits = 0
+        for s in cycles[i]:
+            bits |= 1 << s
+        rec(i + 1, a + weight[i][0], b + weight[i][1], m | bits)
+
+    rec(0, 0, 0, 0)
+    return out
+
+
+def character_dimension(oracle, group, stats_code, chi, n_filled, species=None, n_states=None):
+    """Sector dimension from the trace of the projector onto the irrep chi,
+    (1/|G|) sum_g conj(chi(g)) sum_{m : g(m) = m} alpha_g(m), over the fixed
+    masks of each element only: a check of the sector basis (one row per
+    compatible orbit, SRE:534-556) that needs no enumeration of the basis.  The
+    identity's trace is the number of basis states, ``n_states``."""
+    perm0, phases = group.perm0(), group.phases()
+    tot = 0j
+    for g in range(len(perm0)):
+        if g == group.identity_idx - 1:
+            tr = complex(n_states)
+        else:
+            tr = 0j
+            for m in fixed_masks(perm0[g], n_filled, species):
+                img, a = oracle.apply_op(perm0[g], phases[g], stats_code, m)
+                assert img == m
+                tr += a
+        tot += np.conj(chi[g]) * tr
+    d = tot / len(perm0)
+    assert abs(d.imag) < 1e-6 and abs(d.real - round(d.real)) < 1e-6, d
+    return int(round(d.real))

@@ -1,7 +1,7 @@
 """Extract the reference's stored known answers into reference_golden.json.
 
-Reads (from a checkout of RealSpace_ExactDiagonalization, default
-/root/reference):
+Reads (from a checkout of RealSpace_ExactDiagonalization, given as the first
+argument or in the environment variable SED_REFERENCE_ROOT):
   * benchmark/benchmark_data/benchmark_raw.csv -- per (model, size, mode):
     n_site, n_filled, full_dim, n_orbits, |G|, sector_dim and the ground
     energy of the k=(0,0) sector;
@@ -9,7 +9,7 @@ Reads (from a checkout of RealSpace_ExactDiagonalization, default
     LinTable / rank agreement over C(12,3), and the Haldane 2x3 counts
     (orbits, full basis, sector dim, nnz(H), projection-table entries).
 The JSON is committed; tests read only the JSON.  Re-run with
-``python tests/golden/make_golden.py [reference_root]``.
+``python tests/golden/make_golden.py <reference_root>``.
 """
 import csv
 import json
@@ -17,7 +17,9 @@ import os
 import re
 import sys
 
-ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SED_REFERENCE_ROOT", "")
+if not ROOT:
+    sys.exit("usage: make_golden.py <reference_root> (or set SED_REFERENCE_ROOT)")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_golden.json")
 
 

@@ -17,7 +17,7 @@ def _solver(spec, precision, nev=4, max_requests=256):
     from realspace_exactdiagonalization_gb300.groups import statistics_from_name
 
     G = L.build_translation_group(spec.lattice)
-    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G,
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G,
                                          particle_statistics=statistics_from_name(spec.statistics))
     pairs = [(i, j) for (i, j, _) in spec.bilinear_terms()]
     return BatchedSectorSolver(cat, pairs, spec.density_terms, precision=precision, nev=nev,

@@ -14,7 +14,7 @@ def _device_basis(case, k):
     import realspace_exactdiagonalization_gb300.api as A
     from realspace_exactdiagonalization_gb300.groups import statistics_from_name
 
-    cat = A.build_symmetry_orbit_catalog(n_filled=case.spec.n_filled, symmetry_group=case.group(),
+    cat = A.build_symmetry_orbit_catalog(n_filled=case.spec.n_filled, species=case.spec.species, symmetry_group=case.group(),
                                          particle_statistics=statistics_from_name(case.statistics))
     return A.build_symmetry_sector_basis(cat, case.irreps()[k])
 

@@ -20,7 +20,7 @@ def _device_sector(case: Case, sector: int, catalog=None):
 
     G = case.group()
     if catalog is None:
-        catalog = A.build_symmetry_orbit_catalog(n_filled=case.spec.n_filled, symmetry_group=G,
+        catalog = A.build_symmetry_orbit_catalog(n_filled=case.spec.n_filled, species=case.spec.species, symmetry_group=G,
                                                  particle_statistics=statistics_from_name(case.statistics))
     return catalog, A.build_symmetry_sector_basis(catalog, case.irreps()[sector], group=G)
 

@@ -21,7 +21,7 @@ def _device(case, sector=None, precision="fp64"):
 
     st = statistics_from_name(case.statistics)
     G = case.group()
-    cat = A.build_symmetry_orbit_catalog(n_filled=case.spec.n_filled, symmetry_group=G, particle_statistics=st)
+    cat = A.build_symmetry_orbit_catalog(n_filled=case.spec.n_filled, species=case.spec.species, symmetry_group=G, particle_statistics=st)
     if sector is None:
         return cat
     basis = A.build_symmetry_sector_basis(cat, case.irreps()[sector])
@@ -144,6 +144,27 @@ def test_eigenvalues_match_dense(oracle, name):
                 assert np.linalg.norm(r) < bound * max(1.0, abs(vals[i])), (name, k, precision, i)
 
 
+def test_ring16_k0_lowest_four_eigenvalues_within_1e12(oracle):
+    """Plain method on the 16-site ring of hard-core bosons (t = 1, V = 2,
+    8 particles, k = 0, 810 representatives): the sector and its tables are
+    bit-exact (test_catalog_tables_bit_exact, test_sector_bases_bit_exact), and
+    the FP64 device Lanczos (810 > 500 rows, so not the dense branch) gives the
+    lowest four eigenvalues within 1e-12 (absolute) of a dense diagonalisation
+    of the oracle's matrix-mode block, from a seeded Gaussian start vector.
+    These four levels are non-degenerate, so the Lanczos and the reference's
+    matrix mode list the same values."""
+    case = case_by_name("ring16")
+    _, _, op = oracle_objects(oracle, case, 0)
+    assert op.dim == 810
+    ref = np.linalg.eigvalsh(op.dense())
+    assert np.min(np.diff(ref[:5])) > 1e-3  # no degenerate copies among them
+    for seed in (0, 1, 12345):
+        _, _, H = _device(case, 0, "fp64")
+        vals, vecs, info = H.solve(4, tol=1e-10, seed=seed)
+        assert np.abs(vals - ref[:4]).max() <= 1e-12, (seed, vals - ref[:4])
+        assert info.n_restarts >= 0 and info.converged == 4
+
+
 def test_lanczos_odd_orbit_count(oracle):
     """A catalog with an odd orbit count: a ring of 16 sites with 7 particles
     at a twist, 715 orbits, every sector above the dense branch's 500 rows.
@@ -263,7 +284,7 @@ def test_flux_refresh_matches_fresh_build(oracle):
 
     G0 = L.build_translation_group(spec.lattice, (0.0, 0.0))
     Gt = case.group()
-    dc = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G0, particle_statistics=st)
+    dc = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G0, particle_statistics=st)
     A.update_orbit_stabilizer_phases_(dc, Gt, st)
     oc = oracle.Catalog(G0.perm0(), G0.phases(), 0, case.stats_code, spec.n_filled)
     oc.update_phases(Gt.phases())

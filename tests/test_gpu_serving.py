@@ -61,7 +61,7 @@ def test_op_priority_keeps_results():
 
     spec = L.ring_xxz(16, 1.0, 2.0)
     G = L.build_translation_group(spec.lattice, (0.2, 0.0))
-    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G,
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G,
                                          particle_statistics=A.Bosonic())
     basis = A.build_symmetry_sector_basis(cat, L.build_translation_irrep_list(G, spec.lattice)[3], group=G)
     H = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms((0.2, 0.0)), spec.density_terms, precision="mixed")
