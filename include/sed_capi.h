@@ -332,6 +332,17 @@ int sed_batch_set_x_in_shared_memory(sed_batch* b, int enable);
  * more than four distinct values per group element, or whose sectors leave no
  * shared memory for its coefficient tables, use the on-the-fly matvec. */
 int sed_batch_set_hop_table(sed_batch* b, int enable);
+/* Site gauge (on by default; no counterpart in the reference).  When every
+ * request of a run has a site gauge w -- per-site phases under which its
+ * group's phases all become 1, as the flux-twisted translation groups of
+ * build_translation_group (SRE:1374-1405) do with w_j = exp(2 pi i theta .
+ * r_j / L) -- the run solves W H W^-1 (the twist spread evenly over the
+ * bonds; same sector, same eigenvalues): the hop table then carries only the
+ * sign of each hop and a matvec gathers one coefficient per hop instead of
+ * two.  Otherwise the run uses phase-class records.  sed_batch_last_gauge
+ * reports which the last run used. */
+int sed_batch_set_site_gauge(sed_batch* b, int enable);
+int sed_batch_last_gauge(const sed_batch* b, int32_t* gauge);
 /* Same solve with every buffer in device memory (inputs resident in HBM),
  * queued on the batch stream.  Device arrays have the layouts of
  * sed_batch_run; outputs may not be NULL.  SED_PREC_FP64 returns without

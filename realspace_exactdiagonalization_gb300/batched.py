@@ -117,14 +117,22 @@ class BatchedSectorSolver:
         check(_lib.load().sed_batch_last_info(self._h, C.byref(nf), C.byref(tab), C.byref(nrec)))
         caps, reps = C.c_int32(0), C.c_int32(0)
         check(_lib.load().sed_batch_graph_info(self._h, C.byref(caps), C.byref(reps)))
+        gauge = C.c_int32(0)
+        check(_lib.load().sed_batch_last_gauge(self._h, C.byref(gauge)))
         return {"hops": hops, "t_start_ns": t0, "t_end_ns": t1, "fp64_fallbacks": int(nf.value),
-                "hop_table": bool(tab.value), "hop_records": int(nrec.value),
+                "hop_table": bool(tab.value), "hop_records": int(nrec.value), "site_gauge": bool(gauge.value),
                 "graph_captures": int(caps.value), "graph_replays": int(reps.value)}
 
     def set_x_in_shared_memory(self, enable: bool) -> None:
         """Keep the complex64 matvec input in shared memory (default when it
         fits) or in global memory (the layout of sectors too large for it)."""
         check(_lib.load().sed_batch_set_x_in_shared_memory(self._h, int(bool(enable))))
+
+    def set_site_gauge(self, enable: bool) -> None:
+        """Solve runs whose requests all have a site gauge (the flux-twisted
+        translation groups do) in that gauge, with sign-only hop records
+        (default), or always with phase-class records."""
+        check(_lib.load().sed_batch_set_site_gauge(self._h, int(bool(enable))))
 
     def set_hop_table(self, enable: bool) -> None:
         """Stream the shared hop table (default) or derive every hop on the fly."""

@@ -66,6 +66,12 @@ struct BatchArgs {
   // hop table (use_tab != 0): SELL-32 records, per-slice offsets / widths,
   // phase-id descriptors and each group element's class representative sites
   int use_tab, n_phi, phi_cap;
+  // gauge mode (use_tab != 0): every request's group phases become exactly 1
+  // under its site gauge gauge_w[b][site], so a hop's coefficient is one
+  // table entry times the sign its record carries (phase id 0: +, 1: -)
+  int gauge;
+  const double2* gauge_w;  // [n_req][N]
+  const int32_t* bil_dev;  // [n_bil][2] (from, to) sites of the bilinear terms
   const uint64_t* hop;
   const uint32_t* sl_off;
   const int32_t* sl_w;
@@ -96,8 +102,8 @@ static BatchSmem batch_layout(const BatchArgs& a, bool x_in_smem) {
   auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
   L.x = o;
   o = al(o + (x_in_smem ? (size_t)a.n_orb * sizeof(VT) : 0));
-  L.tchi = o;
-  o = al(o + (size_t)a.n_bil * a.G * sizeof(VT));
+  L.tchi = o;  // n_bil * G coefficients and a zero entry for padding records
+  o = al(o + ((size_t)a.n_bil * a.G + 1) * sizeof(VT));
   L.eta = o;
   o = al(o + (size_t)a.G * a.N * sizeof(VT));
   L.chi64 = o;
@@ -603,6 +609,54 @@ __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typen
       const V ph = pwc[(uint32_t)(r >> 42)];
       const V xc = x[(uint32_t)r & 0xFFFFFFu];
       const S cr = P::mad(t.x, ph.x, -t.y * ph.y), ci = P::mad(t.x, ph.y, t.y * ph.x);
+      ar = P::mad(cr, xc.x, ar);
+      ar = P::mad(-ci, xc.y, ar);
+      ai = P::mad(cr, xc.y, ai);
+      ai = P::mad(ci, xc.x, ai);
+    }
+    if (!rowflag[o]) {
+      zero_row(w, o);
+      continue;
+    }
+    const S is = sizeof(S) == 4 ? (S)s_isrf[a.stab[o]] : (S)s_isr[a.stab[o]];
+    store_row(w, o, ar * is, ai * is);
+  }
+}
+
+// sign of v flipped when bit 31 of f is set
+__device__ __forceinline__ float flip_sign(float v, uint32_t f) { return __uint_as_float(__float_as_uint(v) ^ f); }
+__device__ __forceinline__ double flip_sign(double v, uint32_t f) {
+  return __longlong_as_double(__double_as_longlong(v) ^ ((unsigned long long)f << 32));
+}
+
+// The hop-table matvec in gauge mode: the record's phase id is only the sign
+// of the hop (0: +, 1: -; padding records point at the zero coefficient), so
+// a hop costs the record load, one coefficient gather and the x gather --
+// one shared-memory gather fewer than block_matvec_tab, whose random gathers
+// (with their bank conflicts) bound the matvec on the L1 data pipe.
+template <class P, class WT>
+__device__ __forceinline__ void block_matvec_tab_gauge(const BatchArgs& a, const typename P::V* x,
+                                                       const typename P::V* tchi, const double* s_isr,
+                                                       const float* s_isrf, const uint8_t* __restrict__ rowflag,
+                                                       WT* __restrict__ w) {
+  using V = typename P::V;
+  using S = typename P::S;
+  const int lane = threadIdx.x & 31;
+  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
+    const int64_t sl = o >> 5;
+    const uint64_t* rp = a.hop + a.sl_off[sl] + lane;
+    const int wdt = a.sl_w[sl];
+    const double2 dg = a.diag[o];
+    const V xo = x[o];
+    S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
+    S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
+#pragma unroll 8
+    for (int k = 0; k < wdt; ++k) {
+      const uint64_t r = __ldg(rp + 32 * k);
+      const V t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
+      const V xc = x[(uint32_t)r & 0xFFFFFFu];
+      const uint32_t f = ((uint32_t)(r >> 42) & 1u) << 31;
+      const S cr = flip_sign(t.x, f), ci = flip_sign(t.y, f);
       ar = P::mad(cr, xc.x, ar);
       ar = P::mad(-ci, xc.y, ar);
       ai = P::mad(cr, xc.y, ai);
@@ -1474,7 +1528,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
   BV* Rb = reinterpret_cast<BV*>(a.R + (size_t)blockIdx.x * slots * a.ld);
   BV* W = reinterpret_cast<BV*>(a.W + (size_t)blockIdx.x * a.ld);
   double2* X64 = a.X64 + (size_t)blockIdx.x * a.ld;
-  double2* tchi64 = a.tchi64 + (size_t)blockIdx.x * a.n_bil * a.G;
+  double2* tchi64 = a.tchi64 + (size_t)blockIdx.x * ((size_t)a.n_bil * a.G + 1);
   uint8_t* rowflag = a.rowflag + (size_t)blockIdx.x * a.ld;
   double2* pwc64 = a.pwc64 ? a.pwc64 + (size_t)blockIdx.x * a.phi_cap : nullptr;
   V* x = X_SMEM ? s_x : reinterpret_cast<V*>(X64);
@@ -1552,7 +1606,17 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       }
     }
     __syncthreads();
-    if (a.use_tab) {
+    if (a.use_tab && a.gauge) {
+      // gauge mode: no per-site phase product (base 1); phase ids 0 and 1
+      // are the signs +1 and -1, entry 2 the zero of the padding records
+      for (int h = threadIdx.x; h < a.G; h += blockDim.x) s_basek[h] = make_double2(1.0, 0.0);
+      for (int f = threadIdx.x; f <= 2; f += blockDim.x) {
+        const double p = f == 0 ? 1.0 : (f == 1 ? -1.0 : 0.0);
+        reinterpret_cast<float4*>(pwc64)[f] = make_float4((float)p, 0.f, 0.f, 0.f);
+        s_pwc[f].x = p;
+        s_pwc[f].y = 0.0;
+      }
+    } else if (a.use_tab) {
       // family phase classes of the hop table: this request's phase on each
       // class (read at the class's first site; constant on the class by
       // construction), P_h(new) = v0^k prod_c (v_c / v0)^(n_c)
@@ -1605,11 +1669,21 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
     if (pmode == 2 && !a.use_tab)
       for (int h = threadIdx.x; h < a.G; h += blockDim.x) s_basek[h] = make_double2(1.0, 0.0);
     __syncthreads();
-    for (int i = threadIdx.x; i < a.n_bil * a.G; i += blockDim.x) {
+    const double2* gw = (a.use_tab && a.gauge) ? a.gauge_w + (size_t)b * a.N : nullptr;
+    for (int i = threadIdx.x; i <= a.n_bil * a.G; i += blockDim.x) {
       const int k = i / a.G, h = i % a.G;
-      const double2 t = amp[k], c0 = chi[h], bk = s_basek[h];
-      const double2 c = make_double2(c0.x * bk.x + c0.y * bk.y, c0.y * bk.x - c0.x * bk.y);  // chi conj(base^k)
-      const double2 v = make_double2(t.x * c.x + t.y * c.y, t.x * c.y - t.y * c.x);          // conj(t) chi'
+      double2 v = make_double2(0.0, 0.0);  // entry n_bil * G: the padding records' zero
+      if (i < a.n_bil * a.G) {
+        double2 t = amp[k];
+        if (gw) {  // the hop i -> j in the site gauge: t w_j conj(w_i)
+          const double2 wi = gw[a.bil_dev[2 * k]], wj = gw[a.bil_dev[2 * k + 1]];
+          const double2 q = make_double2(wj.x * wi.x + wj.y * wi.y, wj.y * wi.x - wj.x * wi.y);
+          t = make_double2(t.x * q.x - t.y * q.y, t.x * q.y + t.y * q.x);
+        }
+        const double2 c0 = chi[h], bk = s_basek[h];
+        const double2 c = make_double2(c0.x * bk.x + c0.y * bk.y, c0.y * bk.x - c0.x * bk.y);  // chi conj(base^k)
+        v = make_double2(t.x * c.x + t.y * c.y, t.x * c.y - t.y * c.x);                       // conj(t) chi'
+      }
       if (a.use_tab) {  // double-float pairs for the table-path polish
         float4 vd;
         d_to_df(v.x, vd.x, vd.z);
@@ -1696,7 +1770,9 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       int jend = m;
       for (int j = k; j < m; ++j) {
         BV* vj = Vb + (size_t)j * a.ld;
-        if (a.use_tab)
+        if (a.use_tab && a.gauge)
+          block_matvec_tab_gauge<P>(a, x, s_tchi, s_isr, s_isrf, rowflag, W);
+        else if (a.use_tab)
           block_matvec_tab<P>(a, x, s_tchi, s_pwc, s_isr, s_isrf, rowflag, W);
         else
           block_matvec<P, FERMI, PHASES>(a, x, s_tchi, s_eta, s_isr, s_isrf, s_rank, s_rec, s_off, s_inv, rowflag, W,
@@ -2039,6 +2115,11 @@ struct BatchImpl {
   std::vector<int32_t> row_cnt;     // hops per orbit row
   DevBuf hop, sl_off, sl_w, phi_desc, rep_site, pwc64, fmask_dev;
   int64_t hop_records = 0;
+  // the table's records carry signs only (gauge mode) rather than phase ids
+  bool tab_gauge = false;
+  bool gauge_enabled = true;  // use gauge mode whenever every request allows it
+  int last_gauge = 0;
+  DevBuf gauge_w, bil_dev;  // [max_req][n_site] site gauges; [n_bil][2] term sites
   int last_tab = 0;
   bool tab_enabled = true;
   // complex64 matvec input in shared memory (else in global memory, for
@@ -2138,6 +2219,7 @@ static BatchArgs base_args(BatchImpl& B) {
   a.atol = 1e-12;
   a.kp1 = C.n_filled + 1;
   a.phi_cap = B.phi_cap;
+  a.bil_dev = B.bil_dev.as<int32_t>();
   return a;
 }
 
@@ -2344,22 +2426,88 @@ static bool family_classes(const GroupImpl& G, int n_req, const double* phase, c
   return true;
 }
 
-// Make the hop table match this run's phase classes; returns whether the run
-// can use it.  phase is the host copy of the requests' group phases.
-static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStream_t s) {
+// A site gauge w_j = e^{i phi_j} for each request, under which its group
+// phases become exactly 1: eta_g(j) w_{perm_g(j)} conj(w_j) = 1 for every g and
+// site j.  The flux-twisted translation groups of build_translation_group
+// (SRE:1374-1405) have one, w_j = exp(2 pi i theta . r_j / L): the twist then
+// spreads evenly over the bonds, and U_g' = W U_g W^-1 is the plain
+// permutation.  A breadth-first walk from one site per site orbit fixes w;
+// every (g, j) is then checked to 1e-10.  Under the gauge the sector matrix
+// becomes D H D^-1, D diagonal and unitary on the same orbits (the membership
+// test still uses the request's own phases), so eigenvalues are unchanged; a
+// hop (i -> j, t) carries t w_j conj(w_i) and no per-site phase product.
+// False (nothing usable) when some request has no such gauge.
+static bool site_gauges(const GroupImpl& G, int n_req, const double* phase, std::vector<double>& w) {
+  const int N = G.n_site, nG = G.n_ops;
+  w.assign((size_t)n_req * N * 2, 0.0);
+  std::vector<char> seen(N);
+  std::vector<int> fifo(N);
+  for (int b = 0; b < n_req; ++b) {
+    const double* ph = phase + (size_t)b * nG * N * 2;
+    double* wb = w.data() + (size_t)b * N * 2;
+    std::fill(seen.begin(), seen.end(), 0);
+    for (int root = 0; root < N; ++root) {
+      if (seen[root]) continue;
+      seen[root] = 1;
+      wb[2 * root] = 1.0;
+      wb[2 * root + 1] = 0.0;
+      int head = 0, tail = 0;
+      fifo[tail++] = root;
+      while (head < tail) {
+        const int j = fifo[head++];
+        for (int g = 0; g < nG; ++g) {
+          const int q = G.perm[(size_t)g * N + j];
+          if (seen[q]) continue;
+          // w_q = w_j / eta_g(j)
+          const double er = ph[((size_t)g * N + j) * 2], ei = ph[((size_t)g * N + j) * 2 + 1];
+          const double n2 = er * er + ei * ei;
+          if (!(n2 > 0.0)) return false;
+          const double wr = wb[2 * j], wi = wb[2 * j + 1];
+          wb[2 * q] = (wr * er + wi * ei) / n2;
+          wb[2 * q + 1] = (wi * er - wr * ei) / n2;
+          seen[q] = 1;
+          fifo[tail++] = q;
+        }
+      }
+    }
+    for (int g = 0; g < nG; ++g)
+      for (int j = 0; j < N; ++j) {
+        const int q = G.perm[(size_t)g * N + j];
+        const double er = ph[((size_t)g * N + j) * 2], ei = ph[((size_t)g * N + j) * 2 + 1];
+        // eta * w_q * conj(w_j)
+        const double ar = wb[2 * q] * wb[2 * j] + wb[2 * q + 1] * wb[2 * j + 1];
+        const double ai = wb[2 * q + 1] * wb[2 * j] - wb[2 * q] * wb[2 * j + 1];
+        const double re = er * ar - ei * ai, im = er * ai + ei * ar;
+        if (std::hypot(re - 1.0, im) > 1e-10) return false;
+      }
+  }
+  return true;
+}
+
+// Make the hop table match this run: in gauge mode the records carry signs
+// only and serve every run; otherwise they carry phase ids of this run's phase
+// classes.  Returns whether the run can use the table.  phase is the host copy
+// of the requests' group phases.
+static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStream_t s, bool gauge) {
   if (B.phi_cap == 0 || !B.tab_enabled) return false;
   const CatalogImpl& C = *B.cat;
   const GroupImpl& G = *C.group;
   if (C.n_orbits >= (1 << 24) || (int64_t)B.n_bil * G.n_ops >= (1 << 18) || C.n_filled > 63) return false;
   std::vector<uint64_t> fmask;
   std::vector<int8_t> rep;
-  // refine the current table's partition; if that needs too many classes,
-  // partition this run alone
-  const std::vector<uint64_t> none;
-  if (!(B.tab_valid && family_classes(G, n_req, phase, B.tab_fmask, fmask, rep)) &&
-      !family_classes(G, n_req, phase, none, fmask, rep))
-    return false;
-  if (B.tab_valid && fmask == B.tab_fmask) {
+  if (gauge) {
+    if (B.tab_valid && B.tab_gauge) return true;
+    fmask.assign((size_t)G.n_ops * 3, 0);  // no class counts: the keys hold h and the sign
+    rep.assign((size_t)G.n_ops * 4, -1);
+  } else {
+    // refine the current table's partition; if that needs too many classes,
+    // partition this run alone
+    const std::vector<uint64_t> none;
+    if (!(B.tab_valid && !B.tab_gauge && family_classes(G, n_req, phase, B.tab_fmask, fmask, rep)) &&
+        !family_classes(G, n_req, phase, none, fmask, rep))
+      return false;
+  }
+  if (B.tab_valid && !B.tab_gauge && !gauge && fmask == B.tab_fmask) {
     if (rep != B.tab_rep) {
       B.tab_rep = rep;
       upload(B.rep_site, B.tab_rep, s);
@@ -2428,6 +2576,25 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
   // outside them
   std::unordered_map<uint32_t, uint32_t> id;
   std::vector<uint32_t> desc;
+  const uint64_t n_tchi = (uint64_t)B.n_bil * G.n_ops;
+  if (gauge) {
+    // phase id = the sign; padding: the zero coefficient (tchi entry n_tchi,
+    // phase id 2)
+    for (int64_t t = 0; t < tot; ++t) {
+      const bool pad = keys[t] == 0xFFFFFFFFu;
+      SED_REQUIRE(pad || ((recs[t] & 0xFFFFFFu) < (uint64_t)C.n_orbits && ((recs[t] >> 24) & 0x3FFFFu) < n_tchi &&
+                          (int)(keys[t] & 0x3F) < G.n_ops && (keys[t] >> 25) == 0),
+                  5, "internal error: hop-table record out of range");
+      recs[t] = pad ? (n_tchi << 24) | (2ULL << 42) : (recs[t] & ((1ULL << 42) - 1)) | ((uint64_t)(keys[t] >> 24) << 42);
+    }
+    SED_CUDA(cudaMemcpyAsync(B.hop.p, recs.data(), (size_t)tot * 8, cudaMemcpyHostToDevice, s));
+    SED_CUDA(cudaStreamSynchronize(s));
+    B.n_phi = 2;
+    B.tab_gauge = true;
+    B.tab_fmask.clear();
+    B.tab_valid = true;
+    return true;
+  }
   for (int64_t t = 0; t < tot; ++t) {
     if (keys[t] == 0xFFFFFFFFu) continue;
     auto it = id.find(keys[t]);
@@ -2443,7 +2610,6 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
     }
   }
   const uint64_t zero_id = desc.size();
-  const uint64_t n_tchi = (uint64_t)B.n_bil * G.n_ops;
   for (int64_t t = 0; t < tot; ++t) {
     const bool pad = keys[t] == 0xFFFFFFFFu;
     SED_REQUIRE(pad || ((recs[t] & 0xFFFFFFu) < (uint64_t)C.n_orbits && ((recs[t] >> 24) & 0x3FFFFu) < n_tchi), 5,
@@ -2454,6 +2620,7 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
   SED_CUDA(cudaMemcpyAsync(B.hop.p, recs.data(), (size_t)tot * 8, cudaMemcpyHostToDevice, s));
   upload(B.phi_desc, desc, s);
   B.n_phi = (int)desc.size();
+  B.tab_gauge = false;
   B.tab_fmask = fmask;
   B.tab_rep = rep;
   upload(B.rep_site, B.tab_rep, s);
@@ -2493,6 +2660,12 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
     by_site[i].push_back({j, k});
   }
   check_species_terms(C, n_bil, bil_ij);
+  {
+    std::vector<int32_t> bij(bil_ij, bil_ij + 2 * n_bil);
+    B->bil_dev.alloc((size_t)std::max(2 * n_bil, 1) * 4);
+    if (n_bil) SED_CUDA(cudaMemcpy(B->bil_dev.p, bij.data(), bij.size() * 4, cudaMemcpyHostToDevice));
+    B->gauge_w.alloc((size_t)max_req * G.n_site * 16);
+  }
   B->tt.site_off.assign(G.n_site + 1, 0);
   for (int i = 0; i < G.n_site; ++i) {
     B->tt.site_off[i] = (uint16_t)B->tt.rec.size();
@@ -2562,7 +2735,7 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   B->R.alloc((size_t)ncta * slots * B->ld * 16);
   B->W.alloc((size_t)ncta * B->ld * 16);
   B->X64.alloc((size_t)ncta * B->ld * 16);
-  B->tchi64.alloc((size_t)ncta * std::max(n_bil * G.n_ops, 1) * 16);
+  B->tchi64.alloc((size_t)ncta * (n_bil * G.n_ops + 1) * 16);
   B->rowflag.alloc((size_t)ncta * B->ld);
   if (B->phi_cap) B->pwc64.alloc((size_t)ncta * B->phi_cap * 16);
   B->in_chi.alloc((size_t)max_req * G.n_ops * 16);
@@ -2660,7 +2833,17 @@ void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const doubl
     SED_CUDA(cudaStreamSynchronize(s));
     phase_host = ph_h.data();
   }
-  a.use_tab = phase_host && prepare_table(B, n_req, phase_host, s) ? 1 : 0;
+  // gauge mode when every request has a site gauge (sign-only records)
+  std::vector<double> gw;
+  const bool gauge = phase_host && B.gauge_enabled && B.phi_cap > 0 && B.tab_enabled &&
+                     site_gauges(*B.cat->group, n_req, phase_host, gw);
+  a.use_tab = phase_host && prepare_table(B, n_req, phase_host, s, gauge) ? 1 : 0;
+  a.gauge = a.use_tab && gauge ? 1 : 0;
+  if (a.gauge) {
+    SED_CUDA(cudaMemcpyAsync(B.gauge_w.p, gw.data(), gw.size() * 8, cudaMemcpyHostToDevice, s));
+    a.gauge_w = B.gauge_w.as<double2>();
+  }
+  B.last_gauge = a.gauge;
   if (a.use_tab) {
     a.n_phi = B.n_phi;
     a.hop = B.hop.as<uint64_t>();
@@ -2802,6 +2985,18 @@ int sed_batch_last_info(const sed_batch* b, int32_t* n_fallback, int32_t* hop_ta
   });
 }
 
+int sed_batch_set_site_gauge(sed_batch* b, int enable) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    b->p->gauge_enabled = enable != 0;
+  });
+}
+int sed_batch_last_gauge(const sed_batch* b, int32_t* gauge) {
+  return bguard([&] {
+    SED_REQUIRE(b && gauge, 1, "NULL argument");
+    *gauge = b->p->last_gauge;
+  });
+}
 int sed_batch_set_hop_table(sed_batch* b, int enable) {
   return bguard([&] {
     SED_REQUIRE(b, 1, "NULL batch");

@@ -205,3 +205,34 @@ def test_batch_sector_too_large_for_shared_memory():
                                     spec.density_terms)
         ref, _, _ = H.solve(2, tol=1e-10, want_vectors=False)
         assert abs(out["evals"][b, 0] - ref[0]) <= 1e-9 * max(1.0, abs(ref[0])), (b, out["evals"][b], ref)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("model", ["haldane2x4", "checkerboard3x2_f"])
+def test_site_gauge_matches_phase_classes(model, precision):
+    """Flux-twisted translation groups have a site gauge, so flux-scan runs
+    take the sign-only hop table (site_gauge in last_stats).  The same run
+    with phase-class records (gauge off) solves the same sectors: eigenvalues
+    agree within the path's tolerance (1e-9 relative mixed, 1e-11 FP64)."""
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = {"haldane2x4": lambda: L.haldane_honeycomb(2, 4),
+            "checkerboard3x2_f": lambda: L.checkerboard(3, 2, n_filled=4)}[model]()
+    reqs = flux_scan_requests(spec, TWISTS)
+    solver = _solver(spec, precision)
+    on = solver.run(reqs)
+    st_on = solver.last_stats()
+    assert st_on["hop_table"] and st_on["site_gauge"]
+    solver.set_site_gauge(False)
+    off = solver.run(reqs)
+    st_off = solver.last_stats()
+    assert st_off["hop_table"] and not st_off["site_gauge"]
+    assert (on["status"] == 0).all() and (off["status"] == 0).all()
+    np.testing.assert_array_equal(on["dims"], off["dims"])
+    ok = ~np.isnan(off["evals"])
+    tol = 1e-9 if precision == "mixed" else 1e-11
+    np.testing.assert_allclose(on["evals"][ok], off["evals"][ok], rtol=tol, atol=1e-12)
+    solver.set_site_gauge(True)
+    again = solver.run(reqs)
+    assert solver.last_stats()["site_gauge"]
+    np.testing.assert_array_equal(again["evals"], on["evals"])
