@@ -80,8 +80,9 @@ def lanczos_bytes(nmv: int, dim: int, m: int = 24, keep: int = 8, n_polish: int 
 
 
 def profiled_traffic_per_sector():
-    """DRAM bytes (read + write) per sector of one k_batch launch, from the ncu
-    capture summarised in profiles/ (the capture scales with the sector count)."""
+    """DRAM bytes (read + write) per sector of one k_batch launch, read from the
+    committed ncu capture summary of the 192-sector case (the capture scales
+    with the sector count)."""
     path = os.path.join(ROOT, "profiles", "k_batch_flux_scan_haldane3x4.md")
     try:
         for line in open(path):
@@ -245,7 +246,7 @@ def run_ours(args, rank, world):
     spec, twists, reqs = workload_requests(args.twist_grid)
     n = len(reqs)
     G0 = reqs[0].group
-    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G0,
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G0,
                                          particle_statistics=A.Bosonic())
     pairs = [(i, j) for (i, j, _) in spec.bilinear_terms()]
     solver = BatchedSectorSolver(cat, pairs, spec.density_terms, precision="mixed", nev=4, max_requests=n)
@@ -306,8 +307,8 @@ def run_ours(args, rank, world):
     assert (st == 0).all(), "unconverged requests in the batch"
 
     # --- roofline of the batch kernel: algorithmic bytes of its matvecs and
-    # of its Lanczos vector work (the per-H|psi> and per-iteration figures of
-    # the survey's measurement section)
+    # of its Lanczos vector work (per H|psi>: D*(8+4+2s) + hops*(4+1+4+s); per
+    # Lanczos iteration: (3+k)*D*8; per restart: (m+keep)*D*8)
     s = 8  # complex64 matvec input
     b_mv = dims * (8 + 4 + 2 * s) + stats["hops"] * (4 + 1 + 4 + s)
     bytes_mv = float((nmv * b_mv).sum())
@@ -339,8 +340,9 @@ def run_ours(args, rank, world):
     n_plain = args.plain_sample
     idx = [(i * 97) % n for i in range(n_plain)]
     t0 = time.perf_counter()
-    plain_ev = {}
+    plain_ev, plain_svc = {}, []
     for b in idx:
+        t1 = time.perf_counter()
         rq = reqs[b]
         A.update_orbit_stabilizer_phases_(cat, rq.group, A.Bosonic())
         basis = A.build_symmetry_sector_basis(cat, rq.irrep)
@@ -348,12 +350,21 @@ def run_ours(args, rank, world):
                                     spec.density_terms)
         vals, _, info = H.solve(4, tol=1e-10, seed=rq.seed, want_vectors=False)
         plain_ev[b] = vals
+        plain_svc.append(time.perf_counter() - t1)
     plain = None
     if n_plain:
         plain_s = (time.perf_counter() - t0) / n_plain
+        svc = np.array(plain_svc)
         max_rel_plain = max(float(np.max(np.abs(ev_mixed[b] - plain_ev[b]) / np.abs(plain_ev[b]))) for b in idx)
+        # the whole batch arrives at once; one solve at a time, request i waits
+        # for the i solves before it: latencies modelled from the sample's
+        # measured service times (the served stream below measures both arms)
+        q = np.cumsum(np.resize(svc, n))
         plain = {"solves_per_s": 1.0 / plain_s, "sample": n_plain,
-                 "p50_ms": 1e3 * plain_s * (n / 2 + 0.5), "p99_ms": 1e3 * plain_s * (0.99 * n + 1),
+                 "service_ms_p50": float(np.percentile(svc, 50) * 1e3),
+                 "service_ms_p99": float(np.percentile(svc, 99) * 1e3),
+                 "queue_p50_ms_modelled": float(np.percentile(q, 50) * 1e3),
+                 "queue_p99_ms_modelled": float(np.percentile(q, 99) * 1e3),
                  "max_rel_dE_mixed_vs_plain": max_rel_plain}
 
     cpu = None
@@ -363,6 +374,21 @@ def run_ours(args, rank, world):
                                            for b in cpu_ev)
 
     clocks = clk.summary()
+    extras = {}
+    if not args.no_extras and world == 1:
+        # the other configurations, measured after the timed region: the large
+        # single-sector kernels and solves (configs 2 and 3) and a short served
+        # stream (config 5) with both arms' latencies measured
+        del solver64
+        torch.cuda.empty_cache()
+        kernels = {}
+        for cfg in (config2_spec, config3_spec):
+            spec2, sec2, name2 = cfg()
+            kernels[name2] = large_sector_report(spec2, sec2, name2, steps=5, nev=3 if cfg is config2_spec else 1,
+                                                 krylovdim=30)
+            torch.cuda.empty_cache()
+        extras["kernels"] = kernels
+        extras["served"] = served_report(args.extras_served_n, 50.0, args.large_workers)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -371,8 +397,10 @@ def run_ours(args, rank, world):
         "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": (lambda t: t * n if t else None)(profiled_traffic_per_sector()),
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_batch launch "
-                                       "(192-sector capture, scaled by sectors)", "peak_kind": peak_kind, "kernel": "k_batch (persistent batched Lanczos)",
+                     "traffic_source": "from the committed ncu profile (profiles/k_batch_flux_scan_haldane3x4.md): "
+                                       "dram__bytes_read.sum + dram__bytes_write.sum of one 192-sector k_batch launch, "
+                                       "scaled by sectors; not measured in this run",
+                     "peak_kind": peak_kind, "kernel": "k_batch (persistent batched Lanczos)",
                      "bytes_per_launch": bytes_launch, "matvec_bytes_per_launch": bytes_mv,
                      "lanczos_bytes_per_launch": bytes_lz, "frac_matvec_bytes_only": bytes_mv / t_launch / 1e9 / peak,
                      "note": "algorithmic bytes of one launch: every matvec D*(8+4+2s)+hops*(4+1+4+s) (s=8), plus "
@@ -393,35 +421,32 @@ def run_ours(args, rank, world):
         "dims": {"min": int(dims.min()), "max": int(dims.max())},
         "matvecs_per_solve": float(nmv.mean()),
         "wall_s_timed": t_wall,
+        **extras,
     }
     print(json.dumps(line), flush=True)
 
 
-def run_large(args):
-    """One large sector: checkerboard 4x6 spinless fermions (48 sites, NN t=1
-    e^{+-i pi/4}, NNN +-0.3, NNNN -0.2, V=1), Np=8, k=(0,0), nev=3 by default.  Reports
-    the device catalog build, the H|psi> kernel in FP64 and complex64 (GB/s of
-    algorithmic bytes against the HBM peak), and the FP64 / mixed solves."""
+def large_sector_report(spec, sector: int, name: str, steps: int, nev: int, krylovdim: int,
+                        precisions=("fp64", "mixed"), solve: bool = True):
+    """One large sector: the device catalog and sector builds, the H|psi>
+    kernels -- the matrix-free gather and the stored hop table -- in FP64 and
+    complex64 (CUDA-event medians over ``steps`` launches, L2 flushed between
+    them; GB/s of the algorithmic bytes D*(8+4+2s) + hops*(4+1+4+s) against the
+    measured HBM peak), and the FP64 and mixed-precision solves."""
+    import ctypes as C
+
     import torch
 
     import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300 import _lib
     from realspace_exactdiagonalization_gb300 import lattice as L
+    from realspace_exactdiagonalization_gb300.groups import statistics_from_name
 
-    torch.cuda.set_device(0)
-    L1, L2, npart = args.large_shape
-    if args.large_model == "hubbard":
-        # config 3: Hubbard 4x4, t=1, U=8, 7+7 electrons in the reference's encoding
-        # (fixed total particle number over 2*L1*L2 modes), momentum (pi, 0)
-        spec = L.hubbard_square(L1, L2, n_filled=npart)
-        sector = (L1 // 2) * L2
-        name = f"hubbard{L1}x{L2}_n{npart}_k(pi,0)"
-    else:
-        spec = L.checkerboard(L1, L2, n_filled=npart)
-        sector = 0
-        name = f"checkerboard{L1}x{L2}_np{npart}_k00"
     G = L.build_translation_group(spec.lattice)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G, particle_statistics=A.Fermionic())
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G,
+                                         particle_statistics=statistics_from_name(spec.statistics))
     t_cat = time.perf_counter() - t0
     irr = L.build_translation_irrep_list(G, spec.lattice)[sector]
     t0 = time.perf_counter()
@@ -430,18 +455,15 @@ def run_large(args):
     stream = torch.cuda.current_stream()
     res = {}
     peak, peak_kind = measured_peak()
-    for prec in (("fp64", "mixed") if args.large_precision == "both" else (args.large_precision,)):
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for prec in precisions:
         H = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms(), spec.density_terms, precision=prec)
         info = H.info()
-        from realspace_exactdiagonalization_gb300 import _lib
-        import ctypes as C
-
         _lib.check(_lib.load().sed_op_set_stream(H.handle, C.c_void_p(stream.cuda_stream)))
         n_orb = info["n_orbits"]
         s = 16 if prec == "fp64" else 8
         xs = torch.randn(n_orb * 2, dtype=torch.float64 if prec == "fp64" else torch.float32, device="cuda")
         y = torch.empty(n_orb * 2, dtype=torch.float64, device="cuda")
-        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
         def time_matvec():
             for _ in range(2):
@@ -449,7 +471,7 @@ def run_large(args):
                                                           C.c_void_p(y.data_ptr())))
             torch.cuda.synchronize()
             ms = []
-            for _ in range(args.steps):
+            for _ in range(steps):
                 flush.zero_()
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
@@ -464,9 +486,10 @@ def run_large(args):
         H.set_hop_table(H.HOP_TABLE_OFF)
         t_fly = time_matvec()
         b_alg = info["dim"] * (8 + 4 + 2 * s) + info["hops"] * (4 + 1 + 4 + s)
-        r = {"matvec_ms": 1e3 * t_fly, "bytes_alg": b_alg, "achieved_gbs": b_alg / t_fly / 1e9,
-             "frac": b_alg / t_fly / 1e9 / peak, "hops": info["hops"],
-             "gather_shape_threads_per_row_block": list(H.apply_shape(prec == "mixed"))}
+        r = {"k_apply": {"matvec_ms": 1e3 * t_fly, "bytes_alg": b_alg, "achieved_gbs": b_alg / t_fly / 1e9,
+                         "frac": b_alg / t_fly / 1e9 / peak,
+                         "shape_threads_per_row_block": list(H.apply_shape(prec == "mixed"))},
+             "hops": info["hops"]}
         # the stored hop table (8 bytes per hop, streamed)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -477,97 +500,166 @@ def run_large(args):
             t_tab = time_matvec()
             # bytes the table matvec must move: records, x gathers, row reads and writes
             b_tab = tinfo["records"] * 8 + info["hops"] * s + info["dim"] * (16 + 4 + 1 + s + 16)
-            r["hop_table"] = {"matvec_ms": 1e3 * t_tab, "build_s": t_build, "table_gb": tinfo["bytes"] / 1e9,
-                              "records": tinfo["records"], "padding": tinfo["records"] / max(info["hops"], 1) - 1,
-                              "achieved_gbs_alg": b_alg / t_tab / 1e9, "frac_alg": b_alg / t_tab / 1e9 / peak,
-                              "table_bytes": b_tab, "achieved_gbs_table": b_tab / t_tab / 1e9,
-                              "frac_table": b_tab / t_tab / 1e9 / peak, "speedup_vs_gather": t_fly / t_tab}
+            r["k_apply_tab"] = {"matvec_ms": 1e3 * t_tab, "build_s": t_build, "table_gb": tinfo["bytes"] / 1e9,
+                                "records": tinfo["records"], "padding": tinfo["records"] / max(info["hops"], 1) - 1,
+                                "achieved_gbs": b_alg / t_tab / 1e9, "frac": b_alg / t_tab / 1e9 / peak,
+                                "table_bytes": b_tab, "achieved_gbs_table_bytes": b_tab / t_tab / 1e9,
+                                "frac_table_bytes": b_tab / t_tab / 1e9 / peak, "speedup_vs_gather": t_fly / t_tab}
         except _lib.SEDError as e:
-            r["hop_table"] = {"unavailable": str(e)}
-        if not args.no_solve:
+            r["k_apply_tab"] = {"unavailable": str(e)}
+        if solve:
             t0 = time.perf_counter()
-            vals, _, sinfo = H.solve(args.large_nev, tol=1e-10, krylovdim=args.krylovdim, want_vectors=False)
+            vals, _, sinfo = H.solve(nev, tol=1e-10, krylovdim=krylovdim, want_vectors=False)
             r.update({"solve_s": time.perf_counter() - t0, "evals": [float(v) for v in vals],
-                      "nev": args.large_nev, "krylovdim": args.krylovdim, "restarts": sinfo.n_restarts,
+                      "nev": nev, "krylovdim": krylovdim, "restarts": sinfo.n_restarts,
                       "matvecs": sinfo.n_matvec, "matvecs_fp64": sinfo.n_matvec_fp64,
                       "max_residual": sinfo.max_residual, "delta_polish": sinfo.max_delta_polish,
                       "solve_uses_hop_table": H.hop_table_info()["built"]})
         res[prec] = r
-        del H
+        del H, xs, y
+        torch.cuda.synchronize()
     if "evals" in res.get("fp64", {}) and "evals" in res.get("mixed", {}):
         e64, em = np.array(res["fp64"]["evals"]), np.array(res["mixed"]["evals"])
         res["max_rel_dE_mixed_vs_fp64"] = float(np.max(np.abs(em - e64) / np.abs(e64)))
-    line = {"workload": name, "n_states": cat.n_states, "n_orbits": cat.n_orbits,
-            "dim": basis.dim, "catalog_build_s": t_cat, "sector_build_s": t_sec, "peak_gbs": peak,
-            "peak_kind": peak_kind, **res}
+        res["mixed_speedup_vs_fp64_solve"] = res["fp64"]["solve_s"] / res["mixed"]["solve_s"]
+    return {"workload": name, "n_states": cat.n_states, "n_orbits": cat.n_orbits, "dim": basis.dim,
+            "catalog_build_s": t_cat, "sector_build_s": t_sec, "peak_gbs": peak, "peak_kind": peak_kind, **res}
+
+
+def config2_spec():
+    """Checkerboard 4x6 spinless fermions (48 sites; NN |t| = 1 with
+    e^{+-i pi/4}, NNN +-0.3, NNNN -0.2, V = 1), 8 particles, momentum (0, 0)."""
+    from realspace_exactdiagonalization_gb300 import lattice as L
+
+    return L.checkerboard(4, 6, n_filled=8), 0, "checkerboard4x6_np8_k(0,0)"
+
+
+def config3_spec():
+    """Hubbard 4x4 (t = 1, U = 8) as 32 modes, up spin at bit i and down spin
+    at bit i + 16, N_up = N_down = 7, momentum (pi, 0) = label (2, 0)."""
+    from realspace_exactdiagonalization_gb300 import lattice as L
+
+    return L.hubbard_square(4, 4, n_up=7, n_dn=7), 2 * 4 + 0, "hubbard4x4_7u7d_k(pi,0)"
+
+
+def run_large(args):
+    import torch
+
+    from realspace_exactdiagonalization_gb300 import lattice as L
+
+    torch.cuda.set_device(0)
+    L1, L2, npart = args.large_shape
+    if args.large_model == "hubbard":
+        spec, sector, name = config3_spec()
+        if (L1, L2, npart) != (4, 6, 8):  # a shape other than the default: N_up = N_down = npart / 2
+            spec = L.hubbard_square(L1, L2, n_up=npart // 2, n_dn=npart - npart // 2)
+            sector = (L1 // 2) * L2
+            name = f"hubbard{L1}x{L2}_{npart // 2}u{npart - npart // 2}d_k(pi,0)"
+    else:
+        spec = L.checkerboard(L1, L2, n_filled=npart)
+        sector, name = 0, f"checkerboard{L1}x{L2}_np{npart}_k(0,0)"
+    precs = ("fp64", "mixed") if args.large_precision == "both" else (args.large_precision,)
+    line = large_sector_report(spec, sector, name, args.steps, args.large_nev, args.krylovdim, precs,
+                               solve=not args.no_solve)
     print(json.dumps(line), flush=True)
 
 
-def run_served(args):
+def fifo_latencies(arrivals, service):
+    """One server answering requests in arrival order: request i starts when
+    it has arrived and request i-1 is done."""
+    t, out = 0.0, []
+    for a, sv in zip(arrivals, service):
+        t = max(t, a) + sv
+        out.append(t - a)
+    return np.asarray(out), t
+
+
+def served_report(n_req: int, rate: float, large_workers: int = 3, plain_all: bool = True, plain_per_family: int = 2,
+                  seed: int = 20261203):
     """Config 5: a seeded Poisson stream of ground-state requests drawn
     uniformly from rings N in {20, 24, 28}, checkerboard 3x4 / 4x4 and Hubbard
-    3x4 / 4x4 with N_up = N_down in {5, 6}, random momentum and twist; served
-    with continuous batching under a 160 GB device budget, against the plain
-    FP64 drop-in answering the same requests one at a time."""
-    import torch
-
+    3x4 / 4x4 with N_up = N_down in {5, 6} (two-species blocks), random momentum
+    and twist, nev = 1; served with continuous batching under a 160 GB device
+    budget.  Against it, the plain FP64 drop-in answers the same requests one
+    at a time: every request's FP64 solve is timed (plain_all), and the same
+    arrival times are replayed through a first-in-first-out single server with
+    those service times; or, for long streams, per-family means of a sample of
+    plain_per_family requests stand in for the service times (stated in the
+    result)."""
     import realspace_exactdiagonalization_gb300.api as A
     from realspace_exactdiagonalization_gb300 import lattice as L
     from realspace_exactdiagonalization_gb300.serving import (SectorServer, config5_families, latency_stats,
                                                               random_requests)
 
-    torch.cuda.set_device(0)
     fams = config5_families()
     t0 = time.perf_counter()
-    srv = SectorServer(fams, budget_bytes=160e9, batch_lanes=2, large_workers=args.large_workers)
+    srv = SectorServer(fams, budget_bytes=160e9, batch_lanes=2, large_workers=large_workers)
     t_setup = time.perf_counter() - t0
-    reqs = random_requests(fams, args.served_n, rate=args.served_rate, seed=20261203)
+    reqs = random_requests(fams, n_req, rate=rate, seed=seed)
     done = sorted(srv.serve(reqs), key=lambda r: r.rid)
     st = latency_stats(done)
-    bad = [r.rid for r in done if r.status != 0]
     errors = {r.rid: f"{r.family}: {r.error or r.status}" for r in done if r.status != 0}
-    # the plain FP64 drop-in, one request at a time, on a per-family sample
+
+    def plain_solve(r):
+        fam = srv.families[r.family]
+        G = L.build_translation_group(fam.spec.lattice, r.twist)
+        irr = L.build_translation_irrep_list(G, fam.spec.lattice)[r.k_index]
+        t1 = time.perf_counter()
+        basis = A.build_symmetry_sector_basis(fam.catalog, irr, group=G)
+        e = float("nan")
+        if basis.dim:
+            H = A.MatrixFreeHamiltonian(basis, fam.spec.bilinear_terms(r.twist), fam.spec.density_terms)
+            vals, _, _ = H.solve(r.nev, tol=1e-10, seed=r.seed, want_vectors=False)
+            e = float(vals[0])
+            del H
+        return time.perf_counter() - t1, e
+
+    plain_ev, service = {}, {}
+    if plain_all:
+        for r in done:
+            service[r.rid], plain_ev[r.rid] = plain_solve(r)
+        kind = "measured: every request's FP64 solve timed, FIFO replay of the stream's arrival times"
+    else:
+        per = {}
+        for name in sorted(fams):
+            for r in [q for q in done if q.family == name][:plain_per_family]:
+                sv, plain_ev[r.rid] = plain_solve(r)
+                per.setdefault(name, []).append(sv)
+        for r in done:
+            service[r.rid] = float(np.mean(per[r.family]))
+        kind = (f"modelled: FIFO replay with per-family mean FP64 service times of {plain_per_family} measured "
+                f"requests per family")
+    arr = np.array([r.arrival for r in done])
+    sv = np.array([service[r.rid] for r in done])
+    order = np.argsort(arr, kind="stable")
+    lat, t_last = fifo_latencies(arr[order], sv[order])
+    plain = {"solves_per_s": len(done) / (t_last - arr.min()), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+             "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_service_s": float(sv.mean()), "latencies": kind}
+    rel = [abs(done[i].evals[0] - e) / abs(e) for i, e in plain_ev.items() if np.isfinite(e)]
     per_fam = {}
-    plain_ev = {}
     for name in sorted(fams):
-        sample = [r for r in done if r.family == name][: args.plain_per_family]
-        times, mixed_times = [], []
-        fam = srv.families[name]
-        for r in sample:
-            G = L.build_translation_group(fam.spec.lattice, r.twist)
-            irr = L.build_translation_irrep_list(G, fam.spec.lattice)[r.k_index]
-            t1 = time.perf_counter()
-            basis = A.build_symmetry_sector_basis(fam.catalog, irr, group=G)
-            if basis.dim:
-                H = A.MatrixFreeHamiltonian(basis, fam.spec.bilinear_terms(r.twist), fam.spec.density_terms)
-                vals, _, _ = H.solve(1, tol=1e-10, seed=r.seed, want_vectors=False)
-                plain_ev[r.rid] = vals[0]
-                del H
-            times.append(time.perf_counter() - t1)
-            if fam.route == "large" and basis.dim:
-                # the same request alone through the served large route's mixed solve
-                t1 = time.perf_counter()
-                basis = A.build_symmetry_sector_basis(fam.catalog, irr, group=G)
-                H = A.MatrixFreeHamiltonian(basis, fam.spec.bilinear_terms(r.twist), fam.spec.density_terms,
-                                            precision="mixed")
-                H.solve(1, tol=1e-10, seed=r.seed, want_vectors=False)
-                del H
-                mixed_times.append(time.perf_counter() - t1)
         mine = [r for r in done if r.family == name]
-        per_fam[name] = {"plain_fp64_s": float(np.mean(times)) if times else None, "route": fam.route,
-                         "n_orbits": fam.n_orbits, "served": len(mine),
-                         # time from the start of the request's solve (or of its batch) to its answer
+        fam = srv.families[name]
+        per_fam[name] = {"route": fam.route, "n_orbits": fam.n_orbits, "served": len(mine),
+                         "plain_fp64_service_s": float(np.mean([service[r.rid] for r in mine])) if mine else None,
                          "mean_service_s": float(np.mean([r.t_end - r.t_start for r in mine])) if mine else None,
-                         "mean_wait_s": float(np.mean([r.t_start - r.arrival for r in mine])) if mine else None,
-                         "mixed_alone_s": float(np.mean(mixed_times)) if mixed_times else None}
-    mix_s = np.mean([per_fam[r.family]["plain_fp64_s"] for r in done])
-    rel = [abs(done[i].evals[0] - e) / abs(e) for i, e in plain_ev.items()]
-    line = {"workload": "served_config5", "requests": len(done), "rate_per_s": args.served_rate,
-            "served": st, "unconverged": bad, "errors": errors, "setup_s": t_setup, "peak_reserved_gb": srv.peak_reserved / 1e9,
-            "resident_gb": srv.resident / 1e9,
-            "plain_fp64_one_at_a_time_solves_per_s": 1.0 / mix_s,
-            "speedup_vs_plain_fp64": st["solves_per_s"] * mix_s,
+                         "mean_wait_s": float(np.mean([r.t_start - r.arrival for r in mine])) if mine else None}
+    return {"workload": "served_config5", "requests": len(done), "rate_per_s": rate, "seed": seed,
+            "served": st, "plain_fp64_one_at_a_time": plain,
+            "speedup_solves_per_s": st["solves_per_s"] / plain["solves_per_s"],
+            "p50_ratio_plain_over_served": plain["p50_ms"] / st["p50_ms"],
+            "p99_ratio_plain_over_served": plain["p99_ms"] / st["p99_ms"],
+            "unconverged": [r.rid for r in done if r.status != 0], "errors": errors, "setup_s": t_setup,
+            "peak_reserved_gb": srv.peak_reserved / 1e9, "resident_gb": srv.resident / 1e9,
             "max_rel_dE_vs_plain_fp64": float(max(rel)) if rel else None, "families": per_fam}
+
+
+def run_served(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    line = served_report(args.served_n, args.served_rate, args.large_workers, plain_all=not args.plain_sampled,
+                         plain_per_family=args.plain_per_family)
     print(json.dumps(line), flush=True)
 
 
@@ -588,6 +680,12 @@ def main():
     ap.add_argument("--served-rate", type=float, default=50.0)
     ap.add_argument("--large-workers", type=int, default=3)
     ap.add_argument("--plain-per-family", type=int, default=2)
+    ap.add_argument("--plain-sampled", action="store_true",
+                    help="served workload: model the plain FP64 arm from per-family samples instead of timing "
+                         "every request (long streams)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the config-2/3 kernel and solve report and the short served stream")
+    ap.add_argument("--extras-served-n", type=int, default=200)
     ap.add_argument("--large-shape", type=int, nargs=3, default=[4, 6, 8], metavar=("L1", "L2", "NP"))
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--large-nev", type=int, default=3, help="eigenpairs of the large-sector solve")
