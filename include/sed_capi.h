@@ -305,6 +305,23 @@ int sed_batch_create(const sed_catalog* c, int n_bil, const int32_t* bil_ij, int
 int sed_batch_run(sed_batch* b, int n_req, const double* chi_reim, const double* group_phase_reim,
                   const double* bil_t_reim, const uint64_t* seeds, double tol, int maxiter, double* evals,
                   int32_t* status, int64_t* dims, double* delta_polish, int32_t* n_matvec);
+/* The same run returning eigenvectors as well (the (vals, vecs) layout of
+ * ed_scan_at_irrep_matrixfree!, SRE:1124, per request): evecs_reim receives
+ * n_req x nev complex128 vectors, vector i of request b at
+ * evecs_reim[2 * ((b * nev + i) * ld + row)], row < dims[b] in the sector's
+ * row order (ascending representative, as sed_sector_build_group orders the
+ * sector of that request's momentum and group).  ld >= the catalog's orbit
+ * count; entries at rows >= dims[b] are not written.  Each vector is in the
+ * gauge of the request's own group (the site gauge of sed_batch_set_site_gauge
+ * is undone).  The device variant takes device buffers. */
+int sed_batch_run_vectors(sed_batch* b, int n_req, const double* chi_reim, const double* group_phase_reim,
+                          const double* bil_t_reim, const uint64_t* seeds, double tol, int maxiter, double* evals,
+                          int32_t* status, int64_t* dims, double* delta_polish, int32_t* n_matvec,
+                          double* evecs_reim, int64_t ld);
+int sed_batch_run_device_vectors(sed_batch* b, int n_req, const double* d_chi, const double* d_group_phase,
+                                 const double* d_bil_t, const uint64_t* d_seeds, double tol, int maxiter,
+                                 double* d_evals, int32_t* d_status, int64_t* d_dims, double* d_delta,
+                                 int32_t* d_n_matvec, double* d_evecs, int64_t ld);
 /* Per-request diagnostics of the last run (host buffers of n_req entries, any
  * may be NULL): hops evaluated by one matvec of the request's sector, and the
  * device clock (ns) when its block picked it up and when it finished. */

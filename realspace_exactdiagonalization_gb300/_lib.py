@@ -83,6 +83,8 @@ SIGNATURES = [
     ("sed_solve", _i32, [_p, _i32, _dbl, _i32, _i32, _u64, _p, _p, _p]),
     ("sed_batch_create", _i32, [_p, _i32, _p, _i32, _p, _p, _i32, _i32, _i32, _i32, _p]),
     ("sed_batch_run", _i32, [_p, _i32, _p, _p, _p, _p, _dbl, _i32, _p, _p, _p, _p, _p]),
+    ("sed_batch_run_vectors", _i32, [_p, _i32, _p, _p, _p, _p, _dbl, _i32, _p, _p, _p, _p, _p, _p, _i64]),
+    ("sed_batch_run_device_vectors", _i32, [_p, _i32, _p, _p, _p, _p, _dbl, _i32, _p, _p, _p, _p, _p, _p, _i64]),
     ("sed_batch_last_stats", _i32, [_p, _p, _p, _p]),
     ("sed_batch_last_info", _i32, [_p, _p, _p, _p]),
     ("sed_batch_graph_info", _i32, [_p, _p, _p]),

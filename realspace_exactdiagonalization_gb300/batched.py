@@ -92,7 +92,7 @@ class BatchedSectorSolver:
             seeds[b] = r.seed
         return chi, ph, amp, seeds
 
-    def run_packed(self, chi, ph, amp, seeds, tol: float = 1e-10, maxiter: int = 300):
+    def run_packed(self, chi, ph, amp, seeds, tol: float = 1e-10, maxiter: int = 300, want_vectors: bool = False):
         n = len(seeds)
         self._last_n = n
         if n > self.max_requests:
@@ -102,9 +102,19 @@ class BatchedSectorSolver:
         dims = np.zeros(n, dtype=np.int64)
         delta = np.zeros(n, dtype=np.float64)
         nmv = np.zeros(n, dtype=np.int32)
-        check(_lib.load().sed_batch_run(self._h, n, ptr(chi), ptr(ph), ptr(amp), ptr(seeds), float(tol), int(maxiter),
-                                        ptr(ev), ptr(st), ptr(dims), ptr(delta), ptr(nmv)))
-        return {"evals": ev, "status": st, "dims": dims, "delta_polish": delta, "matvecs": nmv}
+        out = {"evals": ev, "status": st, "dims": dims, "delta_polish": delta, "matvecs": nmv}
+        if not want_vectors:
+            check(_lib.load().sed_batch_run(self._h, n, ptr(chi), ptr(ph), ptr(amp), ptr(seeds), float(tol),
+                                            int(maxiter), ptr(ev), ptr(st), ptr(dims), ptr(delta), ptr(nmv)))
+            return out
+        ld = max(int(self.catalog.n_orbits), 1)
+        vec = np.zeros((n, self.nev, ld), dtype=np.complex128)
+        check(_lib.load().sed_batch_run_vectors(self._h, n, ptr(chi), ptr(ph), ptr(amp), ptr(seeds), float(tol),
+                                                int(maxiter), ptr(ev), ptr(st), ptr(dims), ptr(delta), ptr(nmv),
+                                                ptr(vec), ld))
+        # request b: vecs[:, i] is its i-th eigenvector in sector-row order
+        out["evecs"] = [vec[b, :min(self.nev, int(dims[b])), :int(dims[b])].T.copy() for b in range(n)]
+        return out
 
     def last_stats(self):
         """Hops of one matvec and device start/end clocks (ns) of the last run's requests."""
@@ -150,8 +160,12 @@ class BatchedSectorSolver:
     def set_stream(self, stream_ptr: int) -> None:
         check(_lib.load().sed_batch_set_stream(self._h, C.c_void_p(stream_ptr)))
 
-    def run(self, requests: Sequence[SectorRequest], tol: float = 1e-10, maxiter: int = 300):
-        return self.run_packed(*self.pack(requests), tol=tol, maxiter=maxiter)
+    def run(self, requests: Sequence[SectorRequest], tol: float = 1e-10, maxiter: int = 300,
+            want_vectors: bool = False):
+        """Solve the requests in one launch.  With want_vectors, out["evecs"][b]
+        holds request b's eigenvectors as columns (sector-row order, the
+        reference's (vals, vecs) layout, SRE:1124)."""
+        return self.run_packed(*self.pack(requests), tol=tol, maxiter=maxiter, want_vectors=want_vectors)
 
 
 def flux_scan_requests(spec, twists: Sequence[Sequence[float]], seed0: int = 0x5EED0000) -> List[SectorRequest]:

@@ -88,6 +88,10 @@ struct BatchArgs {
   int64_t* hops;
   int64_t* t_ns;  // [n_req][2]
   unsigned int* queue;
+  // eigenvector output (NULL: none): request b's vector i in sector-row order
+  // at evecs[(b * nev + i) * ev_ld + row], complex128, rows < dims[b]
+  double2* evecs;
+  int64_t ev_ld;
 };
 
 struct BatchSmem {
@@ -1378,6 +1382,56 @@ __device__ __forceinline__ float4 lz_to_df(float4 v) { return v; }
 __device__ __forceinline__ float4 lz_to_df(float2 v) { return make_float4(v.x, v.y, 0.f, 0.f); }
 __device__ __forceinline__ double2 lz_to_d(float4 v) { return make_double2(df_to_d(v.x, v.z), df_to_d(v.y, v.w)); }
 __device__ __forceinline__ double2 lz_to_d(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 lz_to_d(double2 v) { return v; }
+
+// Eigenvector output of one request: vector i (i < nvec) of src (stride ld,
+// orbit-indexed, in the site gauge when gw is set) into sector-row order.  A
+// row's index is the number of sector orbits before it, counted by a
+// block-wide scan over rowflag one block-stride at a time; in gauge mode a
+// row's coefficient is multiplied by conj(prod_{j in rep} w_j), which undoes
+// the gauge (W |r> = prod_{j in rep} w_j |r'> for the sector basis states).
+// s_cnt holds kNW + 1 ints of shared scratch.
+template <class SRC>
+__device__ void block_write_vectors(const BatchArgs& a, const SRC* src, int64_t ld, int nvec,
+                                    const uint8_t* __restrict__ rowflag, const double2* gw, double2* out,
+                                    int* s_cnt) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int carry = 0;
+  for (int64_t base = 0; base < a.n_orb; base += blockDim.x) {
+    const int64_t o = base + threadIdx.x;
+    const bool f = o < a.n_orb && rowflag[o];
+    const unsigned bal = __ballot_sync(0xFFFFFFFFu, f);
+    if (lane == 0) s_cnt[wid] = __popc(bal);
+    __syncthreads();
+    int wpre = 0;
+    for (int w = 0; w < wid; ++w) wpre += s_cnt[w];
+    if (f) {
+      const int64_t row = carry + wpre + __popc(bal & ((1u << lane) - 1u));
+      double2 gc = make_double2(1.0, 0.0);  // conj(prod_{j in rep} w_j)
+      if (gw) {
+        uint64_t m = a.reps[o];
+        while (m) {
+          const int j = __ffsll((long long)m) - 1;
+          m &= m - 1;
+          const double2 w = gw[j];
+          gc = make_double2(gc.x * w.x + gc.y * w.y, gc.y * w.x - gc.x * w.y);
+        }
+      }
+      for (int i = 0; i < nvec; ++i) {
+        const double2 v = lz_to_d(src[(size_t)i * ld + o]);
+        out[(size_t)i * a.ev_ld + row] = make_double2(v.x * gc.x - v.y * gc.y, v.x * gc.y + v.y * gc.x);
+      }
+    }
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < kNW; ++w) tot += s_cnt[w];
+      s_cnt[kNW] = carry + tot;
+    }
+    __syncthreads();
+    carry = s_cnt[kNW];
+    __syncthreads();
+  }
+}
 
 // ---------------------------------------------------------------- the kernel
 // Rayleigh-Ritz on a block B that is only semi-orthogonal (kSelReorth): with
@@ -1763,6 +1817,10 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
     __syncthreads();
 
     int k = 0, restarts = 0, nmv = 0, n64 = 0, status = 0;
+    // where the returned eigenvectors end up: 0 the Ritz vectors in Vb (FP64
+    // kernel), 1 the polished double-float block in the restart buffer (hop
+    // table), 2 the polished FP64 block there (on-the-fly gather)
+    int vec_src = 0, vec_nw = 0;
     double beta = 0.0, prev_res = 1e300, best_prev = 1e300, dmax = 0.0;
     double tau = 1e-6;  // mixed: relative Ritz-estimate threshold of the complex64 run
     const bool mixed = sizeof(typename P::S) == 4;
@@ -2046,6 +2104,8 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         __syncthreads();
         if (ok) {
           if (threadIdx.x < nw) s_theta[threadIdx.x] = s_lam[threadIdx.x];
+          vec_src = a.use_tab ? 1 : 2;
+          vec_nw = nw;
           __syncthreads();
           break;
         }
@@ -2086,6 +2146,19 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       k = keep;
       ++restarts;
     }
+    if (a.evecs && status != kPolishFailed) {
+      double2* out = a.evecs + (size_t)b * a.nev * a.ev_ld;
+      const double2* gwv = (a.use_tab && a.gauge) ? a.gauge_w + (size_t)b * a.N : nullptr;
+      int* s_cnt = s_int + 2;
+      if (vec_src == 0)
+        block_write_vectors(a, Vb, a.ld, nev_out, rowflag, gwv, out, s_cnt);
+      else if (vec_src == 1)
+        block_write_vectors(a, reinterpret_cast<const float4*>(Rb) + (size_t)vec_nw * a.ld, a.ld, nev_out, rowflag,
+                            gwv, out, s_cnt);
+      else
+        block_write_vectors(a, reinterpret_cast<const double2*>(Rb) + (size_t)vec_nw * a.ld, a.ld, nev_out,
+                            rowflag, gwv, out, s_cnt);
+    }
     if (threadIdx.x == 0) {
       for (int i = 0; i < a.nev; ++i) a.evals[(size_t)b * a.nev + i] = i < nev_out ? s_theta[i] : nan("");
       a.status[b] = status;
@@ -2104,6 +2177,7 @@ struct BatchImpl {
   TermTables tt;
   DevBuf site_off, rec, diag, V, R, W, X64, tchi64, rowflag;
   DevBuf in_chi, in_phase, in_amp, in_seed, o_evals, o_status, o_dims, o_delta, o_nmv, o_hops, o_tns, queue;
+  DevBuf o_evecs;  // device staging of the host eigenvector output
   int last_n = 0, n_fallback = 0;
   DevBuf redo;
   // hop table (built at the first run, rebuilt when the phase classes change)
@@ -2793,7 +2867,10 @@ static void validate_requests(BatchImpl& B, int n_req, const double* phase, cons
 // Launch on device-resident buffers (asynchronous on the batch stream).
 void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const double* phase, const double* amp,
                          const uint64_t* seeds, double tol, int maxiter, double* evals, int32_t* status,
-                         int64_t* dims, double* delta, int32_t* nmv, const double* phase_host = nullptr) {
+                         int64_t* dims, double* delta, int32_t* nmv, const double* phase_host = nullptr,
+                         double* evecs = nullptr, int64_t ev_ld = 0) {
+  SED_REQUIRE(!evecs || ev_ld >= B.cat->n_orbits, 1,
+              "eigenvector leading dimension must be at least the catalog's orbit count");
   SED_REQUIRE(n_req >= 0 && n_req <= B.max_req, 1, "n_req exceeds max_requests");
   SED_REQUIRE(tol > 0.0 && maxiter >= 1, 1, "tol and maxiter must be positive");
   SED_REQUIRE(chi && phase && seeds && evals && status && dims && delta && nmv, 1, "NULL argument");
@@ -2824,6 +2901,8 @@ void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const doubl
   a.hops = B.o_hops.as<int64_t>();
   a.t_ns = B.o_tns.as<int64_t>();
   a.queue = B.queue.as<unsigned int>();
+  a.evecs = reinterpret_cast<double2*>(evecs);
+  a.ev_ld = evecs ? ev_ld : 0;
   // hop table for this run's phase classes (needs the phases on the host)
   std::vector<double> ph_h;
   if (B.phi_cap > 0 && B.tab_enabled && !phase_host) {
@@ -2887,7 +2966,7 @@ void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const doubl
 
 void batch_run(BatchImpl& B, int n_req, const double* chi, const double* phase, const double* amp,
                const uint64_t* seeds, double tol, int maxiter, double* evals, int32_t* status, int64_t* dims,
-               double* delta, int32_t* nmv) {
+               double* delta, int32_t* nmv, double* evecs = nullptr, int64_t ev_ld = 0) {
   const GroupImpl& G = *B.cat->group;
   SED_REQUIRE(n_req >= 0 && n_req <= B.max_req, 1, "n_req exceeds max_requests");
   SED_REQUIRE(chi && phase && seeds && evals, 1, "NULL argument");
@@ -2901,9 +2980,18 @@ void batch_run(BatchImpl& B, int n_req, const double* chi, const double* phase, 
   if (B.n_bil)
     SED_CUDA(cudaMemcpyAsync(B.in_amp.p, amp, (size_t)n_req * B.n_bil * 16, cudaMemcpyHostToDevice, s));
   SED_CUDA(cudaMemcpyAsync(B.in_seed.p, seeds, (size_t)n_req * 8, cudaMemcpyHostToDevice, s));
+  double* d_evecs = nullptr;
+  if (evecs) {
+    SED_REQUIRE(ev_ld >= B.cat->n_orbits, 1, "eigenvector leading dimension must be at least the catalog's orbit count");
+    const size_t bytes = (size_t)n_req * B.nev * ev_ld * 16;
+    if (B.o_evecs.bytes < bytes) B.o_evecs.alloc(bytes);
+    d_evecs = B.o_evecs.as<double>();
+  }
   batch_launch_device(B, n_req, B.in_chi.as<double>(), B.in_phase.as<double>(), B.in_amp.as<double>(),
                       B.in_seed.as<uint64_t>(), tol, maxiter, B.o_evals.as<double>(), B.o_status.as<int32_t>(),
-                      B.o_dims.as<int64_t>(), B.o_delta.as<double>(), B.o_nmv.as<int32_t>(), phase);
+                      B.o_dims.as<int64_t>(), B.o_delta.as<double>(), B.o_nmv.as<int32_t>(), phase, d_evecs, ev_ld);
+  if (evecs)
+    SED_CUDA(cudaMemcpyAsync(evecs, d_evecs, (size_t)n_req * B.nev * ev_ld * 16, cudaMemcpyDeviceToHost, s));
   SED_CUDA(cudaMemcpyAsync(evals, B.o_evals.p, (size_t)n_req * B.nev * 8, cudaMemcpyDeviceToHost, s));
   if (status) SED_CUDA(cudaMemcpyAsync(status, B.o_status.p, (size_t)n_req * 4, cudaMemcpyDeviceToHost, s));
   if (dims) SED_CUDA(cudaMemcpyAsync(dims, B.o_dims.p, (size_t)n_req * 8, cudaMemcpyDeviceToHost, s));
@@ -3004,6 +3092,26 @@ int sed_batch_set_hop_table(sed_batch* b, int enable) {
   });
 }
 
+int sed_batch_run_vectors(sed_batch* b, int n_req, const double* chi_reim, const double* group_phase_reim,
+                          const double* bil_t_reim, const uint64_t* seeds, double tol, int maxiter, double* evals,
+                          int32_t* status, int64_t* dims, double* delta_polish, int32_t* n_matvec,
+                          double* evecs_reim, int64_t ld) {
+  return bguard([&] {
+    SED_REQUIRE(b && evecs_reim, 1, "NULL argument");
+    sed::batch_run(*b->p, n_req, chi_reim, group_phase_reim, bil_t_reim, seeds, tol, maxiter, evals, status, dims,
+                   delta_polish, n_matvec, evecs_reim, ld);
+  });
+}
+int sed_batch_run_device_vectors(sed_batch* b, int n_req, const double* d_chi, const double* d_group_phase,
+                                 const double* d_bil_t, const uint64_t* d_seeds, double tol, int maxiter,
+                                 double* d_evals, int32_t* d_status, int64_t* d_dims, double* d_delta,
+                                 int32_t* d_n_matvec, double* d_evecs, int64_t ld) {
+  return bguard([&] {
+    SED_REQUIRE(b && d_evecs, 1, "NULL argument");
+    sed::batch_launch_device(*b->p, n_req, d_chi, d_group_phase, d_bil_t, d_seeds, tol, maxiter, d_evals, d_status,
+                             d_dims, d_delta, d_n_matvec, nullptr, d_evecs, ld);
+  });
+}
 int sed_batch_run_device(sed_batch* b, int n_req, const double* d_chi, const double* d_group_phase,
                          const double* d_bil_t, const uint64_t* d_seeds, double tol, int maxiter, double* d_evals,
                          int32_t* d_status, int64_t* d_dims, double* d_delta, int32_t* d_n_matvec) {

@@ -167,14 +167,76 @@ def flux_point_states(spec: L.ModelSpec, flux: Sequence[float], manifold_size: i
     return pt
 
 
+def flux_points_batched(spec: L.ModelSpec, fluxes: Sequence[Sequence[float]], manifold_size: int,
+                        catalog: A.Symmetry_Orbit_Catalog, want_fock: bool = True, tol: float = 1e-10,
+                        precision: str = "fp64") -> List[FluxPoint]:
+    """flux_point_states for many fluxes at once: every (flux, momentum)
+    sector of the list is solved in one persistent batched launch, which
+    returns eigenvalues and eigenvectors (the reference solves them one at a
+    time, many_body_chern_number.jl:193-210, charge_pump.jl:288-303); each
+    point then selects its globally lowest manifold_size states and checks the
+    gap above them as flux_point_states does."""
+    from .batched import BatchedSectorSolver, flux_scan_requests
+
+    nev = manifold_size + 1
+    if nev > 6:
+        raise ValueError("the batched path solves at most 6 levels per sector (manifold_size <= 5)")
+    fluxes = [tuple(float(f) for f in fl) for fl in fluxes]
+    reqs = flux_scan_requests(spec, fluxes)
+    pairs = [(i, j) for (i, j, _) in spec.bilinear_terms()]
+    solver = BatchedSectorSolver(catalog, pairs, spec.density_terms, precision=precision, nev=nev,
+                                 max_requests=len(reqs))
+    out = solver.run(reqs, tol=tol, want_vectors=True)
+    bad = np.nonzero(out["status"] != 0)[0]
+    if bad.size:
+        raise RuntimeError(f"batched solve did not converge for requests {bad.tolist()}")
+    n_k = len(reqs) // len(fluxes)
+    pts = []
+    for f, flux in enumerate(fluxes):
+        cands = []
+        bases: Dict[Tuple[int, int], A.Symmetry_Sector_Basis] = {}
+        vecs: Dict[Tuple[int, int], np.ndarray] = {}
+        for q in range(f * n_k, (f + 1) * n_k):
+            r = reqs[q]
+            if out["dims"][q] == 0:
+                continue
+            label = tuple(int(x) for x in r.irrep.label)
+            basis = A.build_symmetry_sector_basis(catalog, r.irrep, group=r.group)
+            if basis.dim != out["dims"][q]:
+                raise RuntimeError("batched sector dimension differs from the sector basis")
+            bases[label] = basis
+            vecs[label] = out["evecs"][q]
+            for lev in range(vecs[label].shape[1]):
+                cands.append((float(out["evals"][q, lev]), label, lev))
+        cands.sort(key=lambda c: c[0])
+        if len(cands) <= manifold_size:
+            raise ValueError("Need a state above the selected manifold to check its gap.")
+        pt = FluxPoint()
+        pt.gap = cands[manifold_size][0] - cands[manifold_size - 1][0]
+        if not pt.gap > 1e-9:
+            raise ValueError(f"Low-energy manifold is not isolated at flux {list(flux)} (gap={pt.gap}).")
+        pt.bases = bases
+        for e, label, lev in cands[:manifold_size]:
+            pt.energies.append(e)
+            pt.labels.append((label, lev + 1))
+            v = vecs[label][:, lev]
+            pt.vectors.append(v)
+            if want_fock:
+                pt.states.append(A.expand_sector_state_to_fock(v, bases[label]))
+        pts.append(pt)
+    return pts
+
+
 # ------------------------------------------------------------ Chern number
 def many_body_chern_number(spec: L.ModelSpec, manifold_size: int, flux_grid_size=(5, 5),
-                           det_atol: float = 1e-10) -> dict:
+                           det_atol: float = 1e-10, solver: str = "batch") -> dict:
     """Fukui-Hatsugai-Suzuki Chern number of the globally lowest
     ``manifold_size`` states over the flux torus
     (many_body_chern_number.jl:166-257): U(1) links are the phases of the
     overlap-matrix determinants between neighbouring flux points, the
-    curvature is the plaquette phase, and C = sum / 2 pi."""
+    curvature is the plaquette phase, and C = sum / 2 pi.  solver="batch"
+    solves the whole grid's sectors in one batched launch (FP64);
+    solver="single" one sector at a time."""
     if isinstance(flux_grid_size, int):
         nx = ny = int(flux_grid_size)
     else:
@@ -188,8 +250,13 @@ def many_body_chern_number(spec: L.ModelSpec, manifold_size: int, flux_grid_size
                                          particle_statistics=statistics_from_name(spec.statistics))
     fx = [ix / nx for ix in range(nx)]
     fy = [iy / ny for iy in range(ny)]
-    pts = [[flux_point_states(spec, (fx[ix], fy[iy]), manifold_size, catalog=cat) for iy in range(ny)]
-           for ix in range(nx)]
+    if solver == "batch" and manifold_size + 1 <= 6:
+        flat = flux_points_batched(spec, [(fx[ix], fy[iy]) for ix in range(nx) for iy in range(ny)],
+                                   manifold_size, cat)
+        pts = [[flat[ix * ny + iy] for iy in range(ny)] for ix in range(nx)]
+    else:
+        pts = [[flux_point_states(spec, (fx[ix], fy[iy]), manifold_size, catalog=cat) for iy in range(ny)]
+               for ix in range(nx)]
     Ux = np.zeros((nx, ny), dtype=np.complex128)
     Uy = np.zeros((nx, ny), dtype=np.complex128)
     dx = np.zeros((nx, ny))
@@ -266,7 +333,8 @@ def _tracked_phase_branches(raw_phases: np.ndarray) -> np.ndarray:
 def flux_charge_pump(spec: L.ModelSpec, manifold_size: int, flux_direction: int = 1,
                      polarization_direction: Optional[int] = None,
                      twisted_phases_over_2pi_list: Optional[Sequence[float]] = None,
-                     polarization_atol: float = 1e-10, include_sublattice: bool = True) -> dict:
+                     polarization_atol: float = 1e-10, include_sublattice: bool = True,
+                     solver: str = "batch") -> dict:
     """Many-body charge pump (charge_pump.jl:228-386): at every flux along
     ``flux_direction`` the globally lowest ``manifold_size`` states are
     selected, Resta's position operator along ``polarization_direction`` is
@@ -288,10 +356,18 @@ def flux_charge_pump(spec: L.ModelSpec, manifold_size: int, flux_direction: int 
     site_phases = many_body_position_phases(lat, polarization_direction, include_sublattice)
     gaps, min_sv, selected = [], [], []
     pol_eigs = np.zeros((len(fluxes), manifold_size), dtype=np.complex128)
-    for it, th in enumerate(fluxes):
+    path = []
+    for th in fluxes:
         flux = [0.0] * dim
         flux[flux_direction - 1] = float(th)
-        pt = flux_point_states(spec, flux, manifold_size, catalog=cat, want_fock=False)
+        path.append(flux)
+    if solver == "batch" and manifold_size + 1 <= 6:  # the whole flux path in one batched launch
+        batched = flux_points_batched(spec, path, manifold_size, cat, want_fock=False)
+    for it, th in enumerate(fluxes):
+        if solver == "batch" and manifold_size + 1 <= 6:
+            pt = batched[it]
+        else:
+            pt = flux_point_states(spec, path[it], manifold_size, catalog=cat, want_fock=False)
         gaps.append(pt.gap)
         selected.append(list(pt.labels))
         blocks = {}

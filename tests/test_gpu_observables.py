@@ -61,20 +61,26 @@ def test_fock_overlaps_match_numpy():
         np.testing.assert_allclose(M, ref, rtol=1e-12, atol=1e-12 * n)
 
 
-def test_chern_number_haldane2x3():
+@pytest.mark.parametrize("solver", ["batch", "single"])
+def test_chern_number_haldane2x3(solver):
+    """The 5x5 flux grid's 150 sector solves in one batched launch (eigenvalues
+    and eigenvectors), or one sector at a time: the same Chern number, gap and
+    link determinant as the reference notebook."""
     from realspace_exactdiagonalization_gb300.observables import many_body_chern_number
 
-    res = many_body_chern_number(L.haldane_honeycomb(2, 3), manifold_size=2, flux_grid_size=(5, 5))
+    res = many_body_chern_number(L.haldane_honeycomb(2, 3), manifold_size=2, flux_grid_size=(5, 5), solver=solver)
     assert abs(res["chern_number"] - 1.0) <= 1e-8 and res["rounded_chern"] == 1
     assert abs(res["min_gap"] - CHERN_MIN_GAP) <= 1e-9
     assert abs(res["min_link_det"] - CHERN_MIN_LINK_DET) <= 1e-9
 
 
-def test_charge_pump_haldane2x3():
+@pytest.mark.parametrize("solver", ["batch", "single"])
+def test_charge_pump_haldane2x3(solver):
     from realspace_exactdiagonalization_gb300.observables import flux_charge_pump
 
     res = flux_charge_pump(L.haldane_honeycomb(2, 3), manifold_size=2, flux_direction=1,
-                           polarization_direction=2, twisted_phases_over_2pi_list=[k / 16 for k in range(17)])
+                           polarization_direction=2, twisted_phases_over_2pi_list=[k / 16 for k in range(17)],
+                           solver=solver)
     np.testing.assert_allclose(res["pumped_charges"], [0.5, 0.5], atol=1e-8)
     assert abs(res["min_gap"] - PUMP_MIN_GAP) <= 1e-9
     assert min(res["min_position_singular_values"]) > 1e-10
