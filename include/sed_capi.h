@@ -299,6 +299,8 @@ int sed_solve(sed_op* op, int nev, double tol, int maxiter, int krylovdim, uint6
  * eigenvalues (ascending), status (0 ok, SED_ERR_NOT_CONVERGED), sector
  * dimension, |E_polished - E_c64| and the matvec count. */
 typedef struct sed_batch sed_batch;
+/* krylovdim: the Lanczos basis size (0: chosen by the autotuner, see
+ * sed_batch_set_shape). */
 int sed_batch_create(const sed_catalog* c, int n_bil, const int32_t* bil_ij, int n_den, const int32_t* den_ij,
                      const double* den_v_reim, int precision, int nev, int krylovdim, int max_requests,
                      sed_batch** out);
@@ -349,6 +351,21 @@ int sed_batch_set_x_in_shared_memory(sed_batch* b, int enable);
  * more than four distinct values per group element, or whose sectors leave no
  * shared memory for its coefficient tables, use the on-the-fly matvec. */
 int sed_batch_set_hop_table(sed_batch* b, int enable);
+/* Launch shape of the batched solve (no counterpart in the reference): the
+ * threads per row of the hop-table matvec (1, or 2 lanes splitting a row's
+ * records) and the Krylov dimension of the thick-restart Lanczos.  By default
+ * an autotuner times the candidates -- threads per row 1 and 2, and Krylov
+ * dimensions 24, 20 and 28 when sed_batch_create got krylovdim 0 (else that
+ * one) -- on one wave of the first run's requests per catalog shape, with
+ * CUDA events on the batch stream (so that run waits on the host), and keeps
+ * the fastest for the process.  SED_BATCH_SHAPE="krylovdim,threads_per_row"
+ * in the environment or sed_batch_set_shape pins a shape ((0, 0) returns to
+ * the autotuner; krylovdim at most 28 or the one given at creation).
+ * sed_batch_shape reports the shape of the last run and how many autotuner
+ * sweeps this batch object ran.  The shape changes results only within the
+ * solver's tolerance. */
+int sed_batch_set_shape(sed_batch* b, int krylovdim, int threads_per_row);
+int sed_batch_shape(const sed_batch* b, int32_t* krylovdim, int32_t* threads_per_row, int32_t* tune_runs);
 /* Site gauge (on by default; no counterpart in the reference).  When every
  * request of a run has a site gauge w -- per-site phases under which its
  * group's phases all become 1, as the flux-twisted translation groups of

@@ -91,6 +91,8 @@ SIGNATURES = [
     ("sed_batch_set_x_in_shared_memory", _i32, [_p, _i32]),
     ("sed_batch_set_hop_table", _i32, [_p, _i32]),
     ("sed_batch_set_site_gauge", _i32, [_p, _i32]),
+    ("sed_batch_set_shape", _i32, [_p, _i32, _i32]),
+    ("sed_batch_shape", _i32, [_p, _p, _p, _p]),
     ("sed_batch_last_gauge", _i32, [_p, _p]),
     ("sed_batch_run_device", _i32, [_p, _i32, _p, _p, _p, _p, _dbl, _i32, _p, _p, _p, _p, _p]),
     ("sed_batch_set_stream", _i32, [_p, _p]),

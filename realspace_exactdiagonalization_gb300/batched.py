@@ -36,10 +36,12 @@ class BatchedSectorSolver:
     ``bilinear_pairs`` is the fixed 1-based (i, j) list; every request supplies
     the amplitude of each pair (twisted boundary phases change amplitudes, not
     the pair list).  ``precision="mixed"`` runs complex64 matvecs with FP64
-    Lanczos and an FP64 Rayleigh-Ritz polish; ``"fp64"`` is all FP64."""
+    Lanczos and an FP64 Rayleigh-Ritz polish; ``"fp64"`` is all FP64.
+    ``krylovdim=0`` lets the launch autotuner choose the Krylov dimension
+    (with the matvec's threads per row); a positive value fixes it."""
 
     def __init__(self, catalog: Symmetry_Orbit_Catalog, bilinear_pairs, density_terms, precision: str = "mixed",
-                 nev: int = 4, krylovdim: int = 24, max_requests: int = 1024):
+                 nev: int = 4, krylovdim: int = 0, max_requests: int = 1024):
         self.catalog = catalog
         n_site = catalog.symmetry_group.n_site
         self.pairs = [(int(i), int(j)) for (i, j) in bilinear_pairs]
@@ -137,6 +139,17 @@ class BatchedSectorSolver:
         """Keep the complex64 matvec input in shared memory (default when it
         fits) or in global memory (the layout of sectors too large for it)."""
         check(_lib.load().sed_batch_set_x_in_shared_memory(self._h, int(bool(enable))))
+
+    def set_shape(self, krylovdim: int = 0, threads_per_row: int = 0) -> None:
+        """Pin the launch shape, or (0, 0) to let the autotuner choose."""
+        check(_lib.load().sed_batch_set_shape(self._h, int(krylovdim), int(threads_per_row)))
+
+    def shape(self):
+        """(krylovdim, threads_per_row) of the last run and the number of
+        autotuner sweeps this solver ran."""
+        m, t, n = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        check(_lib.load().sed_batch_shape(self._h, C.byref(m), C.byref(t), C.byref(n)))
+        return {"krylovdim": m.value, "threads_per_row": t.value, "tune_runs": n.value}
 
     def set_site_gauge(self, enable: bool) -> None:
         """Solve runs whose requests all have a site gauge (the flux-twisted

@@ -21,8 +21,12 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <thread>
 #include <type_traits>
 #include <unordered_map>
@@ -70,6 +74,7 @@ struct BatchArgs {
   // under its site gauge gauge_w[b][site], so a hop's coefficient is one
   // table entry times the sign its record carries (phase id 0: +, 1: -)
   int gauge;
+  int tpr;                 // threads per row of the hop-table matvec (1 or 2)
   const double2* gauge_w;  // [n_req][N]
   const int32_t* bil_dev;  // [n_bil][2] (from, to) sites of the bilinear terms
   const uint64_t* hop;
@@ -585,39 +590,75 @@ __device__ __forceinline__ void block_matvec(const BatchArgs& a, const typename 
   }
 }
 
+// sign of v flipped when bit 31 of f is set
+__device__ __forceinline__ float flip_sign(float v, uint32_t f) { return __uint_as_float(__float_as_uint(v) ^ f); }
+__device__ __forceinline__ double flip_sign(double v, uint32_t f) {
+  return __longlong_as_double(__double_as_longlong(v) ^ ((unsigned long long)f << 32));
+}
+
 // The same matvec through the hop table: one coalesced 8-byte record per hop
-// (thread l of a warp owns row 32s + l of slice s), then the column value,
-// the term-group coefficient and the phase-id coefficient from shared memory
-// or L1; the records carry the signs and phase-class counts, so a hop costs
-// no rank lookup, state word or popcount.
-template <class P, class WT>
+// (row 32s + l of slice s at sl_off[s] + 32k + l), then the column value and
+// the coefficient from shared memory; the records carry the signs and
+// phase-class counts, so a hop costs no rank lookup, state word or popcount.
+//   GAUGE = false: coefficient = tchi[term x element] * pwc[phase id] (the
+//     phase-id coefficient of the run's twist-phase classes);
+//   GAUGE = true (site-gauge runs): the phase id is only the hop's sign (0 +,
+//     1 -; padding records point at the zero coefficient), so a hop costs one
+//     shared-memory gather fewer -- the random gathers, with their bank
+//     conflicts, bound this matvec on the L1 data pipe.
+// TPR threads share a row (1, or 2: a lane pair splits the row's records by
+// parity and combines by a shuffle; 16 rows per warp), the batched launch's
+// threads-per-row shape, chosen by the autotuner.  Passes are uniform over the
+// block, so the pair shuffle never meets an exited lane.
+template <class P, bool GAUGE, int TPR, class WT>
 __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typename P::V* x,
                                                  const typename P::V* tchi, const typename P::V* pwc,
                                                  const double* s_isr, const float* s_isrf,
                                                  const uint8_t* __restrict__ rowflag, WT* __restrict__ w) {
   using V = typename P::V;
   using S = typename P::S;
-  const int lane = threadIdx.x & 31;
-  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
-    const int64_t sl = o >> 5;
-    const uint64_t* rp = a.hop + a.sl_off[sl] + lane;
-    const int wdt = a.sl_w[sl];
-    const double2 dg = a.diag[o];
-    const V xo = x[o];
-    S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
-    S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
+  const int sub = TPR == 1 ? 0 : (threadIdx.x & (TPR - 1));
+  const int64_t rows_per_pass = blockDim.x / TPR;
+  for (int64_t base = 0; base < a.n_orb; base += rows_per_pass) {
+    const int64_t o = base + threadIdx.x / TPR;
+    const bool valid = o < a.n_orb;
+    S ar = 0, ai = 0;
+    if (valid) {
+      const int64_t sl = o >> 5;
+      const uint64_t* rp = a.hop + a.sl_off[sl] + (o & 31);
+      const int wdt = a.sl_w[sl];
+      if (sub == 0) {
+        const double2 dg = a.diag[o];
+        const V xo = x[o];
+        ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
+        ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
+      }
 #pragma unroll 8
-    for (int k = 0; k < wdt; ++k) {
-      const uint64_t r = __ldg(rp + 32 * k);
-      const V t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
-      const V ph = pwc[(uint32_t)(r >> 42)];
-      const V xc = x[(uint32_t)r & 0xFFFFFFu];
-      const S cr = P::mad(t.x, ph.x, -t.y * ph.y), ci = P::mad(t.x, ph.y, t.y * ph.x);
-      ar = P::mad(cr, xc.x, ar);
-      ar = P::mad(-ci, xc.y, ar);
-      ai = P::mad(cr, xc.y, ai);
-      ai = P::mad(ci, xc.x, ai);
+      for (int k = sub; k < wdt; k += TPR) {
+        const uint64_t r = __ldg(rp + 32 * k);
+        const V t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
+        const V xc = x[(uint32_t)r & 0xFFFFFFu];
+        S cr, ci;
+        if (GAUGE) {
+          const uint32_t f = ((uint32_t)(r >> 42) & 1u) << 31;
+          cr = flip_sign(t.x, f);
+          ci = flip_sign(t.y, f);
+        } else {
+          const V ph = pwc[(uint32_t)(r >> 42)];
+          cr = P::mad(t.x, ph.x, -t.y * ph.y);
+          ci = P::mad(t.x, ph.y, t.y * ph.x);
+        }
+        ar = P::mad(cr, xc.x, ar);
+        ar = P::mad(-ci, xc.y, ar);
+        ai = P::mad(cr, xc.y, ai);
+        ai = P::mad(ci, xc.x, ai);
+      }
     }
+    if (TPR == 2) {
+      ar += __shfl_xor_sync(0xFFFFFFFFu, ar, 1);
+      ai += __shfl_xor_sync(0xFFFFFFFFu, ai, 1);
+    }
+    if (!valid || sub != 0) continue;
     if (!rowflag[o]) {
       zero_row(w, o);
       continue;
@@ -627,51 +668,17 @@ __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typen
   }
 }
 
-// sign of v flipped when bit 31 of f is set
-__device__ __forceinline__ float flip_sign(float v, uint32_t f) { return __uint_as_float(__float_as_uint(v) ^ f); }
-__device__ __forceinline__ double flip_sign(double v, uint32_t f) {
-  return __longlong_as_double(__double_as_longlong(v) ^ ((unsigned long long)f << 32));
-}
-
-// The hop-table matvec in gauge mode: the record's phase id is only the sign
-// of the hop (0: +, 1: -; padding records point at the zero coefficient), so
-// a hop costs the record load, one coefficient gather and the x gather --
-// one shared-memory gather fewer than block_matvec_tab, whose random gathers
-// (with their bank conflicts) bound the matvec on the L1 data pipe.
 template <class P, class WT>
-__device__ __forceinline__ void block_matvec_tab_gauge(const BatchArgs& a, const typename P::V* x,
-                                                       const typename P::V* tchi, const double* s_isr,
-                                                       const float* s_isrf, const uint8_t* __restrict__ rowflag,
-                                                       WT* __restrict__ w) {
-  using V = typename P::V;
-  using S = typename P::S;
-  const int lane = threadIdx.x & 31;
-  for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
-    const int64_t sl = o >> 5;
-    const uint64_t* rp = a.hop + a.sl_off[sl] + lane;
-    const int wdt = a.sl_w[sl];
-    const double2 dg = a.diag[o];
-    const V xo = x[o];
-    S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
-    S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
-#pragma unroll 8
-    for (int k = 0; k < wdt; ++k) {
-      const uint64_t r = __ldg(rp + 32 * k);
-      const V t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
-      const V xc = x[(uint32_t)r & 0xFFFFFFu];
-      const uint32_t f = ((uint32_t)(r >> 42) & 1u) << 31;
-      const S cr = flip_sign(t.x, f), ci = flip_sign(t.y, f);
-      ar = P::mad(cr, xc.x, ar);
-      ar = P::mad(-ci, xc.y, ar);
-      ai = P::mad(cr, xc.y, ai);
-      ai = P::mad(ci, xc.x, ai);
-    }
-    if (!rowflag[o]) {
-      zero_row(w, o);
-      continue;
-    }
-    const S is = sizeof(S) == 4 ? (S)s_isrf[a.stab[o]] : (S)s_isr[a.stab[o]];
-    store_row(w, o, ar * is, ai * is);
+__device__ __forceinline__ void block_matvec_tab_any(const BatchArgs& a, const typename P::V* x,
+                                                     const typename P::V* tchi, const typename P::V* pwc,
+                                                     const double* s_isr, const float* s_isrf,
+                                                     const uint8_t* __restrict__ rowflag, WT* __restrict__ w) {
+  if (a.gauge) {
+    if (a.tpr == 2) block_matvec_tab<P, true, 2>(a, x, tchi, pwc, s_isr, s_isrf, rowflag, w);
+    else block_matvec_tab<P, true, 1>(a, x, tchi, pwc, s_isr, s_isrf, rowflag, w);
+  } else {
+    if (a.tpr == 2) block_matvec_tab<P, false, 2>(a, x, tchi, pwc, s_isr, s_isrf, rowflag, w);
+    else block_matvec_tab<P, false, 1>(a, x, tchi, pwc, s_isr, s_isrf, rowflag, w);
   }
 }
 
@@ -1828,10 +1835,8 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       int jend = m;
       for (int j = k; j < m; ++j) {
         BV* vj = Vb + (size_t)j * a.ld;
-        if (a.use_tab && a.gauge)
-          block_matvec_tab_gauge<P>(a, x, s_tchi, s_isr, s_isrf, rowflag, W);
-        else if (a.use_tab)
-          block_matvec_tab<P>(a, x, s_tchi, s_pwc, s_isr, s_isrf, rowflag, W);
+        if (a.use_tab)
+          block_matvec_tab_any<P>(a, x, s_tchi, s_pwc, s_isr, s_isrf, rowflag, W);
         else
           block_matvec<P, FERMI, PHASES>(a, x, s_tchi, s_eta, s_isr, s_isrf, s_rank, s_rec, s_off, s_inv, rowflag, W,
                                          pcl);
@@ -2192,6 +2197,11 @@ struct BatchImpl {
   // the table's records carry signs only (gauge mode) rather than phase ids
   bool tab_gauge = false;
   bool gauge_enabled = true;  // use gauge mode whenever every request allows it
+  // launch shape: Krylov dimension and threads per row of the table matvec;
+  // pinned (pin_m / pin_tpr > 0) or chosen by the autotuner per catalog shape
+  bool m_fixed = false;
+  int m_cap = 24, pin_m = 0, pin_tpr = 0, last_m = 0, last_tpr = 0;
+  int tune_runs = 0;  // autotuner sweeps this batch object ran
   int last_gauge = 0;
   DevBuf gauge_w, bil_dev;  // [max_req][n_site] site gauges; [n_bil][2] term sites
   int last_tab = 0;
@@ -2714,12 +2724,14 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   SED_REQUIRE(n_bil >= 0 && n_bil < 65535, 5, "at most 65534 bilinear terms");
   SED_REQUIRE(n_bil == 0 || bil_ij, 1, "bilinear index array must not be NULL");
   SED_REQUIRE(n_den == 0 || (den_ij && den_v), 1, "density arrays must not be NULL");
-  if (krylovdim <= 0) krylovdim = 24;
   auto B = std::make_shared<BatchImpl>();
+  B->m_fixed = krylovdim > 0;  // else the autotuner picks the Krylov dimension
+  if (krylovdim <= 0) krylovdim = 24;
   B->cat = cp;
   B->precision = precision;
   B->nev = nev;
   B->m = std::min(std::max(krylovdim, 2 * (nev + 2) + 1), kMaxM);
+  B->m_cap = B->m_fixed ? B->m : std::max(B->m, std::min(28, kMaxM));
   B->max_req = max_req;
   B->n_bil = n_bil;
   B->n_den = n_den;
@@ -2800,7 +2812,7 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   B->smem = L.total;
   // per-block workspace, bounded to 16 GB
   // basis and restart buffers of equal capacity (they trade places), work vector, FP64 input
-  const size_t slots = (size_t)std::max(B->m + 1, 5 * (nev + 2));
+  const size_t slots = (size_t)std::max(B->m_cap + 1, 5 * (nev + 2));  // the largest Krylov dimension tried
   const size_t per_cta = (2 * slots + 2) * B->ld * 16 + (size_t)n_bil * G.n_ops * 16 + B->ld;
   ncta = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)ncta, (int64_t)max_req,
                                                       (int64_t)((16ull << 30) / std::max<size_t>(per_cta, 1))}));
@@ -2862,6 +2874,115 @@ static void validate_requests(BatchImpl& B, int n_req, const double* phase, cons
   for (int t = 1; t < nthr; ++t)
     if (first_bad[t] < first_bad[tb]) tb = t;
   if (first_bad[tb] != INT_MAX) throw err[tb];
+}
+
+// ------------------------------------------------------------ autotuner
+// The batched launch's shape -- threads per row of the hop-table matvec (1,
+// or a lane pair splitting each row's records) and, unless the caller fixed
+// it, the Krylov dimension m of the thick-restart Lanczos (20, 24 or 28) -- is
+// picked by measurement: on the first run of a catalog shape every candidate
+// solves one wave of the run's own requests (at most one request per resident
+// block), twice, timed with CUDA events on the batch stream, and the fastest
+// is kept for that shape for the whole process.  SED_BATCH_SHAPE="m,tpr" in
+// the environment or sed_batch_set_shape pins a shape.  Results depend on the
+// shape only within the solver's tolerance (the Krylov space and a row's
+// summation order change); a given shape is reproducible bit for bit.
+struct BatchShapeKey {
+  int64_t n_orb;
+  int n_terms, n_ops, n_site, fermi, precision, nev, use_tab, gauge, m_fixed_to;
+  bool operator<(const BatchShapeKey& o) const {
+    return std::tie(n_orb, n_terms, n_ops, n_site, fermi, precision, nev, use_tab, gauge, m_fixed_to) <
+           std::tie(o.n_orb, o.n_terms, o.n_ops, o.n_site, o.fermi, o.precision, o.nev, o.use_tab, o.gauge,
+                    o.m_fixed_to);
+  }
+};
+static std::mutex g_bshape_mu;
+static std::map<BatchShapeKey, std::pair<int, int>> g_bshapes;
+
+static bool env_batch_shape(int* m, int* tpr) {
+  const char* e = std::getenv("SED_BATCH_SHAPE");
+  if (!e) return false;
+  int a = 0, b = 0;
+  if (std::sscanf(e, "%d,%d", &a, &b) != 2 || (b != 1 && b != 2) || a < 2 || a > kMaxM) return false;
+  *m = a;
+  *tpr = b;
+  return true;
+}
+
+static void choose_shape(BatchImpl& B, BatchArgs& a, int n_req, cudaStream_t s) {
+  const int m_lo = 2 * (B.nev + 2) + 1;
+  auto clamp_m = [&](int m) { return std::min(std::max(m, m_lo), B.m_cap); };
+  int m = B.m, tpr = 1;
+  if (B.pin_m > 0) {
+    m = clamp_m(B.pin_m);
+    tpr = B.pin_tpr;
+  } else if (env_batch_shape(&m, &tpr)) {
+    m = B.m_fixed ? B.m : clamp_m(m);
+  } else {
+    const CatalogImpl& C = *B.cat;
+    const GroupImpl& G = *C.group;
+    const BatchShapeKey key{C.n_orbits, B.tt.n_terms, G.n_ops, G.n_site, B.fermi ? 1 : 0, B.precision, B.nev,
+                            a.use_tab, a.gauge, B.m_fixed ? B.m : 0};
+    bool found = false;
+    {
+      std::lock_guard<std::mutex> lock(g_bshape_mu);
+      auto it = g_bshapes.find(key);
+      if (it != g_bshapes.end()) {
+        m = it->second.first;
+        tpr = it->second.second;
+        found = true;
+      }
+    }
+    if (!found) {
+      std::vector<int> ms = B.m_fixed ? std::vector<int>{B.m} : std::vector<int>{24, 20, 28};
+      std::vector<int> tprs = a.use_tab ? std::vector<int>{1, 2} : std::vector<int>{1};
+      const int sample = std::min(n_req, B.n_cta);
+      cudaEvent_t e0, e1;
+      SED_CUDA(cudaEventCreate(&e0));
+      SED_CUDA(cudaEventCreate(&e1));
+      float best = 1e30f;
+      for (int mc : ms) {
+        mc = clamp_m(mc);
+        for (int tc : tprs) {
+          BatchArgs t = a;
+          t.m = mc;
+          t.tpr = tc;
+          t.n_req = sample;
+          t.evecs = nullptr;  // the trial runs write only the caller's scalar outputs, overwritten below
+          BatchSmem L;
+          int ncta = 1;
+          dispatch_prepare(B, t, L, ncta, B.precision == 0);
+          ncta = std::min(B.n_cta, sample);
+          float ms_best = 1e30f;
+          for (int rep = 0; rep < 2; ++rep) {
+            SED_CUDA(cudaMemsetAsync(B.queue.p, 0, 16, s));
+            SED_CUDA(cudaEventRecord(e0, s));
+            dispatch_launch(B, t, L, ncta, s, B.precision == 0);
+            SED_CUDA(cudaEventRecord(e1, s));
+            SED_CUDA(cudaEventSynchronize(e1));
+            float el = 0.f;
+            SED_CUDA(cudaEventElapsedTime(&el, e0, e1));
+            ms_best = std::min(ms_best, el);
+          }
+          if (ms_best < best) {
+            best = ms_best;
+            m = mc;
+            tpr = tc;
+          }
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      ++B.tune_runs;
+      std::lock_guard<std::mutex> lock(g_bshape_mu);
+      g_bshapes[key] = {m, tpr};
+    }
+  }
+  if (!a.use_tab) tpr = 1;
+  a.m = m;
+  a.tpr = tpr;
+  B.last_m = m;
+  B.last_tpr = tpr;
 }
 
 // Launch on device-resident buffers (asynchronous on the batch stream).
@@ -2933,6 +3054,8 @@ void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const doubl
     a.pwc64 = B.pwc64.as<double2>();
   }
   B.last_tab = a.use_tab;
+  a.tpr = 1;
+  choose_shape(B, a, n_req, s);
   BatchSmem L;
   int ncta = 1;
   dispatch_prepare(B, a, L, ncta, B.precision == 0);
@@ -3073,6 +3196,25 @@ int sed_batch_last_info(const sed_batch* b, int32_t* n_fallback, int32_t* hop_ta
   });
 }
 
+int sed_batch_set_shape(sed_batch* b, int krylovdim, int threads_per_row) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    SED_REQUIRE((krylovdim == 0 && threads_per_row == 0) ||
+                    (krylovdim >= 2 && krylovdim <= sed::kMaxM && (threads_per_row == 1 || threads_per_row == 2)),
+                1, "batch shape must be (0, 0) or (krylovdim <= 32, 1 or 2 threads per row)");
+    SED_REQUIRE(krylovdim <= b->p->m_cap, 1, "krylovdim above the batch's workspace (create it with that krylovdim)");
+    b->p->pin_m = krylovdim;
+    b->p->pin_tpr = threads_per_row;
+  });
+}
+int sed_batch_shape(const sed_batch* b, int32_t* krylovdim, int32_t* threads_per_row, int32_t* tune_runs) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    if (krylovdim) *krylovdim = b->p->last_m;
+    if (threads_per_row) *threads_per_row = b->p->last_tpr;
+    if (tune_runs) *tune_runs = b->p->tune_runs;
+  });
+}
 int sed_batch_set_site_gauge(sed_batch* b, int enable) {
   return bguard([&] {
     SED_REQUIRE(b, 1, "NULL batch");

@@ -283,3 +283,38 @@ def test_batch_eigenvectors(oracle, model, precision):
                 hi = ref[i + 1] if i + 1 < len(ref) else np.inf
                 if min(ref[i] - lo, hi - ref[i]) > 1e-6:
                     assert abs(abs(np.vdot(vs[:, i], V[:, i])) - 1.0) <= 1e-6, (model, b, i, precision)
+
+
+def test_batch_launch_autotuner(oracle):
+    """The first run of a catalog shape sweeps the candidate launch shapes
+    (threads per row 1 and 2 of the table matvec; Krylov dimensions 20, 24,
+    28) on one wave of its requests and keeps the fastest; a second solver of
+    the same shape reuses it without a sweep.  Every pinned shape solves the
+    same sectors to the oracle's dense spectrum, and agrees with the tuned one
+    within the mixed path's 1e-9."""
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.haldane_honeycomb(2, 4, tp=0.55)
+    reqs = flux_scan_requests(spec, TWISTS[:2])
+    s1 = _solver(spec, "mixed", nev=5)  # nev 5: a shape key no other test tunes first
+    tuned = s1.run(reqs)
+    sh = s1.shape()
+    assert sh["tune_runs"] == 1 and sh["threads_per_row"] in (1, 2) and sh["krylovdim"] in (20, 24, 28)
+    s2 = _solver(spec, "mixed", nev=5)
+    s2.run(reqs)
+    assert s2.shape()["tune_runs"] == 0 and s2.shape()["krylovdim"] == sh["krylovdim"]
+    nG = len(reqs) // 2
+    for m, tpr in ((20, 1), (24, 2), (28, 2)):
+        s2.set_shape(m, tpr)
+        out = s2.run(reqs)
+        assert s2.shape()["krylovdim"] == m and s2.shape()["threads_per_row"] == tpr
+        assert (out["status"] == 0).all()
+        ok = ~np.isnan(out["evals"])
+        np.testing.assert_allclose(out["evals"][ok], tuned["evals"][ok], rtol=1e-9, atol=1e-12)
+        for b in range(0, len(reqs), 3):
+            _, sec, op = oracle_objects(oracle, Case("haldane2x4_tp", spec, theta=TWISTS[b // nG]), b % nG)
+            if sec.dim == 0:
+                continue
+            ref = np.linalg.eigvalsh(op.dense())
+            assert_lanczos_spectrum(out["evals"][b, :min(5, sec.dim)], ref, 1e-9 * max(1.0, abs(ref[0])))
+    s2.set_shape(0, 0)
