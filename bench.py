@@ -333,6 +333,7 @@ def run_ours(args, rank, world):
     t0 = time.perf_counter()
     r64 = solver64.run_packed(chi, ph, amp, seeds)
     fp64_batch_s = time.perf_counter() - t0
+    shape64 = solver64.shape()
     ev64 = r64["evals"]
     rel = np.abs(ev_mixed - ev64) / np.maximum(np.abs(ev64), 1e-300)
     max_rel = float(np.nanmax(rel))
@@ -416,7 +417,7 @@ def run_ours(args, rank, world):
         "launch_shape": solver.shape(), "site_gauge": stats["site_gauge"],
         "clocks": clocks,
         "plain_fp64_dropin": plain,
-        "fp64_batched": {"solves_per_s": n / fp64_batch_s, "launch_shape": solver64.shape()},
+        "fp64_batched": {"solves_per_s": n / fp64_batch_s, "launch_shape": shape64},
         "speedup_vs_plain_fp64": value / plain["solves_per_s"] if plain else None,
         "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99))},
         "max_rel_dE_mixed_vs_fp64": max_rel,

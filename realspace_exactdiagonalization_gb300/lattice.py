@@ -10,12 +10,13 @@ be generated without it:
 * a representative bond ``((cell_a, sub_a), (cell_b, sub_b)) => t`` added with
   ``is_hermitian=True`` is translated over every unit cell of the periodic
   sample, and its Hermitian partner is added with ``conj(t)``;
-* bonds that land on the same ordered site pair are **summed**.  This is the
-  semantics that reproduces the reference's stored numbers for samples with a
-  side of length 2, where a bond and the partner of a translated bond coincide
-  (tests/test_oracle_golden.py pins it against the Haldane 2x3 projection-table
-  size and the Hubbard 2xL ground energies of
-  ``benchmark/benchmark_data/benchmark_raw.csv``);
+* bonds that land on the same ordered site pair with the same winding are
+  **summed**; bonds on the same pair with different windings stay separate
+  terms (their twist phases differ).  This is the semantics that reproduces
+  the reference's stored numbers for samples with a side of length 2, where a
+  bond and the partner of a translated bond coincide (tests/test_oracle_golden.py
+  pins it against the Haldane 2x3 projection-table size and the Hubbard 2xL
+  ground energies of ``benchmark/benchmark_data/benchmark_raw.csv``);
 * twisted boundary phases follow the reference's docstring
   (``src/second_quantized_model.jl:29-37``): the hop from site ``i`` to site
   ``j`` is multiplied by ``exp(i 2 pi theta_d w_d)`` where ``w_d`` is the
