@@ -2192,6 +2192,8 @@ struct BatchImpl {
   std::vector<uint64_t> tab_fmask;  // [G][3] family class masks of the table
   std::vector<int8_t> tab_rep;      // [G][4] class representative sites
   std::vector<int32_t> row_cnt;     // hops per orbit row
+  std::vector<uint32_t> h_sl_off;   // host copies of the slice offsets and widths
+  std::vector<int32_t> h_sl_w;
   DevBuf hop, sl_off, sl_w, phi_desc, rep_site, pwc64, fmask_dev;
   int64_t hop_records = 0;
   // the table's records carry signs only (gauge mode) rather than phase ids
@@ -2572,6 +2574,145 @@ static bool site_gauges(const GroupImpl& G, int n_req, const double* phase, std:
 // only and serve every run; otherwise they carry phase ids of this run's phase
 // classes.  Returns whether the run can use the table.  phase is the host copy
 // of the requests' group phases.
+// Bank-aware order of each row's records.  Step k of a warp's pass over a
+// slice gathers, for its 32 rows' k-th records, x[col] and the coefficient
+// (and, with phase classes, the phase-id coefficient) from shared memory.
+// An E-byte gather is served 128 / E lanes at a time, and each further
+// distinct word that falls into an already used bank group (E consecutive
+// bytes of the 32 banks) costs one more shared-memory wavefront; with random
+// columns that is about 5 wavefronts per gather, where 2 would do, and these
+// gathers bound the matvec on the L1 data pipe.  A row's records may be summed
+// in any order and its padding slots may sit anywhere, so the host reorders
+// every slice greedily, step by step: each lane takes the remaining record
+// that raises the worst bank-group load of its lane group least (ties: the
+// emptier bank groups), padding where that is cheaper and the row can still
+// place the rest.  A padding record's coefficient is zero, so it takes a
+// column another lane of its group reads (no extra word).
+//   elem: bytes per gathered element (8 complex64, 16 complex128);
+//   use_x: x is in shared memory (else only the coefficient gathers count);
+//   use_p: records carry phase ids whose coefficients are gathered too;
+//   pad_hi: bits 24.. of a padding record (its coefficient and phase id).
+static void bank_schedule(std::vector<uint64_t>& recs, const std::vector<uint32_t>& off,
+                          const std::vector<int32_t>& width, int64_t n_orb, int elem, bool use_x, bool use_p,
+                          uint64_t pad_hi) {
+  const int G = 128 / elem;  // lanes per wavefront and bank groups per wavefront
+  constexpr int kMaxG = 16;
+  struct Bins {
+    uint32_t word[kMaxG][kMaxG];
+    int cnt[kMaxG];
+    int mx;
+    void clear(int g) {
+      for (int b = 0; b < g; ++b) cnt[b] = 0;
+      mx = 0;
+    }
+    // (raise of the worst load, load after) when `w` is added
+    void cost(uint32_t w, int g, int& raise, int& load) const {
+      const int b = (int)(w % (uint32_t)g);
+      for (int i = 0; i < cnt[b]; ++i)
+        if (word[b][i] == w) {
+          raise = 0;
+          load = cnt[b];
+          return;
+        }
+      load = cnt[b] + 1;
+      raise = load > mx ? load - mx : 0;
+    }
+    void add(uint32_t w, int g) {
+      const int b = (int)(w % (uint32_t)g);
+      for (int i = 0; i < cnt[b]; ++i)
+        if (word[b][i] == w) return;
+      word[b][cnt[b]++] = w;
+      if (cnt[b] > mx) mx = cnt[b];
+    }
+  };
+  const uint32_t pad_t = (uint32_t)(pad_hi & 0x3FFFFu), pad_p = (uint32_t)(pad_hi >> 18);
+  const int n_arr = (use_x ? 1 : 0) + 1 + (use_p ? 1 : 0);
+  const int64_t n_sl = (int64_t)off.size();
+  std::vector<std::vector<uint64_t>> rem(32);
+  for (int64_t sl = 0; sl < n_sl; ++sl) {
+    const int W = width[sl];
+    const int lanes = (int)std::min<int64_t>(32, n_orb - sl * 32);  // lanes past the last row never load
+    uint64_t* base = recs.data() + off[sl];
+    for (int l = 0; l < lanes; ++l) {
+      rem[l].clear();
+      for (int k = 0; k < W; ++k) {
+        const uint64_t r = base[32 * (size_t)k + l];
+        if ((r >> 24) != pad_hi) rem[l].push_back(r);
+      }
+    }
+    Bins bx, bt, bp;
+    for (int k = 0; k < W; ++k) {
+      for (int g0 = 0; g0 < lanes; g0 += G) {
+        bx.clear(G);
+        bt.clear(G);
+        bp.clear(G);
+        int pads[kMaxG], n_pads = 0;
+        uint32_t any_col = 0;
+        bool have_col = false;
+        for (int l = g0; l < std::min(lanes, g0 + G); ++l) {
+          std::vector<uint64_t>& rl = rem[l];
+          const bool may_pad = (int)rl.size() < W - k;
+          // the best real record: least raise of a worst load, then least load
+          int best = -1, best_raise = INT_MAX, best_load = INT_MAX;
+          for (int i = 0; i < (int)rl.size(); ++i) {
+            const uint64_t r = rl[i];
+            int ra = 0, lo = 0, r1, l1;
+            if (use_x) {
+              bx.cost((uint32_t)(r & 0xFFFFFFu), G, r1, l1);
+              ra += r1;
+              lo += l1;
+            }
+            bt.cost((uint32_t)(r >> 24) & 0x3FFFFu, G, r1, l1);
+            ra += r1;
+            lo += l1;
+            if (use_p) {
+              bp.cost((uint32_t)(r >> 42), G, r1, l1);
+              ra += r1;
+              lo += l1;
+            }
+            if (ra < best_raise || (ra == best_raise && lo < best_load)) {
+              best = i;
+              best_raise = ra;
+              best_load = lo;
+              if (ra == 0 && lo == n_arr) break;  // every word alone in its bank group
+            }
+          }
+          // padding only where it raises a worst load less than the best real
+          // record does (padding is cheapest at the end of a slice, where
+          // every lane pads together)
+          if (may_pad && best >= 0) {
+            int r1, l1, r2 = 0, l2 = 0;
+            bt.cost(pad_t, G, r1, l1);
+            if (use_p) bp.cost(pad_p, G, r2, l2);
+            if (r1 + r2 < best_raise) best = -1;
+          }
+          uint64_t* dst = base + 32 * (size_t)k + l;
+          if (best < 0) {
+            pads[n_pads++] = l;
+            bt.add(pad_t, G);
+            if (use_p) bp.add(pad_p, G);
+            continue;
+          }
+          const uint64_t r = rl[best];
+          rl[best] = rl.back();
+          rl.pop_back();
+          *dst = r;
+          if (use_x) bx.add((uint32_t)(r & 0xFFFFFFu), G);
+          bt.add((uint32_t)(r >> 24) & 0x3FFFFu, G);
+          if (use_p) bp.add((uint32_t)(r >> 42), G);
+          if (!have_col) any_col = (uint32_t)(r & 0xFFFFFFu), have_col = true;
+        }
+        for (int i = 0; i < n_pads; ++i) base[32 * (size_t)k + pads[i]] = (pad_hi << 24) | any_col;
+      }
+    }
+  }
+}
+
+static bool bank_order_enabled() {
+  const char* e = std::getenv("SED_BATCH_BANK_ORDER");
+  return !(e && e[0] == '0');
+}
+
 static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStream_t s, bool gauge) {
   if (B.phi_cap == 0 || !B.tab_enabled) return false;
   const CatalogImpl& C = *B.cat;
@@ -2624,6 +2765,8 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
     B.hop.alloc((size_t)std::max<int64_t>(tot, 1) * 8);
     upload(B.sl_off, off, s);
     upload(B.sl_w, w, s);
+    B.h_sl_off = off;
+    B.h_sl_w = w;
     B.hop_records = tot;
     B.row_cnt.swap(row_cnt);  // the slices exist from here on
   }
@@ -2671,6 +2814,9 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
                   5, "internal error: hop-table record out of range");
       recs[t] = pad ? (n_tchi << 24) | (2ULL << 42) : (recs[t] & ((1ULL << 42) - 1)) | ((uint64_t)(keys[t] >> 24) << 42);
     }
+    if (bank_order_enabled())
+      bank_schedule(recs, B.h_sl_off, B.h_sl_w, C.n_orbits, B.precision == 1 ? 8 : 16, B.x_smem && B.precision == 1,
+                    false, n_tchi | (2ULL << 18));
     SED_CUDA(cudaMemcpyAsync(B.hop.p, recs.data(), (size_t)tot * 8, cudaMemcpyHostToDevice, s));
     SED_CUDA(cudaStreamSynchronize(s));
     B.n_phi = 2;
@@ -2701,6 +2847,9 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
     const uint64_t phi = pad ? zero_id : id[keys[t]];
     recs[t] = (pad ? 0 : recs[t] & ((1ULL << 42) - 1)) | (phi << 42);
   }
+  if (bank_order_enabled())
+    bank_schedule(recs, B.h_sl_off, B.h_sl_w, C.n_orbits, B.precision == 1 ? 8 : 16, B.x_smem && B.precision == 1,
+                  true, zero_id << 18);
   SED_CUDA(cudaMemcpyAsync(B.hop.p, recs.data(), (size_t)tot * 8, cudaMemcpyHostToDevice, s));
   upload(B.phi_desc, desc, s);
   B.n_phi = (int)desc.size();
@@ -2937,6 +3086,7 @@ static void choose_shape(BatchImpl& B, BatchArgs& a, int n_req, cudaStream_t s) 
       std::vector<int> ms = B.m_fixed ? std::vector<int>{B.m} : std::vector<int>{24, 20, 28};
       std::vector<int> tprs = a.use_tab ? std::vector<int>{1, 2} : std::vector<int>{1};
       const int sample = std::min(n_req, B.n_cta);
+      std::vector<int64_t> tns((size_t)sample * 2);
       cudaEvent_t e0, e1;
       SED_CUDA(cudaEventCreate(&e0));
       SED_CUDA(cudaEventCreate(&e1));
@@ -2953,16 +3103,28 @@ static void choose_shape(BatchImpl& B, BatchArgs& a, int n_req, cudaStream_t s) 
           int ncta = 1;
           dispatch_prepare(B, t, L, ncta, B.precision == 0);
           ncta = std::min(B.n_cta, sample);
+          // score: the mean request duration from the kernel's own per-request
+          // timestamps. A multi-wave launch's throughput follows the mean,
+          // whereas one wave's wall time is set by its slowest request.
           float ms_best = 1e30f;
           for (int rep = 0; rep < 2; ++rep) {
             SED_CUDA(cudaMemsetAsync(B.queue.p, 0, 16, s));
             SED_CUDA(cudaEventRecord(e0, s));
             dispatch_launch(B, t, L, ncta, s, B.precision == 0);
             SED_CUDA(cudaEventRecord(e1, s));
-            SED_CUDA(cudaEventSynchronize(e1));
+            SED_CUDA(cudaMemcpyAsync(tns.data(), t.t_ns, (size_t)sample * 16, cudaMemcpyDeviceToHost, s));
+            SED_CUDA(cudaStreamSynchronize(s));
             float el = 0.f;
             SED_CUDA(cudaEventElapsedTime(&el, e0, e1));
-            ms_best = std::min(ms_best, el);
+            double sum = 0.0;
+            int cnt = 0;
+            for (int i = 0; i < sample; ++i) {
+              const int64_t d = tns[2 * (size_t)i + 1] - tns[2 * (size_t)i];
+              if (d > 0) sum += (double)d, ++cnt;
+            }
+            // the event time stands in when no request was timed (all sectors empty)
+            const float score = cnt ? (float)(sum / cnt * 1e-6) : el;
+            ms_best = std::min(ms_best, score);
           }
           if (ms_best < best) {
             best = ms_best;

@@ -147,7 +147,7 @@ class SectorServer:
                  large_workers: int = 3, max_batch: int = 512, small_max_orbits: int = SMALL_MAX_ORBITS,
                  precision: str = "mixed", tol: float = 1e-10, nev: int = 1,
                  medium_max_orbits: int = MEDIUM_MAX_ORBITS, medium_lanes: int = 1,
-                 priority_max_orbits: int = PRIORITY_MAX_ORBITS):
+                 priority_max_orbits: int = PRIORITY_MAX_ORBITS, warm_up: bool = True):
         self.budget = float(budget_bytes)
         self.priority_max_orbits = priority_max_orbits
         self.precision = precision
@@ -189,6 +189,29 @@ class SectorServer:
         self._t0 = 0.0
         self._threads: List[threading.Thread] = []
         self.peak_reserved = 0.0
+        if warm_up:
+            self.warm_up()
+
+    def warm_up(self, max_wave: int = 152) -> None:
+        """Before any request arrives, run one wave of every batched family's
+        own sectors (its momenta at a few twists) through each of its lanes:
+        every lane builds its hop table, and the first run of the catalog
+        shape lets the launch autotuner pick the batch's launch shape (its
+        trial launches take a few seconds per family).  Served requests then
+        wait for neither.  Results of the warm-up are discarded."""
+        for fam in self.families.values():
+            if fam.route == "large":
+                continue
+            lat = fam.spec.lattice
+            nk = lat.sample_size[0] * lat.sample_size[1]
+            n = min(max_wave, fam.solvers[0].max_requests, int(fam.solvers[0].info()["blocks"]))
+            twists = [(0.0, 0.0), (0.5, 0.25 if lat.sample_size[1] > 1 else 0.0),
+                      (0.25, 0.75 if lat.sample_size[1] > 1 else 0.0), (0.75, 0.5 if lat.sample_size[1] > 1 else 0.0)]
+            reqs = [Request(-1 - i, fam.name, i % nk, twists[(i // nk) % len(twists)], 1, 0x5EED0000 + i)
+                    for i in range(n)]
+            arrays = self._request_arrays(fam, reqs)
+            for solver in fam.solvers:
+                solver.run(arrays, tol=self.tol)
 
     # ------------------------------------------------------------ workers
     def _now(self) -> float:

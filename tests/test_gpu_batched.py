@@ -238,6 +238,37 @@ def test_site_gauge_matches_phase_classes(model, precision):
     np.testing.assert_array_equal(again["evals"], on["evals"])
 
 
+@pytest.mark.parametrize("gauge", [True, False])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("model", ["haldane2x4", "checkerboard3x2_f"])
+def test_bank_ordered_records_solve_the_same_sectors(monkeypatch, model, precision, gauge):
+    """The hop table's records are reordered within each row so that a warp's
+    shared-memory gathers fall into different bank groups
+    (SED_BATCH_BANK_ORDER=0 keeps the fill order).  Only the summation order
+    of a row changes: both orders give the same sectors and eigenvalues within
+    the path's tolerance (1e-9 relative mixed, 1e-11 FP64), in site-gauge and
+    in phase-class mode."""
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = {"haldane2x4": lambda: L.haldane_honeycomb(2, 4),
+            "checkerboard3x2_f": lambda: L.checkerboard(3, 2, n_filled=4)}[model]()
+    reqs = flux_scan_requests(spec, TWISTS)
+    out = {}
+    for order in ("1", "0"):
+        monkeypatch.setenv("SED_BATCH_BANK_ORDER", order)
+        solver = _solver(spec, precision)
+        solver.set_site_gauge(gauge)
+        out[order] = solver.run(reqs)
+        st = solver.last_stats()
+        assert st["hop_table"] and st["site_gauge"] == gauge
+        assert (out[order]["status"] == 0).all()
+    np.testing.assert_array_equal(out["1"]["dims"], out["0"]["dims"])
+    ok = ~np.isnan(out["0"]["evals"])
+    np.testing.assert_array_equal(ok, ~np.isnan(out["1"]["evals"]))
+    tol = 1e-9 if precision == "mixed" else 1e-11
+    np.testing.assert_allclose(out["1"]["evals"][ok], out["0"]["evals"][ok], rtol=tol, atol=1e-12)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("model", ["haldane2x4", "checkerboard3x2_f"])
 def test_batch_eigenvectors(oracle, model, precision):

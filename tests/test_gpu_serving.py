@@ -52,6 +52,24 @@ def test_served_mix_matches_oracle_and_alone(oracle, ring_route):
             (r.rid, r.family, alone.evals, r.evals)
 
 
+def test_warm_up_leaves_no_tuning_to_requests():
+    """The server's warm-up runs every batched family's lanes once at setup,
+    so the launch autotuner's trial launches (and the hop-table builds) are
+    behind it: no served batch runs the autotuner."""
+    from realspace_exactdiagonalization_gb300.serving import SectorServer, random_requests
+
+    fams = _families()
+    srv = SectorServer(fams, budget_bytes=8e9, batch_lanes=2, large_workers=1, small_max_orbits=300)
+    batch = [f for f in srv.families.values() if f.route == "batch"]
+    assert batch
+    before = {(f.name, i): s.shape()["tune_runs"] for f in batch for i, s in enumerate(f.solvers)}
+    assert all(s.shape()["krylovdim"] > 0 for f in batch for s in f.solvers)
+    done = srv.serve(random_requests(fams, 24, rate=0.0, seed=11, nev=1))
+    assert all(r.status == 0 for r in done)
+    after = {(f.name, i): s.shape()["tune_runs"] for f in batch for i, s in enumerate(f.solvers)}
+    assert after == before
+
+
 def test_op_priority_keeps_results():
     """sed_op_set_priority moves the operator to a stream of the device's
     greatest (or least) priority; the solve gives the same bits, and a
