@@ -297,7 +297,11 @@ int sed_solve(sed_op* op, int nev, double tol, int maxiter, int krylovdim, uint6
  * request that stagnates at the complex64 noise floor is re-solved by the
  * FP64 kernel in a second launch.  Outputs per request: nev
  * eigenvalues (ascending), status (0 ok, SED_ERR_NOT_CONVERGED), sector
- * dimension, |E_polished - E_c64| and the matvec count. */
+ * dimension, |E_polished - E_c64| and the matvec count.  The batch runs
+ * Lanczos at every sector size (no dense branch for dimensions <= 500, unlike
+ * sed_solve), so like the reference's KrylovKit branch it may list an exactly
+ * degenerate level fewer times than its multiplicity; solve a small sector
+ * with sed_solve to get every copy. */
 typedef struct sed_batch sed_batch;
 /* krylovdim: the Lanczos basis size (0: chosen by the autotuner, see
  * sed_batch_set_shape). */

@@ -38,7 +38,12 @@ class BatchedSectorSolver:
     the pair list).  ``precision="mixed"`` runs complex64 matvecs with FP64
     Lanczos and an FP64 Rayleigh-Ritz polish; ``"fp64"`` is all FP64.
     ``krylovdim=0`` lets the launch autotuner choose the Krylov dimension
-    (with the matvec's threads per row); a positive value fixes it."""
+    (with the matvec's threads per row); a positive value fixes it.
+
+    Every sector is solved by Lanczos, whatever its size (the reference and
+    ``MatrixFreeHamiltonian.solve`` take a dense solve up to 500 rows), so an
+    exactly degenerate level may be listed fewer times than its multiplicity,
+    as in the reference's KrylovKit branch."""
 
     def __init__(self, catalog: Symmetry_Orbit_Catalog, bilinear_pairs, density_terms, precision: str = "mixed",
                  nev: int = 4, krylovdim: int = 0, max_requests: int = 1024):

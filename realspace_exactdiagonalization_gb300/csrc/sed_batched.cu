@@ -75,6 +75,12 @@ struct BatchArgs {
   // table entry times the sign its record carries (phase id 0: +, 1: -)
   int gauge;
   int tpr;                 // threads per row of the hop-table matvec (1 or 2)
+  // coefficient table: tchi_n entries (a prime >= n_bil * G + 1).  Hop-table
+  // runs store entry i (term k = i / G, element i % G; i = n_bil * G is the
+  // padding records' zero) at (i * tchi_mul) mod tchi_n, which spreads the
+  // entries that one warp step gathers over the shared-memory bank groups;
+  // on-the-fly runs store it at i.
+  int tchi_n, tchi_mul;
   const double2* gauge_w;  // [n_req][N]
   const int32_t* bil_dev;  // [n_bil][2] (from, to) sites of the bilinear terms
   const uint64_t* hop;
@@ -111,8 +117,8 @@ static BatchSmem batch_layout(const BatchArgs& a, bool x_in_smem) {
   auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
   L.x = o;
   o = al(o + (x_in_smem ? (size_t)a.n_orb * sizeof(VT) : 0));
-  L.tchi = o;  // n_bil * G coefficients and a zero entry for padding records
-  o = al(o + ((size_t)a.n_bil * a.G + 1) * sizeof(VT));
+  L.tchi = o;  // n_bil * G coefficients and a zero entry for padding records, tchi_n slots
+  o = al(o + (size_t)a.tchi_n * sizeof(VT));
   L.eta = o;
   o = al(o + (size_t)a.G * a.N * sizeof(VT));
   L.chi64 = o;
@@ -596,6 +602,31 @@ __device__ __forceinline__ double flip_sign(double v, uint32_t f) {
   return __longlong_as_double(__double_as_longlong(v) ^ ((unsigned long long)f << 32));
 }
 
+// one hop of the table matvec: coefficient and column value from shared
+// memory, accumulated into (ar, ai)
+template <class P, bool GAUGE>
+__device__ __forceinline__ void hop_acc(uint64_t r, const typename P::V* x, const typename P::V* tchi,
+                                        const typename P::V* pwc, typename P::S& ar, typename P::S& ai) {
+  using V = typename P::V;
+  using S = typename P::S;
+  const V t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
+  const V xc = x[(uint32_t)r & 0xFFFFFFu];
+  S cr, ci;
+  if (GAUGE) {
+    const uint32_t f = ((uint32_t)(r >> 42) & 1u) << 31;
+    cr = flip_sign(t.x, f);
+    ci = flip_sign(t.y, f);
+  } else {
+    const V ph = pwc[(uint32_t)(r >> 42)];
+    cr = P::mad(t.x, ph.x, -t.y * ph.y);
+    ci = P::mad(t.x, ph.y, t.y * ph.x);
+  }
+  ar = P::mad(cr, xc.x, ar);
+  ar = P::mad(-ci, xc.y, ar);
+  ai = P::mad(cr, xc.y, ai);
+  ai = P::mad(ci, xc.x, ai);
+}
+
 // The same matvec through the hop table: one coalesced 8-byte record per hop
 // (row 32s + l of slice s at sl_off[s] + 32k + l), then the column value and
 // the coefficient from shared memory; the records carry the signs and
@@ -609,7 +640,10 @@ __device__ __forceinline__ double flip_sign(double v, uint32_t f) {
 // TPR threads share a row (1, or 2: a lane pair splits the row's records by
 // parity and combines by a shuffle; 16 rows per warp), the batched launch's
 // threads-per-row shape, chosen by the autotuner.  Passes are uniform over the
-// block, so the pair shuffle never meets an exited lane.
+// block, so the pair shuffle never meets an exited lane.  The next pass's
+// slice offset and width are loaded a pass ahead, and a row's flag and
+// stabilizer order before its records: the row then waits on one L2 round
+// trip (its first records) instead of three.
 template <class P, bool GAUGE, int TPR, class WT>
 __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typename P::V* x,
                                                  const typename P::V* tchi, const typename P::V* pwc,
@@ -619,14 +653,28 @@ __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typen
   using S = typename P::S;
   const int sub = TPR == 1 ? 0 : (threadIdx.x & (TPR - 1));
   const int64_t rows_per_pass = blockDim.x / TPR;
-  for (int64_t base = 0; base < a.n_orb; base += rows_per_pass) {
-    const int64_t o = base + threadIdx.x / TPR;
+  int64_t o = threadIdx.x / TPR;
+  uint32_t off = 0;
+  int wdt = 0;
+  if (o < a.n_orb) {
+    off = a.sl_off[o >> 5];
+    wdt = a.sl_w[o >> 5];
+  }
+  for (; o - threadIdx.x / TPR < a.n_orb; o += rows_per_pass) {
     const bool valid = o < a.n_orb;
+    const int64_t o_next = o + rows_per_pass;
+    uint32_t off_next = 0;
+    int wdt_next = 0;
+    if (o_next < a.n_orb) {
+      off_next = a.sl_off[o_next >> 5];
+      wdt_next = a.sl_w[o_next >> 5];
+    }
     S ar = 0, ai = 0;
+    uint8_t flag = 0, st = 0;
     if (valid) {
-      const int64_t sl = o >> 5;
-      const uint64_t* rp = a.hop + a.sl_off[sl] + (o & 31);
-      const int wdt = a.sl_w[sl];
+      flag = rowflag[o];
+      st = a.stab[o];
+      const uint64_t* rp = a.hop + off + (o & 31);
       if (sub == 0) {
         const double2 dg = a.diag[o];
         const V xo = x[o];
@@ -634,36 +682,20 @@ __device__ __forceinline__ void block_matvec_tab(const BatchArgs& a, const typen
         ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
       }
 #pragma unroll 8
-      for (int k = sub; k < wdt; k += TPR) {
-        const uint64_t r = __ldg(rp + 32 * k);
-        const V t = tchi[(uint32_t)(r >> 24) & 0x3FFFFu];
-        const V xc = x[(uint32_t)r & 0xFFFFFFu];
-        S cr, ci;
-        if (GAUGE) {
-          const uint32_t f = ((uint32_t)(r >> 42) & 1u) << 31;
-          cr = flip_sign(t.x, f);
-          ci = flip_sign(t.y, f);
-        } else {
-          const V ph = pwc[(uint32_t)(r >> 42)];
-          cr = P::mad(t.x, ph.x, -t.y * ph.y);
-          ci = P::mad(t.x, ph.y, t.y * ph.x);
-        }
-        ar = P::mad(cr, xc.x, ar);
-        ar = P::mad(-ci, xc.y, ar);
-        ai = P::mad(cr, xc.y, ai);
-        ai = P::mad(ci, xc.x, ai);
-      }
+      for (int k = sub; k < wdt; k += TPR) hop_acc<P, GAUGE>(__ldg(rp + 32 * k), x, tchi, pwc, ar, ai);
     }
+    off = off_next;
+    wdt = wdt_next;
     if (TPR == 2) {
       ar += __shfl_xor_sync(0xFFFFFFFFu, ar, 1);
       ai += __shfl_xor_sync(0xFFFFFFFFu, ai, 1);
     }
     if (!valid || sub != 0) continue;
-    if (!rowflag[o]) {
+    if (!flag) {
       zero_row(w, o);
       continue;
     }
-    const S is = sizeof(S) == 4 ? (S)s_isrf[a.stab[o]] : (S)s_isr[a.stab[o]];
+    const S is = sizeof(S) == 4 ? (S)s_isrf[st] : (S)s_isr[st];
     store_row(w, o, ar * is, ai * is);
   }
 }
@@ -1589,7 +1621,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
   BV* Rb = reinterpret_cast<BV*>(a.R + (size_t)blockIdx.x * slots * a.ld);
   BV* W = reinterpret_cast<BV*>(a.W + (size_t)blockIdx.x * a.ld);
   double2* X64 = a.X64 + (size_t)blockIdx.x * a.ld;
-  double2* tchi64 = a.tchi64 + (size_t)blockIdx.x * ((size_t)a.n_bil * a.G + 1);
+  double2* tchi64 = a.tchi64 + (size_t)blockIdx.x * a.tchi_n;
   uint8_t* rowflag = a.rowflag + (size_t)blockIdx.x * a.ld;
   double2* pwc64 = a.pwc64 ? a.pwc64 + (size_t)blockIdx.x * a.phi_cap : nullptr;
   V* x = X_SMEM ? s_x : reinterpret_cast<V*>(X64);
@@ -1745,16 +1777,17 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         const double2 c = make_double2(c0.x * bk.x + c0.y * bk.y, c0.y * bk.x - c0.x * bk.y);  // chi conj(base^k)
         v = make_double2(t.x * c.x + t.y * c.y, t.x * c.y - t.y * c.x);                       // conj(t) chi'
       }
+      const int pos = a.use_tab ? (int)((uint64_t)i * (uint64_t)a.tchi_mul % (uint64_t)a.tchi_n) : i;
       if (a.use_tab) {  // double-float pairs for the table-path polish
         float4 vd;
         d_to_df(v.x, vd.x, vd.z);
         d_to_df(v.y, vd.y, vd.w);
-        reinterpret_cast<float4*>(tchi64)[i] = vd;
+        reinterpret_cast<float4*>(tchi64)[pos] = vd;
       } else {
-        tchi64[i] = v;
+        tchi64[pos] = v;
       }
-      s_tchi[i].x = v.x;
-      s_tchi[i].y = v.y;
+      s_tchi[pos].x = v.x;
+      s_tchi[pos].y = v.y;
     }
     const PhaseClasses<V> pcl{pmode, a.kp1, s_mask, reinterpret_cast<const V*>(sizeof(V) == 8 ? (void*)s_pw32 : (void*)s_pw64)};
     const PhaseClasses<double2> pcl64{pmode, a.kp1, s_mask, s_pw64};
@@ -2178,6 +2211,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
 struct BatchImpl {
   std::shared_ptr<CatalogImpl> cat;
   int precision = 1, nev = 4, m = 30, max_req = 0, n_bil = 0, n_den = 0, n_cta = 1;
+  int tchi_n = 1, tchi_mul = 1;  // coefficient table slots (prime) and hashing multiplier
   std::vector<int32_t> bil_ij;
   TermTables tt;
   DevBuf site_off, rec, diag, V, R, W, X64, tchi64, rowflag;
@@ -2306,6 +2340,8 @@ static BatchArgs base_args(BatchImpl& B) {
   a.kp1 = C.n_filled + 1;
   a.phi_cap = B.phi_cap;
   a.bil_dev = B.bil_dev.as<int32_t>();
+  a.tchi_n = B.tchi_n;
+  a.tchi_mul = B.tchi_mul;
   return a;
 }
 
@@ -2583,56 +2619,140 @@ static bool site_gauges(const GroupImpl& G, int n_req, const double* phase, std:
 // columns that is about 5 wavefronts per gather, where 2 would do, and these
 // gathers bound the matvec on the L1 data pipe.  A row's records may be summed
 // in any order and its padding slots may sit anywhere, so the host reorders
-// every slice greedily, step by step: each lane takes the remaining record
-// that raises the worst bank-group load of its lane group least (ties: the
-// emptier bank groups), padding where that is cheaper and the row can still
-// place the rest.  A padding record's coefficient is zero, so it takes a
-// column another lane of its group reads (no extra word).
+// every slice, step by step and lane group by lane group:
+//   - greedily: each lane takes the remaining record that raises the worst
+//     bank-group load of its group least (ties: the emptier bank groups),
+//     padding only where that raises it less than any record and the row can
+//     still place the rest;
+//   - then kBankRounds rounds of coordinate descent: each lane in turn puts
+//     its pick back and chooses again against the others' picks.
+// A padding record's coefficient is zero, so it takes a column another lane
+// of its group reads (no extra word).  Slices are independent and are spread
+// over up to eight host threads.
 //   elem: bytes per gathered element (8 complex64, 16 complex128);
 //   use_x: x is in shared memory (else only the coefficient gathers count);
 //   use_p: records carry phase ids whose coefficients are gathered too;
 //   pad_hi: bits 24.. of a padding record (its coefficient and phase id).
-static void bank_schedule(std::vector<uint64_t>& recs, const std::vector<uint32_t>& off,
-                          const std::vector<int32_t>& width, int64_t n_orb, int elem, bool use_x, bool use_p,
-                          uint64_t pad_hi) {
-  const int G = 128 / elem;  // lanes per wavefront and bank groups per wavefront
-  constexpr int kMaxG = 16;
-  struct Bins {
-    uint32_t word[kMaxG][kMaxG];
-    int cnt[kMaxG];
-    int mx;
-    void clear(int g) {
-      for (int b = 0; b < g; ++b) cnt[b] = 0;
-      mx = 0;
-    }
-    // (raise of the worst load, load after) when `w` is added
-    void cost(uint32_t w, int g, int& raise, int& load) const {
-      const int b = (int)(w % (uint32_t)g);
-      for (int i = 0; i < cnt[b]; ++i)
-        if (word[b][i] == w) {
-          raise = 0;
-          load = cnt[b];
-          return;
+static constexpr int kBankRounds = 4;
+
+namespace {
+constexpr int kMaxLaneGroup = 16;
+// distinct words per bank group of one lane group's gather, with use counts
+struct BankBins {
+  uint32_t word[kMaxLaneGroup][kMaxLaneGroup];
+  int uses[kMaxLaneGroup][kMaxLaneGroup];
+  int cnt[kMaxLaneGroup];
+  int g = 16;
+  void clear(int groups) {
+    g = groups;
+    for (int b = 0; b < g; ++b) cnt[b] = 0;
+  }
+  int worst() const {
+    int m = 0;
+    for (int b = 0; b < g; ++b) m = std::max(m, cnt[b]);
+    return m;
+  }
+  // raise of the worst load `mx` and the bank group's load after adding w
+  void cost(uint32_t w, int mx, int& raise, int& load) const {
+    const int b = (int)(w % (uint32_t)g);
+    for (int i = 0; i < cnt[b]; ++i)
+      if (word[b][i] == w) {
+        raise = 0;
+        load = cnt[b];
+        return;
+      }
+    load = cnt[b] + 1;
+    raise = load > mx ? load - mx : 0;
+  }
+  void add(uint32_t w) {
+    const int b = (int)(w % (uint32_t)g);
+    for (int i = 0; i < cnt[b]; ++i)
+      if (word[b][i] == w) {
+        ++uses[b][i];
+        return;
+      }
+    word[b][cnt[b]] = w;
+    uses[b][cnt[b]++] = 1;
+  }
+  void remove(uint32_t w) {
+    const int b = (int)(w % (uint32_t)g);
+    for (int i = 0; i < cnt[b]; ++i)
+      if (word[b][i] == w) {
+        if (--uses[b][i] == 0) {
+          --cnt[b];
+          word[b][i] = word[b][cnt[b]];
+          uses[b][i] = uses[b][cnt[b]];
         }
-      load = cnt[b] + 1;
-      raise = load > mx ? load - mx : 0;
+        return;
+      }
+  }
+};
+
+struct BankSched {
+  int G;
+  bool use_x, use_p;
+  uint64_t pad_hi;
+  uint32_t pad_t, pad_p;
+  static constexpr uint64_t kPad = ~0ull;  // a padding pick (never a record: bits 42.. of records are < 2^22)
+  BankBins bx, bt, bp;
+  void add(uint64_t r) {
+    if (r == kPad) {
+      bt.add(pad_t);
+      if (use_p) bp.add(pad_p);
+      return;
     }
-    void add(uint32_t w, int g) {
-      const int b = (int)(w % (uint32_t)g);
-      for (int i = 0; i < cnt[b]; ++i)
-        if (word[b][i] == w) return;
-      word[b][cnt[b]++] = w;
-      if (cnt[b] > mx) mx = cnt[b];
+    if (use_x) bx.add((uint32_t)(r & 0xFFFFFFu));
+    bt.add((uint32_t)(r >> 24) & 0x3FFFFu);
+    if (use_p) bp.add((uint32_t)(r >> 42));
+  }
+  void remove(uint64_t r) {
+    if (r == kPad) {
+      bt.remove(pad_t);
+      if (use_p) bp.remove(pad_p);
+      return;
     }
-  };
-  const uint32_t pad_t = (uint32_t)(pad_hi & 0x3FFFFu), pad_p = (uint32_t)(pad_hi >> 18);
-  const int n_arr = (use_x ? 1 : 0) + 1 + (use_p ? 1 : 0);
-  const int64_t n_sl = (int64_t)off.size();
-  std::vector<std::vector<uint64_t>> rem(32);
-  for (int64_t sl = 0; sl < n_sl; ++sl) {
-    const int W = width[sl];
-    const int lanes = (int)std::min<int64_t>(32, n_orb - sl * 32);  // lanes past the last row never load
-    uint64_t* base = recs.data() + off[sl];
+    if (use_x) bx.remove((uint32_t)(r & 0xFFFFFFu));
+    bt.remove((uint32_t)(r >> 24) & 0x3FFFFu);
+    if (use_p) bp.remove((uint32_t)(r >> 42));
+  }
+  // take the best of rl (or padding, when slots_left allows it) out of rl
+  uint64_t choose(std::vector<uint64_t>& rl, int slots_left) {
+    const int mx = bx.worst(), mt = bt.worst(), mp = bp.worst();
+    int best = -1, best_raise = INT_MAX, best_load = INT_MAX;
+    for (int i = 0; i < (int)rl.size(); ++i) {
+      const uint64_t r = rl[i];
+      int ra = 0, lo = 0, r1, l1;
+      if (use_x) {
+        bx.cost((uint32_t)(r & 0xFFFFFFu), mx, r1, l1);
+        ra += r1;
+        lo += l1;
+      }
+      bt.cost((uint32_t)(r >> 24) & 0x3FFFFu, mt, r1, l1);
+      ra += r1;
+      lo += l1;
+      if (use_p) {
+        bp.cost((uint32_t)(r >> 42), mp, r1, l1);
+        ra += r1;
+        lo += l1;
+      }
+      if (ra < best_raise || (ra == best_raise && lo < best_load)) {
+        best = i;
+        best_raise = ra;
+        best_load = lo;
+      }
+    }
+    if ((int)rl.size() < slots_left) {
+      int r1, l1, r2 = 0, l2 = 0;
+      bt.cost(pad_t, mt, r1, l1);
+      if (use_p) bp.cost(pad_p, mp, r2, l2);
+      if (best < 0 || r1 + r2 < best_raise) return kPad;
+    }
+    const uint64_t r = rl[best];
+    rl[best] = rl.back();
+    rl.pop_back();
+    return r;
+  }
+  void slice(uint64_t* base, int W, int lanes, std::vector<std::vector<uint64_t>>& rem) {
     for (int l = 0; l < lanes; ++l) {
       rem[l].clear();
       for (int k = 0; k < W; ++k) {
@@ -2640,72 +2760,58 @@ static void bank_schedule(std::vector<uint64_t>& recs, const std::vector<uint32_
         if ((r >> 24) != pad_hi) rem[l].push_back(r);
       }
     }
-    Bins bx, bt, bp;
+    uint64_t pick[32];
     for (int k = 0; k < W; ++k) {
       for (int g0 = 0; g0 < lanes; g0 += G) {
+        const int ge = std::min(lanes, g0 + G);
         bx.clear(G);
         bt.clear(G);
         bp.clear(G);
-        int pads[kMaxG], n_pads = 0;
+        for (int l = g0; l < ge; ++l) add(pick[l] = choose(rem[l], W - k));
+        for (int round = 0; round < kBankRounds; ++round)
+          for (int l = g0; l < ge; ++l) {
+            remove(pick[l]);
+            if (pick[l] != kPad) rem[l].push_back(pick[l]);
+            add(pick[l] = choose(rem[l], W - k));
+          }
         uint32_t any_col = 0;
-        bool have_col = false;
-        for (int l = g0; l < std::min(lanes, g0 + G); ++l) {
-          std::vector<uint64_t>& rl = rem[l];
-          const bool may_pad = (int)rl.size() < W - k;
-          // the best real record: least raise of a worst load, then least load
-          int best = -1, best_raise = INT_MAX, best_load = INT_MAX;
-          for (int i = 0; i < (int)rl.size(); ++i) {
-            const uint64_t r = rl[i];
-            int ra = 0, lo = 0, r1, l1;
-            if (use_x) {
-              bx.cost((uint32_t)(r & 0xFFFFFFu), G, r1, l1);
-              ra += r1;
-              lo += l1;
-            }
-            bt.cost((uint32_t)(r >> 24) & 0x3FFFFu, G, r1, l1);
-            ra += r1;
-            lo += l1;
-            if (use_p) {
-              bp.cost((uint32_t)(r >> 42), G, r1, l1);
-              ra += r1;
-              lo += l1;
-            }
-            if (ra < best_raise || (ra == best_raise && lo < best_load)) {
-              best = i;
-              best_raise = ra;
-              best_load = lo;
-              if (ra == 0 && lo == n_arr) break;  // every word alone in its bank group
-            }
+        for (int l = g0; l < ge; ++l)
+          if (pick[l] != kPad) {
+            any_col = (uint32_t)(pick[l] & 0xFFFFFFu);
+            break;
           }
-          // padding only where it raises a worst load less than the best real
-          // record does (padding is cheapest at the end of a slice, where
-          // every lane pads together)
-          if (may_pad && best >= 0) {
-            int r1, l1, r2 = 0, l2 = 0;
-            bt.cost(pad_t, G, r1, l1);
-            if (use_p) bp.cost(pad_p, G, r2, l2);
-            if (r1 + r2 < best_raise) best = -1;
-          }
-          uint64_t* dst = base + 32 * (size_t)k + l;
-          if (best < 0) {
-            pads[n_pads++] = l;
-            bt.add(pad_t, G);
-            if (use_p) bp.add(pad_p, G);
-            continue;
-          }
-          const uint64_t r = rl[best];
-          rl[best] = rl.back();
-          rl.pop_back();
-          *dst = r;
-          if (use_x) bx.add((uint32_t)(r & 0xFFFFFFu), G);
-          bt.add((uint32_t)(r >> 24) & 0x3FFFFu, G);
-          if (use_p) bp.add((uint32_t)(r >> 42), G);
-          if (!have_col) any_col = (uint32_t)(r & 0xFFFFFFu), have_col = true;
-        }
-        for (int i = 0; i < n_pads; ++i) base[32 * (size_t)k + pads[i]] = (pad_hi << 24) | any_col;
+        for (int l = g0; l < ge; ++l)
+          base[32 * (size_t)k + l] = pick[l] == kPad ? (pad_hi << 24) | any_col : pick[l];
       }
     }
   }
+};
+}  // namespace
+
+static void bank_schedule(std::vector<uint64_t>& recs, const std::vector<uint32_t>& off,
+                          const std::vector<int32_t>& width, int64_t n_orb, int elem, bool use_x, bool use_p,
+                          uint64_t pad_hi) {
+  const int64_t n_sl = (int64_t)off.size();
+  const int nthr = n_sl >= 64 ? (int)std::min(8u, std::max(1u, std::thread::hardware_concurrency())) : 1;
+  auto work = [&](int t) {
+    BankSched bs;
+    bs.G = 128 / elem;
+    bs.use_x = use_x;
+    bs.use_p = use_p;
+    bs.pad_hi = pad_hi;
+    bs.pad_t = (uint32_t)(pad_hi & 0x3FFFFu);
+    bs.pad_p = (uint32_t)(pad_hi >> 18);
+    std::vector<std::vector<uint64_t>> rem(32);
+    for (int64_t sl = t; sl < n_sl; sl += nthr)
+      bs.slice(recs.data() + off[sl], width[sl], (int)std::min<int64_t>(32, n_orb - sl * 32), rem);
+  };
+  if (nthr == 1) {
+    work(0);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthr; ++t) th.emplace_back(work, t);
+  for (auto& t : th) t.join();
 }
 
 static bool bank_order_enabled() {
@@ -2717,7 +2823,7 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
   if (B.phi_cap == 0 || !B.tab_enabled) return false;
   const CatalogImpl& C = *B.cat;
   const GroupImpl& G = *C.group;
-  if (C.n_orbits >= (1 << 24) || (int64_t)B.n_bil * G.n_ops >= (1 << 18) || C.n_filled > 63) return false;
+  if (C.n_orbits >= (1 << 24) || B.tchi_n >= (1 << 18) || C.n_filled > 63) return false;
   std::vector<uint64_t> fmask;
   std::vector<int8_t> rep;
   if (gauge) {
@@ -2804,6 +2910,8 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
   std::unordered_map<uint32_t, uint32_t> id;
   std::vector<uint32_t> desc;
   const uint64_t n_tchi = (uint64_t)B.n_bil * G.n_ops;
+  // a coefficient's slot in the hashed table layout of hop-table runs
+  auto tslot = [&](uint64_t i) { return i * (uint64_t)B.tchi_mul % (uint64_t)B.tchi_n; };
   if (gauge) {
     // phase id = the sign; padding: the zero coefficient (tchi entry n_tchi,
     // phase id 2)
@@ -2812,11 +2920,12 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
       SED_REQUIRE(pad || ((recs[t] & 0xFFFFFFu) < (uint64_t)C.n_orbits && ((recs[t] >> 24) & 0x3FFFFu) < n_tchi &&
                           (int)(keys[t] & 0x3F) < G.n_ops && (keys[t] >> 25) == 0),
                   5, "internal error: hop-table record out of range");
-      recs[t] = pad ? (n_tchi << 24) | (2ULL << 42) : (recs[t] & ((1ULL << 42) - 1)) | ((uint64_t)(keys[t] >> 24) << 42);
+      const uint64_t ti = pad ? n_tchi : (recs[t] >> 24) & 0x3FFFFu;
+      recs[t] = (pad ? 0 : recs[t] & 0xFFFFFFu) | (tslot(ti) << 24) | ((pad ? 2ULL : (uint64_t)(keys[t] >> 24)) << 42);
     }
     if (bank_order_enabled())
       bank_schedule(recs, B.h_sl_off, B.h_sl_w, C.n_orbits, B.precision == 1 ? 8 : 16, B.x_smem && B.precision == 1,
-                    false, n_tchi | (2ULL << 18));
+                    false, tslot(n_tchi) | (2ULL << 18));
     SED_CUDA(cudaMemcpyAsync(B.hop.p, recs.data(), (size_t)tot * 8, cudaMemcpyHostToDevice, s));
     SED_CUDA(cudaStreamSynchronize(s));
     B.n_phi = 2;
@@ -2845,11 +2954,12 @@ static bool prepare_table(BatchImpl& B, int n_req, const double* phase, cudaStre
     SED_REQUIRE(pad || ((recs[t] & 0xFFFFFFu) < (uint64_t)C.n_orbits && ((recs[t] >> 24) & 0x3FFFFu) < n_tchi), 5,
                 "internal error: hop-table record out of range");
     const uint64_t phi = pad ? zero_id : id[keys[t]];
-    recs[t] = (pad ? 0 : recs[t] & ((1ULL << 42) - 1)) | (phi << 42);
+    const uint64_t ti = pad ? n_tchi : (recs[t] >> 24) & 0x3FFFFu;
+    recs[t] = (pad ? 0 : recs[t] & 0xFFFFFFu) | (tslot(ti) << 24) | (phi << 42);
   }
   if (bank_order_enabled())
     bank_schedule(recs, B.h_sl_off, B.h_sl_w, C.n_orbits, B.precision == 1 ? 8 : 16, B.x_smem && B.precision == 1,
-                  true, zero_id << 18);
+                  true, tslot(n_tchi) | (zero_id << 18));
   SED_CUDA(cudaMemcpyAsync(B.hop.p, recs.data(), (size_t)tot * 8, cudaMemcpyHostToDevice, s));
   upload(B.phi_desc, desc, s);
   B.n_phi = (int)desc.size();
@@ -2927,6 +3037,20 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   B->diag.alloc((size_t)std::max<int64_t>(n, 1) * 16);
   compute_diag(n, C.reps.as<uint64_t>(), nullptr, n_den, ddij.as<int32_t>(), ddv.as<double2>(), B->diag.as<double2>(),
                s);
+  // coefficient table slots: the smallest prime >= n_bil * G + 1, and a
+  // multiplier near 0.618 of it (golden-ratio hashing; coprime to the prime)
+  {
+    auto is_prime = [](int64_t v) {
+      if (v < 2) return false;
+      for (int64_t d = 2; d * d <= v; ++d)
+        if (v % d == 0) return false;
+      return true;
+    };
+    int64_t p = (int64_t)n_bil * G.n_ops + 1;
+    while (!is_prime(p)) ++p;
+    B->tchi_n = (int)p;
+    B->tchi_mul = (int)std::max<int64_t>(1, (int64_t)(0.6180339887498949 * (double)p));
+  }
   // the hop table's phase-id coefficients need shared memory; a sector too
   // large for both keeps the on-the-fly matvec
   B->phi_cap = kPhiCap;
@@ -2962,7 +3086,7 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   // per-block workspace, bounded to 16 GB
   // basis and restart buffers of equal capacity (they trade places), work vector, FP64 input
   const size_t slots = (size_t)std::max(B->m_cap + 1, 5 * (nev + 2));  // the largest Krylov dimension tried
-  const size_t per_cta = (2 * slots + 2) * B->ld * 16 + (size_t)n_bil * G.n_ops * 16 + B->ld;
+  const size_t per_cta = (2 * slots + 2) * B->ld * 16 + (size_t)B->tchi_n * 16 + B->ld;
   ncta = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)ncta, (int64_t)max_req,
                                                       (int64_t)((16ull << 30) / std::max<size_t>(per_cta, 1))}));
   B->n_cta = ncta;
@@ -2970,7 +3094,7 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   B->R.alloc((size_t)ncta * slots * B->ld * 16);
   B->W.alloc((size_t)ncta * B->ld * 16);
   B->X64.alloc((size_t)ncta * B->ld * 16);
-  B->tchi64.alloc((size_t)ncta * (n_bil * G.n_ops + 1) * 16);
+  B->tchi64.alloc((size_t)ncta * B->tchi_n * 16);
   B->rowflag.alloc((size_t)ncta * B->ld);
   if (B->phi_cap) B->pwc64.alloc((size_t)ncta * B->phi_cap * 16);
   B->in_chi.alloc((size_t)max_req * G.n_ops * 16);
