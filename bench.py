@@ -27,6 +27,7 @@ import statistics
 import subprocess
 import sys
 import time
+from typing import Optional
 
 import numpy as np
 
@@ -578,7 +579,7 @@ def fifo_latencies(arrivals, service):
 
 
 def served_report(n_req: int, rate: float, large_workers: int = 3, plain_all: bool = True, plain_per_family: int = 2,
-                  seed: int = 20261203):
+                  seed: int = 20261203, partition: Optional[dict] = None):
     """Config 5: a seeded Poisson stream of ground-state requests drawn
     uniformly from rings N in {20, 24, 28}, checkerboard 3x4 / 4x4 and Hubbard
     3x4 / 4x4 with N_up = N_down in {5, 6} (two-species blocks), random momentum
@@ -596,7 +597,7 @@ def served_report(n_req: int, rate: float, large_workers: int = 3, plain_all: bo
 
     fams = config5_families()
     t0 = time.perf_counter()
-    srv = SectorServer(fams, budget_bytes=160e9, batch_lanes=2, large_workers=large_workers)
+    srv = SectorServer(fams, budget_bytes=160e9, batch_lanes=2, large_workers=large_workers, **(partition or {}))
     t_setup = time.perf_counter() - t0
     reqs = random_requests(fams, n_req, rate=rate, seed=seed)
     done = sorted(srv.serve(reqs), key=lambda r: r.rid)
@@ -661,8 +662,16 @@ def run_served(args):
     import torch
 
     torch.cuda.set_device(0)
+    part = {}
+    if args.served_medium_orbits is not None:
+        part["medium_max_orbits"] = args.served_medium_orbits
+    if args.served_medium_batch is not None:
+        part["medium_max_batch"] = args.served_medium_batch
+    if args.served_large_sms:
+        part["large_sm_limit"] = args.served_large_sms
     line = served_report(args.served_n, args.served_rate, args.large_workers, plain_all=not args.plain_sampled,
-                         plain_per_family=args.plain_per_family)
+                         plain_per_family=args.plain_per_family, partition=part)
+    line["partition"] = part
     print(json.dumps(line), flush=True)
 
 
@@ -689,6 +698,12 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the config-2/3 kernel and solve report and the short served stream")
     ap.add_argument("--extras-served-n", type=int, default=200)
+    ap.add_argument("--served-medium-orbits", type=int, default=None,
+                    help="served: catalogs up to this many orbits take the mid-size batch lane")
+    ap.add_argument("--served-medium-batch", type=int, default=None,
+                    help="served: requests (so SMs) of one mid-size batch launch")
+    ap.add_argument("--served-large-sms", type=int, default=0,
+                    help="served: SMs the device-wide solves size their grids for (0: all)")
     ap.add_argument("--large-shape", type=int, nargs=3, default=[4, 6, 8], metavar=("L1", "L2", "NP"))
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--large-nev", type=int, default=3, help="eigenpairs of the large-sector solve")

@@ -229,6 +229,13 @@ int sed_op_set_stream(sed_op* op, void* cuda_stream);
  * before the queued kernels of low-priority ones.  Replaces a stream set by
  * sed_op_set_stream. */
 int sed_op_set_priority(sed_op* op, int high);
+/* SM budget of the operator's kernels (no counterpart in the reference):
+ * the matvec, the Lanczos vector kernels and the solve size their grids for
+ * n_sm SMs instead of the whole device (0: the whole device, the default).
+ * A server that keeps other kernels resident on some SMs (the persistent
+ * batch) gives its device-wide solves the rest, so their one-wave grids still
+ * complete in one wave.  Results do not change. */
+int sed_op_set_sm_limit(sed_op* op, int n_sm);
 /* Orbit-indexed matvec for benchmarking the kernel alone: xs_dev holds
  * sqrt(stab)*x in the op's precision (complex64 or complex128, length
  * n_orbits), y_dev receives complex128 H x (length n_orbits).  Asynchronous. */

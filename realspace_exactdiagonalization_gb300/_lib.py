@@ -77,6 +77,7 @@ SIGNATURES = [
     ("sed_op_hop_table_info", _i32, [_p, _p, _p, _p]),
     ("sed_op_set_stream", _i32, [_p, _p]),
     ("sed_op_set_priority", _i32, [_p, _i32]),
+    ("sed_op_set_sm_limit", _i32, [_p, _i32]),
     ("sed_op_apply_orbit", _i32, [_p, _p, _p]),
     ("sed_op_apply_noalloc", _i32, [_p, _p, _p, _i64]),
     ("sed_op_destroy", None, [_p]),

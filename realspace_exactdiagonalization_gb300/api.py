@@ -431,6 +431,12 @@ class MatrixFreeHamiltonian(_Handle):
         scheduled before the queued kernels of low-priority solves."""
         check(_lib.load().sed_op_set_priority(self._h, 1 if high else 0))
 
+    def set_sm_limit(self, n_sm: int) -> None:
+        """Size this operator's kernel grids for n_sm SMs (0: the whole
+        device; sed_op_set_sm_limit), for a server that keeps other work
+        resident on the remaining SMs.  Results do not change."""
+        check(_lib.load().sed_op_set_sm_limit(self._h, int(n_sm)))
+
     def set_hop_table(self, mode: int) -> None:
         """The stored form of this operator's matvec (8 bytes per hop): 0 off,
         1 built at the first solve when it fits (default), 2 built now."""

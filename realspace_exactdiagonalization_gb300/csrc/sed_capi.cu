@@ -280,6 +280,13 @@ int sed_op_set_priority(sed_op* op, int high) {
     op->p->own_stream = true;
   });
 }
+int sed_op_set_sm_limit(sed_op* op, int n_sm) {
+  return guarded([&] {
+    REQ(op, "NULL operator");
+    REQ(n_sm >= 0, "SM limit must be >= 0");
+    op->p->sm_limit = n_sm;
+  });
+}
 int sed_op_apply_orbit(sed_op* op, const void* xs_dev, double* y_dev) {
   return guarded([&] {
     REQ(op && xs_dev && y_dev, "NULL argument");

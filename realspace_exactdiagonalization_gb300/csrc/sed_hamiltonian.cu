@@ -190,6 +190,7 @@ void compute_phase_classes(const GroupImpl& G, int k, PhaseClassTables& pc) {
 struct ApplyArgs {
   int64_t n_orb;
   int N, G, n_class, n_terms;
+  int sms;  // SMs the grid is sized for (op_sm_count)
   const uint64_t* reps;
   const uint8_t* stab;
   const uint8_t* rowflag;
@@ -497,6 +498,7 @@ static ApplyArgs make_args(const OpImpl& op, bool fp32) {
   const TermTables& tt = op.terms;
   ApplyArgs a{};
   a.n_orb = C.n_orbits;
+  a.sms = op_sm_count(op);
   a.N = G.n_site;
   a.G = G.n_ops;
   a.n_class = tt.n_class;
@@ -552,7 +554,7 @@ static void launch_apply_tpr(const ApplyArgs& a, const void* xs, double* y, cuda
   blocks_per_sm = std::max(blocks_per_sm, 1);
   const int64_t rows_per_block = block / TPR;
   const int64_t want = (a.n_orb + rows_per_block - 1) / rows_per_block;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * blocks_per_sm));
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)a.sms * blocks_per_sm));
   kern<<<grid, block, L.total, s>>>(a, L, reinterpret_cast<const V*>(xs), reinterpret_cast<double2*>(y));
   SED_CUDA(cudaGetLastError());
 }

@@ -194,8 +194,14 @@ struct OpImpl {
   // the gather matvec's launch shape per precision [FP64, complex64]: threads
   // per row and threads per block (0: not chosen yet; the autotuner decides)
   int apply_tpr[2] = {0, 0}, apply_block[2] = {0, 0};
+  // SMs the operator's matvec and solve kernels size their grids for (0: all
+  // of the device's); a server that keeps other work resident on some SMs
+  // gives its device-wide solves the rest, so their one-wave grids still
+  // run in one wave
+  int sm_limit = 0;
   ~OpImpl();
 };
+int op_sm_count(const OpImpl& op);  // sm_limit, or the device's SM count
 void op_set_apply_shape(OpImpl& op, int tpr, int block);
 bool op_build_table(OpImpl& op);
 void op_drop_table(OpImpl& op);
@@ -301,6 +307,10 @@ void eigh_complex_herm(int n, const std::vector<double>& Hreim, std::vector<doub
 static constexpr int kMaxDevices = 64;
 int current_device();  // cudaGetDevice, checked against kMaxDevices
 int device_sm_count(); // SM count of the current device
+inline int op_sm_count(const OpImpl& op) {
+  const int n = device_sm_count();
+  return op.sm_limit > 0 && op.sm_limit < n ? op.sm_limit : n;
+}
 // One kernel's dynamic shared-memory opt-in on every device.  ensure() raises
 // it to at least `bytes` on the current device and never lowers it; callers
 // hold their own lock from ensure() through the launch, so a concurrent caller

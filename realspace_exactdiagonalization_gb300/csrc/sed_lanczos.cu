@@ -639,8 +639,8 @@ struct VecOps {
   cudaStream_t s;
   DevBuf part, part1, coef, scal, flag;  // partial sums, coefficients, scalars, skip flag
   double* host = nullptr;          // pinned scratch
-  VecOps(int64_t n_, cudaStream_t s_) : n(n_), s(s_) {
-    const int64_t sms = device_sm_count();
+  VecOps(int64_t n_, cudaStream_t s_, int sms_) : n(n_), s(s_) {
+    const int64_t sms = sms_;
     nblk = (int)std::max<int64_t>(1, std::min<int64_t>((n + kBS * 4 - 1) / (kBS * 4), sms * 4));
     // the complex64 dot kernel's grid is one full wave of its resident blocks
     int per_sm = 1;
@@ -742,7 +742,7 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
   float2* Rc = Rcb.as<float2>();
   float2* Wc = Wcb.as<float2>();
   const double2* Vout = V;  // where the returned eigenvectors end up (FP64)
-  VecOps ops(n, s);
+  VecOps ops(n, s, op_sm_count(op));
   auto vec = [&](int j) { return V + (size_t)j * ld; };
   auto vecc = [&](int j) { return Vc + (size_t)j * ldc; };
   const int gblk = ops.nblk;

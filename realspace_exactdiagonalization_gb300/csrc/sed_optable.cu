@@ -171,38 +171,62 @@ __global__ void __launch_bounds__(kTabBS) k_apply_tab(int64_t n_orb, const uint6
   __syncthreads();
   const V* cf_tab = smem_coef ? s_coef : coef;
   const int lane = threadIdx.x & 31;
-  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_orb; o += (int64_t)gridDim.x * blockDim.x) {
-    if (!rowflag[o]) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // a row's flag, slice offset and width are loaded one grid-stride step
+  // ahead, so a row waits on one DRAM round trip (its first records) instead
+  // of three dependent ones
+  int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint8_t flag = 0;
+  int64_t off = 0;
+  int wdt = 0;
+  if (o < n_orb) {
+    flag = rowflag[o];
+    off = sl_off[o >> 5];
+    wdt = sl_w[o >> 5];
+  }
+  for (; o < n_orb; o += stride) {
+    const int64_t on = o + stride;
+    uint8_t flag_n = 0;
+    int64_t off_n = 0;
+    int wdt_n = 0;
+    if (on < n_orb) {
+      flag_n = rowflag[on];
+      off_n = sl_off[on >> 5];
+      wdt_n = sl_w[on >> 5];
+    }
+    if (!flag) {
       if (CF)
         reinterpret_cast<float2*>(y)[o] = make_float2(0.f, 0.f);
       else
         y[o] = make_double2(0.0, 0.0);
-      continue;
-    }
-    const int64_t sl = o >> 5;
-    const uint64_t* rp = hop + sl_off[sl] + lane;
-    const int wdt = sl_w[sl];
-    const double2 dg = diag[o];
-    const V xo = xs[o];
-    S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
-    S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
-#pragma unroll 8
-    for (int k = 0; k < wdt; ++k) {
-      const uint64_t r = __ldcs(reinterpret_cast<const unsigned long long*>(rp + 32 * (int64_t)k));
-      const V cf = cf_tab[r >> kCBits];
-      const V xc = xs[r & kCMask];
-      ar = P::mad(cf.x, xc.x, ar);
-      ar = P::mad(-cf.y, xc.y, ar);
-      ai = P::mad(cf.x, xc.y, ai);
-      ai = P::mad(cf.y, xc.x, ai);
-    }
-    const double is = s_isr[stab[o]];
-    const double yr = (double)ar * is, yi = (double)ai * is;
-    if (CF) {
-      reinterpret_cast<float2*>(y)[o] = make_float2((float)yr, (float)yi);
     } else {
-      y[o] = make_double2(yr, yi);
+      const uint64_t* rp = hop + off + lane;
+      const uint8_t st = stab[o];
+      const double2 dg = diag[o];
+      const V xo = xs[o];
+      S ar = (S)dg.x * xo.x - (S)dg.y * xo.y;
+      S ai = (S)dg.x * xo.y + (S)dg.y * xo.x;
+#pragma unroll 8
+      for (int k = 0; k < wdt; ++k) {
+        const uint64_t r = __ldcs(reinterpret_cast<const unsigned long long*>(rp + 32 * (int64_t)k));
+        const V cf = cf_tab[r >> kCBits];
+        const V xc = xs[r & kCMask];
+        ar = P::mad(cf.x, xc.x, ar);
+        ar = P::mad(-cf.y, xc.y, ar);
+        ai = P::mad(cf.x, xc.y, ai);
+        ai = P::mad(cf.y, xc.x, ai);
+      }
+      const double is = s_isr[st];
+      const double yr = (double)ar * is, yi = (double)ai * is;
+      if (CF) {
+        reinterpret_cast<float2*>(y)[o] = make_float2((float)yr, (float)yi);
+      } else {
+        y[o] = make_double2(yr, yi);
+      }
     }
+    flag = flag_n;
+    off = off_n;
+    wdt = wdt_n;
   }
 }
 
@@ -349,7 +373,7 @@ void apply_table(OpImpl& op, bool fp32, const void* xs, double* ypad, cudaStream
   else
     SED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_tab<P64>, kTabBS, smem));
   const int grid =
-      (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * std::max(per_sm, 1)));
+      (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)op_sm_count(op) * std::max(per_sm, 1)));
   if (fp32 && cf_out)
     k_apply_tab<P32, true><<<grid, kTabBS, smem, s>>>(n, op.tab_hop.as<uint64_t>(), op.tab_off.as<int64_t>(),
                                                       op.tab_w.as<int32_t>(), op.tab_coef32.as<float2>(), smem_coef,

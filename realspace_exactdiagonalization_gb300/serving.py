@@ -147,8 +147,13 @@ class SectorServer:
                  large_workers: int = 3, max_batch: int = 512, small_max_orbits: int = SMALL_MAX_ORBITS,
                  precision: str = "mixed", tol: float = 1e-10, nev: int = 1,
                  medium_max_orbits: int = MEDIUM_MAX_ORBITS, medium_lanes: int = 1,
-                 priority_max_orbits: int = PRIORITY_MAX_ORBITS, warm_up: bool = True):
+                 priority_max_orbits: int = PRIORITY_MAX_ORBITS, warm_up: bool = True,
+                 medium_max_batch: int = MEDIUM_MAX_BATCH, large_sm_limit: int = 0):
         self.budget = float(budget_bytes)
+        # device-wide solves size their grids for this many SMs (0: all); the
+        # mid-size lane's persistent blocks (at most medium_max_batch of them,
+        # one SM each) keep the rest
+        self.large_sm_limit = int(large_sm_limit)
         self.priority_max_orbits = priority_max_orbits
         self.precision = precision
         self.tol = tol
@@ -169,7 +174,7 @@ class SectorServer:
             fam = Family(name, spec, cat, pairs, route)
             self.resident += cat.n_states * 8 + cat.n_orbits * 9
             if route != "large":
-                cap = max_batch if route == "batch" else min(max_batch, MEDIUM_MAX_BATCH)
+                cap = max_batch if route == "batch" else min(max_batch, medium_max_batch)
                 for _ in range(batch_lanes if route == "batch" else medium_lanes):
                     s = BatchedSectorSolver(cat, pairs, spec.density_terms, precision=precision, nev=nev,
                                             max_requests=cap)
@@ -285,6 +290,8 @@ class SectorServer:
                                                 precision=self.precision)
                     if fam.n_orbits <= self.priority_max_orbits:
                         H.set_priority(True)
+                    if self.large_sm_limit > 0:
+                        H.set_sm_limit(self.large_sm_limit)
                     vals, _, info = H.solve(r.nev, tol=self.tol, seed=r.seed, want_vectors=False)
                     status, delta = 0, info.max_delta_polish
                     del H

@@ -94,6 +94,34 @@ def test_op_priority_keeps_results():
         _lib.check(_lib.load().sed_op_set_priority(H.handle, 2))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_op_sm_limit_keeps_results(oracle, precision):
+    """sed_op_set_sm_limit sizes the operator's grids for fewer SMs; the
+    reduction partitions change, so the eigenvalues agree within the path's
+    tolerance (and with the oracle), and a negative limit is refused."""
+    import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300 import _lib
+
+    spec = L.ring_xxz(16, 1.0, 2.0)
+    G = L.build_translation_group(spec.lattice, (0.2, 0.0))
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G,
+                                         particle_statistics=A.Bosonic())
+    irr = L.build_translation_irrep_list(G, spec.lattice)[3]
+    basis = A.build_symmetry_sector_basis(cat, irr, group=G)
+    vals = {}
+    for sms in (0, 16, 1):
+        H = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms((0.2, 0.0)), spec.density_terms, precision=precision)
+        H.set_sm_limit(sms)
+        vals[sms], _, _ = H.solve(2, want_vectors=False)
+    _, sec, op = oracle_objects(oracle, Case("ring16", spec, theta=(0.2, 0.0)), 3)
+    ref = np.linalg.eigvalsh(op.dense())
+    for sms, v in vals.items():
+        np.testing.assert_allclose(v, vals[0], rtol=1e-9, atol=1e-12, err_msg=f"sm_limit={sms}")
+        np.testing.assert_allclose(v, ref[:2], rtol=1e-9, atol=1e-12, err_msg=f"sm_limit={sms}")
+    with pytest.raises(_lib.SEDError):
+        _lib.check(_lib.load().sed_op_set_sm_limit(H.handle, -1))
+
+
 def test_concurrent_table_builds_from_two_threads():
     """Catalog expansions and operator hop tables stage per-catalog rank
     tables of different sizes in shared memory; their kernels' shared-memory
