@@ -579,7 +579,7 @@ def fifo_latencies(arrivals, service):
 
 
 def served_report(n_req: int, rate: float, large_workers: int = 3, plain_all: bool = True, plain_per_family: int = 2,
-                  seed: int = 20261203, partition: Optional[dict] = None):
+                  seed: int = 20261203, partition: Optional[dict] = None, native: bool = False):
     """Config 5: a seeded Poisson stream of ground-state requests drawn
     uniformly from rings N in {20, 24, 28}, checkerboard 3x4 / 4x4 and Hubbard
     3x4 / 4x4 with N_up = N_down in {5, 6} (two-species blocks), random momentum
@@ -589,15 +589,22 @@ def served_report(n_req: int, rate: float, large_workers: int = 3, plain_all: bo
     arrival times are replayed through a first-in-first-out single server with
     those service times; or, for long streams, per-family means of a sample of
     plain_per_family requests stand in for the service times (stated in the
-    result)."""
+    result).  native: the same stream through the library's native server
+    (sed_server_*, C++ host threads) instead of the Python scheduler."""
     import realspace_exactdiagonalization_gb300.api as A
     from realspace_exactdiagonalization_gb300 import lattice as L
-    from realspace_exactdiagonalization_gb300.serving import (SectorServer, config5_families, latency_stats,
-                                                              random_requests)
+    from realspace_exactdiagonalization_gb300.serving import (SMALL_MAX_ORBITS, NativeSectorServer, SectorServer,
+                                                              config5_families, latency_stats, random_requests)
 
     fams = config5_families()
     t0 = time.perf_counter()
-    srv = SectorServer(fams, budget_bytes=160e9, batch_lanes=2, large_workers=large_workers, **(partition or {}))
+    if native:
+        srv = NativeSectorServer(fams, budget_bytes=160e9, batch_lanes=2, large_workers=large_workers)
+        fam_of = {n: (srv.specs[n], srv.catalogs[n],
+                      "batch" if srv.catalogs[n].n_orbits <= SMALL_MAX_ORBITS else "large") for n in fams}
+    else:
+        srv = SectorServer(fams, budget_bytes=160e9, batch_lanes=2, large_workers=large_workers, **(partition or {}))
+        fam_of = {n: (f.spec, f.catalog, f.route) for n, f in srv.families.items()}
     t_setup = time.perf_counter() - t0
     reqs = random_requests(fams, n_req, rate=rate, seed=seed)
     done = sorted(srv.serve(reqs), key=lambda r: r.rid)
@@ -605,14 +612,14 @@ def served_report(n_req: int, rate: float, large_workers: int = 3, plain_all: bo
     errors = {r.rid: f"{r.family}: {r.error or r.status}" for r in done if r.status != 0}
 
     def plain_solve(r):
-        fam = srv.families[r.family]
-        G = L.build_translation_group(fam.spec.lattice, r.twist)
-        irr = L.build_translation_irrep_list(G, fam.spec.lattice)[r.k_index]
+        spec, catalog, _ = fam_of[r.family]
+        G = L.build_translation_group(spec.lattice, r.twist)
+        irr = L.build_translation_irrep_list(G, spec.lattice)[r.k_index]
         t1 = time.perf_counter()
-        basis = A.build_symmetry_sector_basis(fam.catalog, irr, group=G)
+        basis = A.build_symmetry_sector_basis(catalog, irr, group=G)
         e = float("nan")
         if basis.dim:
-            H = A.MatrixFreeHamiltonian(basis, fam.spec.bilinear_terms(r.twist), fam.spec.density_terms)
+            H = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms(r.twist), spec.density_terms)
             vals, _, _ = H.solve(r.nev, tol=1e-10, seed=r.seed, want_vectors=False)
             e = float(vals[0])
             del H
@@ -643,18 +650,22 @@ def served_report(n_req: int, rate: float, large_workers: int = 3, plain_all: bo
     per_fam = {}
     for name in sorted(fams):
         mine = [r for r in done if r.family == name]
-        fam = srv.families[name]
-        per_fam[name] = {"route": fam.route, "n_orbits": fam.n_orbits, "served": len(mine),
+        _, catalog, route = fam_of[name]
+        per_fam[name] = {"route": route, "n_orbits": catalog.n_orbits, "served": len(mine),
                          "plain_fp64_service_s": float(np.mean([service[r.rid] for r in mine])) if mine else None,
-                         "mean_service_s": float(np.mean([r.t_end - r.t_start for r in mine])) if mine else None,
-                         "mean_wait_s": float(np.mean([r.t_start - r.arrival for r in mine])) if mine else None}
+                         "mean_latency_s": float(np.mean([r.t_end - r.arrival for r in mine])) if mine else None}
+        if not native:  # the Python scheduler stamps when a request's solve starts
+            per_fam[name]["mean_service_s"] = float(np.mean([r.t_end - r.t_start for r in mine])) if mine else None
+            per_fam[name]["mean_wait_s"] = float(np.mean([r.t_start - r.arrival for r in mine])) if mine else None
     return {"workload": "served_config5", "requests": len(done), "rate_per_s": rate, "seed": seed,
             "served": st, "plain_fp64_one_at_a_time": plain,
             "speedup_solves_per_s": st["solves_per_s"] / plain["solves_per_s"],
             "p50_ratio_plain_over_served": plain["p50_ms"] / st["p50_ms"],
             "p99_ratio_plain_over_served": plain["p99_ms"] / st["p99_ms"],
             "unconverged": [r.rid for r in done if r.status != 0], "errors": errors, "setup_s": t_setup,
-            "peak_reserved_gb": srv.peak_reserved / 1e9, "resident_gb": srv.resident / 1e9,
+            "server": "native" if native else "python",
+            "peak_reserved_gb": (srv.stats()["peak_reserved_bytes"] if native else srv.peak_reserved) / 1e9,
+            "resident_gb": (srv.stats()["resident_bytes"] if native else srv.resident) / 1e9,
             "max_rel_dE_vs_plain_fp64": float(max(rel)) if rel else None, "families": per_fam}
 
 
@@ -670,7 +681,7 @@ def run_served(args):
     if args.served_large_sms:
         part["large_sm_limit"] = args.served_large_sms
     line = served_report(args.served_n, args.served_rate, args.large_workers, plain_all=not args.plain_sampled,
-                         plain_per_family=args.plain_per_family, partition=part)
+                         plain_per_family=args.plain_per_family, partition=part, native=args.served_native)
     line["partition"] = part
     print(json.dumps(line), flush=True)
 
@@ -702,6 +713,8 @@ def main():
                     help="served: catalogs up to this many orbits take the mid-size batch lane")
     ap.add_argument("--served-medium-batch", type=int, default=None,
                     help="served: requests (so SMs) of one mid-size batch launch")
+    ap.add_argument("--served-native", action="store_true",
+                    help="served: use the library's native server (sed_server_*) instead of the Python scheduler")
     ap.add_argument("--served-large-sms", type=int, default=0,
                     help="served: SMs the device-wide solves size their grids for (0: all)")
     ap.add_argument("--large-shape", type=int, nargs=3, default=[4, 6, 8], metavar=("L1", "L2", "NP"))

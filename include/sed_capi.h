@@ -402,6 +402,49 @@ int sed_batch_set_stream(sed_batch* b, void* cuda_stream);
 int sed_batch_info(const sed_batch* b, int64_t* smem_bytes, int64_t* n_blocks, int64_t* footprint_bytes);
 void sed_batch_destroy(sed_batch* b);
 
+/* ---------------------------------------------------------------- serving */
+/* Continuous-batching server on the current device (no counterpart in the
+ * reference, whose per-sector loops -- _ed_scan_sectors!, SRE:1199-1256, and
+ * ed_scan!, SRE:1320-1355 -- answer one sector solve at a time).  Host threads
+ * drive the library's own objects: families whose catalog has at most
+ * small_max_orbits orbits are answered by batch_lanes persistent batched
+ * solves (sed_batch_run) taking turns, the others by up to large_workers
+ * concurrent device-wide solves (sed_solve), each admitted while the device
+ * memory reserved by the solves in flight plus its own footprint stays within
+ * budget_bytes.  A request's result depends only on its own inputs and seed,
+ * not on the mix it is served in.  precision: SED_PREC_*; tol as sed_solve. */
+typedef struct sed_server sed_server;
+int sed_server_create(double budget_bytes, int batch_lanes, int large_workers, int64_t small_max_orbits,
+                      int precision, double tol, sed_server** out);
+/* Register a model family before the first request: its catalog (the server
+ * keeps a reference), its bilinear (i, j) pairs with their default (untwisted)
+ * amplitudes, its density terms and the most eigenvalues a request may ask
+ * for (1..6).  A batched family's lanes are warmed up here on its untwisted
+ * zero-momentum sector (hop tables built, launch shape chosen), so no request
+ * waits for that.  Returns the family id. */
+int sed_server_add_family(sed_server* s, const sed_catalog* c, int n_bil, const int32_t* bil_ij,
+                          const double* bil_t_reim, int n_den, const int32_t* den_ij, const double* den_v_reim,
+                          int nev_max, int32_t* family);
+/* Submit one sector solve: the momentum characters chi (n_ops complex), the
+ * group phases (n_ops x n_site complex: the flux-twisted group of
+ * build_translation_group, SRE:1374-1405), the bilinear amplitudes (n_bil
+ * complex, in the family's pair order), the start-vector seed and nev.  The
+ * inputs are copied; returns a ticket. */
+int sed_server_submit(sed_server* s, int32_t family, const double* chi_reim, const double* group_phase_reim,
+                      const double* bil_t_reim, uint64_t seed, int nev, int64_t* ticket);
+/* Wait up to timeout_ms (0: poll) for a ticket.  When it has finished: its
+ * nev eigenvalues (ascending; NaN beyond the sector dimension), the request's
+ * own status (0, or the error code of its solve, whose message sed_last_error
+ * then returns) and its sector dimension, and the ticket is released.
+ * SED_ERR_TIMEOUT when it has not finished yet. */
+int sed_server_wait(sed_server* s, int64_t ticket, int timeout_ms, double* evals, int32_t* status, int64_t* dim);
+/* Requests finished and waiting, the peak device memory reserved by the
+ * device-wide solves, and the resident catalogs and batch workspaces. */
+int sed_server_stats(const sed_server* s, int64_t* n_done, int64_t* n_pending, double* peak_reserved_bytes,
+                     double* resident_bytes);
+/* Stop accepting requests, finish the ones queued, join the threads. */
+void sed_server_destroy(sed_server* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -349,3 +349,122 @@ def latency_stats(done: Sequence[Request]) -> dict:
     return {"n": len(done), "solves_per_s": len(done) / span if span > 0 else float("nan"),
             "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "span_s": span}
+
+
+class NativeSectorServer:
+    """The same continuous batching, run by the library's native server
+    (``sed_server_*`` in the C ABI): host threads in C++ drive the batch lanes
+    and the device-wide solves, and Python only submits and collects.  Model
+    families come from lattice specs as for :class:`SectorServer`; requests are
+    the same :class:`Request` objects."""
+
+    def __init__(self, families: Dict[str, L.ModelSpec], budget_bytes: float = 160e9, batch_lanes: int = 2,
+                 large_workers: int = 3, small_max_orbits: int = SMALL_MAX_ORBITS, precision: str = "mixed",
+                 tol: float = 1e-10, nev_max: int = 1):
+        import ctypes as C
+
+        self._C = C
+        lib = A._lib.load()
+        prec = {"fp64": A._lib.PREC_FP64, "mixed": A._lib.PREC_MIXED}[precision]
+        h = C.c_void_p()
+        A._lib.check(lib.sed_server_create(float(budget_bytes), int(batch_lanes), int(large_workers),
+                                           int(small_max_orbits), prec, float(tol), C.byref(h)))
+        self._h = h
+        self.specs = dict(families)
+        self.catalogs: Dict[str, A.Symmetry_Orbit_Catalog] = {}
+        self.family_id: Dict[str, int] = {}
+        for name, spec in families.items():
+            G = L.build_translation_group(spec.lattice)
+            cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, species=spec.species, symmetry_group=G,
+                                                 particle_statistics=statistics_from_name(spec.statistics))
+            terms = spec.bilinear_terms()
+            bij = np.ascontiguousarray([[i - 1, j - 1] for (i, j, _) in terms], dtype=np.int32)
+            bt = np.ascontiguousarray([complex(t) for (_, _, t) in terms], dtype=np.complex128)
+            dij = np.ascontiguousarray([[int(i) - 1, int(j) - 1] for (i, j, _) in spec.density_terms], dtype=np.int32)
+            dv = np.ascontiguousarray([complex(v) for (_, _, v) in spec.density_terms], dtype=np.complex128)
+            fid = C.c_int32(-1)
+            A._lib.check(lib.sed_server_add_family(self._h, cat.handle, len(terms), bij.ctypes.data, bt.ctypes.data,
+                                                   len(dv), dij.ctypes.data if len(dv) else None,
+                                                   dv.ctypes.data if len(dv) else None, int(nev_max), C.byref(fid)))
+            self.catalogs[name] = cat
+            self.family_id[name] = fid.value
+        self._t0 = time.perf_counter()
+
+    def _now(self) -> float:
+        return time.perf_counter() - self._t0
+
+    def submit(self, r: Request) -> int:
+        spec = self.specs[r.family]
+        G = L.build_translation_group(spec.lattice, r.twist)
+        irr = L.build_translation_irrep_list(G, spec.lattice)[r.k_index]
+        chi = np.ascontiguousarray(irr.array(), dtype=np.complex128)
+        ph = np.ascontiguousarray(G.phases(), dtype=np.complex128)
+        amp = np.ascontiguousarray([t for (_, _, t) in spec.bilinear_terms(r.twist)], dtype=np.complex128)
+        t = self._C.c_int64(0)
+        A._lib.check(A._lib.load().sed_server_submit(self._h, self.family_id[r.family], chi.ctypes.data,
+                                                     ph.ctypes.data, amp.ctypes.data, int(r.seed), int(r.nev),
+                                                     self._C.byref(t)))
+        r.arrival = self._now()
+        return t.value
+
+    def wait(self, ticket: int, r: Request, timeout_ms: int = 600_000) -> Request:
+        ev = np.zeros(r.nev, dtype=np.float64)
+        st, dim = self._C.c_int32(0), self._C.c_int64(0)
+        rc = A._lib.load().sed_server_wait(self._h, int(ticket), int(timeout_ms), ev.ctypes.data,
+                                           self._C.byref(st), self._C.byref(dim))
+        A._lib.check(rc)
+        r.evals, r.status, r.dim, r.t_end = ev, st.value, dim.value, self._now()
+        if st.value != 0:
+            r.error = A._lib.load().sed_last_error().decode()
+        r.route = "native"
+        return r
+
+    def serve(self, requests: Sequence[Request], time_scale: float = 1.0) -> List[Request]:
+        """Replay a stream: each request submitted at its arrival time (scaled);
+        a collector thread waits for the tickets in submission order and stamps
+        each request when its wait returns, so a request answered ahead of an
+        earlier one is stamped no later than that one's answer."""
+        self._t0 = time.perf_counter()
+        q: "queue.Queue" = queue.Queue()
+        done: List[Request] = []
+
+        def collect():
+            while True:
+                item = q.get()
+                if item is None:
+                    return
+                tk, r = item
+                done.append(self.wait(tk, r))
+
+        th = threading.Thread(target=collect, daemon=True)
+        th.start()
+        for r in sorted(requests, key=lambda x: x.arrival):
+            arr = r.arrival * time_scale
+            delay = arr - self._now()
+            if delay > 0:
+                time.sleep(delay)
+            tk = self.submit(r)
+            r.arrival = arr
+            q.put((tk, r))
+        q.put(None)
+        th.join()
+        return done
+
+    def stats(self) -> dict:
+        C = self._C
+        nd, npend, peak, res = C.c_int64(0), C.c_int64(0), C.c_double(0), C.c_double(0)
+        A._lib.check(A._lib.load().sed_server_stats(self._h, C.byref(nd), C.byref(npend), C.byref(peak),
+                                                    C.byref(res)))
+        return {"done": nd.value, "pending": npend.value, "peak_reserved_bytes": peak.value,
+                "resident_bytes": res.value}
+
+    def close(self) -> None:
+        if self._h:
+            A._lib.load().sed_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -159,3 +159,36 @@ def test_concurrent_table_builds_from_two_threads():
     assert not errs, errs
     for nf, vals in outs.items():
         assert len(vals) == 12 and len(set(vals)) == 1, (nf, vals)
+
+
+def test_native_server_matches_oracle(oracle):
+    """The native server (sed_server_* in the C ABI; C++ host threads driving
+    the batch lanes and the device-wide solves) answers a mixed stream with
+    the oracle's ground energies (1e-9) and the sector dimensions; misuse is
+    refused with SED_ERR_ARG."""
+    from realspace_exactdiagonalization_gb300 import _lib
+    from realspace_exactdiagonalization_gb300.serving import NativeSectorServer, random_requests
+
+    fams = _families()
+    reqs = random_requests(fams, 36, rate=0.0, seed=7, nev=1)
+    srv = NativeSectorServer(fams, budget_bytes=8e9, batch_lanes=2, large_workers=2, small_max_orbits=300)
+    try:
+        done = sorted(srv.serve(reqs), key=lambda r: r.rid)
+        assert len(done) == len(reqs) and all(r.status == 0 for r in done), [r.error for r in done if r.status]
+        for r in done:
+            case = Case(r.family, fams[r.family], theta=r.twist)
+            _, sec, op = oracle_objects(oracle, case, r.k_index)
+            assert r.dim == sec.dim
+            if sec.dim == 0:
+                assert np.isnan(r.evals[0])
+                continue
+            e0 = np.linalg.eigvalsh(op.dense())[0]
+            assert abs(r.evals[0] - e0) <= 1e-9 * max(1.0, abs(e0)), (r.rid, r.family)
+        st = srv.stats()
+        assert st["done"] == len(reqs) and st["pending"] == 0 and st["resident_bytes"] > 0
+        bad = random_requests(fams, 1, rate=0.0, seed=8, nev=2)[0]  # nev above the families' nev_max (1)
+        with pytest.raises(_lib.SEDError) as e:
+            srv.submit(bad)
+        assert e.value.code == _lib.SED_ERR_ARG
+    finally:
+        srv.close()
