@@ -402,6 +402,33 @@ int sed_batch_set_stream(sed_batch* b, void* cuda_stream);
 int sed_batch_info(const sed_batch* b, int64_t* smem_bytes, int64_t* n_blocks, int64_t* footprint_bytes);
 void sed_batch_destroy(sed_batch* b);
 
+/* Device-resident request loop (no counterpart in the reference): one
+ * persistent launch of the batched kernel on n_blocks SMs whose blocks claim
+ * requests from a ring of `capacity` slots as the host publishes them, so a
+ * request starts as soon as a block is free, with no launch per batch.  The
+ * host copies a request's inputs (the layouts of sed_batch_run, one request)
+ * into a slot and then publishes it in mapped memory; a block claims it by
+ * compare-and-swap on the ring's head and leaves its outputs and a done flag
+ * in mapped memory.  Every wait is bounded: a block that finds nothing to do
+ * for idle_ms leaves, and the next submit or wait relaunches.  The ring uses
+ * the site-gauge hop table, so every request's group must have a site gauge
+ * (flux-twisted translation groups do; SED_ERR_ARG otherwise); a request
+ * whose mixed-precision check failed is re-solved in FP64 when collected.
+ * While the ring runs, sed_batch_run on the same object is refused. */
+int sed_batch_ring_start(sed_batch* b, int capacity, int n_blocks, int idle_ms);
+/* SED_ERR_LIMIT when every slot holds a request not yet collected. */
+int sed_batch_ring_submit(sed_batch* b, const double* chi_reim, const double* group_phase_reim,
+                          const double* bil_t_reim, uint64_t seed, int64_t* ticket);
+/* Wait up to timeout_ms (0: poll): nev eigenvalues, the request's status and
+ * sector dimension, and the slot is released; SED_ERR_TIMEOUT when the
+ * request has not finished yet. */
+int sed_batch_ring_wait(sed_batch* b, int64_t ticket, int timeout_ms, double* evals, int32_t* status, int64_t* dim);
+/* Launches so far, blocks per launch, and whether blocks are resident now. */
+int sed_batch_ring_info(const sed_batch* b, int64_t* launches, int32_t* n_blocks, int32_t* running);
+/* Stop the loop (blocks leave within one idle wait or at the end of their
+ * current request) and release the ring. */
+int sed_batch_ring_stop(sed_batch* b);
+
 /* ---------------------------------------------------------------- serving */
 /* Continuous-batching server on the current device (no counterpart in the
  * reference, whose per-sector loops -- _ed_scan_sectors!, SRE:1199-1256, and

@@ -99,6 +99,11 @@ SIGNATURES = [
     ("sed_batch_set_stream", _i32, [_p, _p]),
     ("sed_batch_info", _i32, [_p, _p, _p, _p]),
     ("sed_batch_destroy", None, [_p]),
+    ("sed_batch_ring_start", _i32, [_p, _i32, _i32, _i32]),
+    ("sed_batch_ring_submit", _i32, [_p, _p, _p, _p, _u64, _p]),
+    ("sed_batch_ring_wait", _i32, [_p, _i64, _i32, _p, _p, _p]),
+    ("sed_batch_ring_info", _i32, [_p, _p, _p, _p]),
+    ("sed_batch_ring_stop", _i32, [_p]),
     ("sed_server_create", _i32, [_dbl, _i32, _i32, _i64, _i32, _dbl, _p]),
     ("sed_server_add_family", _i32, [_p, _p, _i32, _p, _p, _i32, _p, _p, _i32, _p]),
     ("sed_server_submit", _i32, [_p, _i32, _p, _p, _p, _u64, _i32, _p]),

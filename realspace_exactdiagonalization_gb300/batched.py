@@ -175,6 +175,39 @@ class BatchedSectorSolver:
                                                float(tol), int(maxiter), vp(d_evals), vp(d_status), vp(d_dims),
                                                vp(d_delta), vp(d_nmv)))
 
+    # ---------------------------------------------------- device-resident loop
+    def ring_start(self, capacity: int = 1024, n_blocks: int = 152, idle_ms: int = 100) -> None:
+        """Start the device-resident request loop (sed_batch_ring_start): one
+        persistent launch whose blocks claim requests from a ring as they are
+        submitted; a block idle for idle_ms leaves, and the next submit or wait
+        relaunches.  Needs a site gauge for every request (flux-twisted
+        translation groups have one)."""
+        check(_lib.load().sed_batch_ring_start(self._h, int(capacity), int(n_blocks), int(idle_ms)))
+
+    def ring_submit(self, r: SectorRequest) -> int:
+        chi, ph, amp, seeds = self.pack([r])
+        t = C.c_int64(0)
+        check(_lib.load().sed_batch_ring_submit(self._h, chi.ctypes.data, ph.ctypes.data, amp.ctypes.data,
+                                                int(seeds[0]), C.byref(t)))
+        return t.value
+
+    def ring_wait(self, ticket: int, timeout_ms: int = 600_000):
+        """(evals, status, dim) of a ticket; raises SEDError (SED_ERR_TIMEOUT)
+        when it has not finished within timeout_ms."""
+        ev = np.zeros(self.nev, dtype=np.float64)
+        st, dim = C.c_int32(0), C.c_int64(0)
+        check(_lib.load().sed_batch_ring_wait(self._h, int(ticket), int(timeout_ms), ev.ctypes.data, C.byref(st),
+                                              C.byref(dim)))
+        return ev, st.value, dim.value
+
+    def ring_info(self) -> dict:
+        n, nb, run = C.c_int64(0), C.c_int32(0), C.c_int32(0)
+        check(_lib.load().sed_batch_ring_info(self._h, C.byref(n), C.byref(nb), C.byref(run)))
+        return {"launches": n.value, "blocks": nb.value, "running": bool(run.value)}
+
+    def ring_stop(self) -> None:
+        check(_lib.load().sed_batch_ring_stop(self._h))
+
     def set_stream(self, stream_ptr: int) -> None:
         check(_lib.load().sed_batch_set_stream(self._h, C.c_void_p(stream_ptr)))
 

@@ -19,6 +19,7 @@
 // sector dimensions); a request's result depends only on its own inputs and
 // seed, never on the other requests in the launch.  No block waits on another.
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -103,6 +104,16 @@ struct BatchArgs {
   // at evecs[(b * nev + i) * ev_ld + row], complex128, rows < dims[b]
   double2* evecs;
   int64_t ev_ld;
+  // ring mode (ring_tail != NULL): the blocks claim request q while q < the
+  // host-published tail, by compare-and-swap on the queue head, from slot
+  // q % ring_cap; each request's outputs (in mapped host memory) are followed
+  // by ring_done[slot] = q + 1.  A block that finds nothing to claim for
+  // ring_spin waits, or sees ring_stop, exits.
+  const unsigned int* ring_tail;
+  const int* ring_stop;
+  unsigned int* ring_done;
+  int ring_cap;
+  int ring_spin;
 };
 
 struct BatchSmem {
@@ -473,6 +484,10 @@ __device__ void block_jacobi(int n, double* A, double* Z, double* w, double* cs,
   }
   __syncthreads();
 }
+
+// request inputs are read through L2 (not L1): in ring mode a slot is reused
+// by later requests, and an L1 line of its earlier contents would be stale
+__device__ __forceinline__ double2 ld_in(const double2* p) { return __ldcg(p); }
 
 __device__ __forceinline__ int64_t global_ns() {
   uint64_t t;
@@ -1628,17 +1643,40 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
 
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) s_int[0] = (int)atomicAdd(a.queue, 1u);
+    if (threadIdx.x == 0) {
+      long long qv = -1;
+      if (a.ring_tail) {
+        for (int it = 0; it < a.ring_spin;) {
+          const unsigned int head = *reinterpret_cast<volatile unsigned int*>(a.queue);
+          const unsigned int tail = *reinterpret_cast<const volatile unsigned int*>(a.ring_tail);
+          if (head < tail) {
+            if (atomicCAS(a.queue, head, head + 1u) == head) {
+              qv = head;
+              break;
+            }
+            continue;  // another block took it: look again at once
+          }
+          if (*reinterpret_cast<const volatile int*>(a.ring_stop)) break;
+          __nanosleep(20000);
+          ++it;
+        }
+      } else {
+        qv = atomicAdd(a.queue, 1u);
+      }
+      s_int[0] = (int)(qv < 0 ? -1 : (qv & 0x7FFFFFFF));
+      s_int[24] = (int)(qv < 0 ? 0 : (unsigned int)qv);
+    }
     __syncthreads();
     const int q = s_int[0];
-    if (q >= a.n_req) break;
-    const int b = a.req_list ? a.req_list[q] : q;
+    if (q < 0 || (!a.ring_tail && q >= a.n_req)) break;
+    const unsigned int q_seq = (unsigned int)s_int[24];
+    const int b = a.ring_tail ? (int)(q_seq % (unsigned int)a.ring_cap) : a.req_list ? a.req_list[q] : q;
     if (threadIdx.x == 0 && !a.req_list) a.t_ns[2 * (size_t)b] = global_ns();
     const double2* chi = a.chi + (size_t)b * a.G;
     const double2* phase = a.phase + (size_t)b * a.G * a.N;
     const double2* amp = a.amp + (size_t)b * a.n_bil;
     // ---- set-up: tables for this momentum / twist
-    for (int i = threadIdx.x; i < a.G; i += blockDim.x) s_chi[i] = chi[i];
+    for (int i = threadIdx.x; i < a.G; i += blockDim.x) s_chi[i] = ld_in(chi + i);
     // phase classes of every twisted group element (see sed_rowgather.cuh)
     if (threadIdx.x == 0) s_int[1] = 1;
     __syncthreads();
@@ -1649,7 +1687,7 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       int nv = 0;
       bool over = false;
       for (int j = 0; j < a.N; ++j) {
-        const double2 e = ph[j];
+        const double2 e = ld_in(ph + j);
         int c = 0;
         while (c < nv && !(val[c].x == e.x && val[c].y == e.y)) ++c;
         if (c == nv) {
@@ -1767,13 +1805,13 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       const int k = i / a.G, h = i % a.G;
       double2 v = make_double2(0.0, 0.0);  // entry n_bil * G: the padding records' zero
       if (i < a.n_bil * a.G) {
-        double2 t = amp[k];
+        double2 t = ld_in(amp + k);
         if (gw) {  // the hop i -> j in the site gauge: t w_j conj(w_i)
-          const double2 wi = gw[a.bil_dev[2 * k]], wj = gw[a.bil_dev[2 * k + 1]];
+          const double2 wi = ld_in(gw + a.bil_dev[2 * k]), wj = ld_in(gw + a.bil_dev[2 * k + 1]);
           const double2 q = make_double2(wj.x * wi.x + wj.y * wi.y, wj.y * wi.x - wj.x * wi.y);
           t = make_double2(t.x * q.x - t.y * q.y, t.x * q.y + t.y * q.x);
         }
-        const double2 c0 = chi[h], bk = s_basek[h];
+        const double2 c0 = s_chi[h], bk = s_basek[h];
         const double2 c = make_double2(c0.x * bk.x + c0.y * bk.y, c0.y * bk.x - c0.x * bk.y);  // chi conj(base^k)
         v = make_double2(t.x * c.x + t.y * c.y, t.x * c.y - t.y * c.x);                       // conj(t) chi'
       }
@@ -1792,8 +1830,9 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
     const PhaseClasses<V> pcl{pmode, a.kp1, s_mask, reinterpret_cast<const V*>(sizeof(V) == 8 ? (void*)s_pw32 : (void*)s_pw64)};
     const PhaseClasses<double2> pcl64{pmode, a.kp1, s_mask, s_pw64};
     for (int i = threadIdx.x; i < a.G * a.N; i += blockDim.x) {
-      s_eta[i].x = phase[i].x;
-      s_eta[i].y = phase[i].y;
+      const double2 e = ld_in(phase + i);
+      s_eta[i].x = e.x;
+      s_eta[i].y = e.y;
     }
     __syncthreads();
     // ---- sector membership (SRE:534-542) and the hop count of one matvec
@@ -1830,12 +1869,16 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
         a.delta[b] = 0.0;
         for (int i = 0; i < a.nev; ++i) a.evals[(size_t)b * a.nev + i] = nan("");
         a.t_ns[2 * (size_t)b + 1] = global_ns();
+        if (a.ring_done) {
+          __threadfence_system();
+          *reinterpret_cast<volatile unsigned int*>(a.ring_done + b) = q_seq + 1u;
+        }
       }
       continue;
     }
     // ---- start vector (same generator as the single-sector path)
     double nrm = 0.0;
-    const uint64_t seed = a.seeds[b];
+    const uint64_t seed = __ldcg(a.seeds + b);
     for (int64_t o = threadIdx.x; o < a.n_orb; o += blockDim.x) {
       double2 v = make_double2(0.0, 0.0);
       if (rowflag[o]) {
@@ -2203,6 +2246,10 @@ __global__ void __launch_bounds__(kBT, 1) k_batch(BatchArgs a, BatchSmem L) {
       a.nmv[b] = nmv + n64;
       a.delta[b] = dmax;
       a.t_ns[2 * (size_t)b + 1] = global_ns();
+      if (a.ring_done) {
+        __threadfence_system();
+        *reinterpret_cast<volatile unsigned int*>(a.ring_done + b) = q_seq + 1u;
+      }
     }
   }
 }
@@ -2212,7 +2259,8 @@ struct BatchImpl {
   std::shared_ptr<CatalogImpl> cat;
   int precision = 1, nev = 4, m = 30, max_req = 0, n_bil = 0, n_den = 0, n_cta = 1;
   int tchi_n = 1, tchi_mul = 1;  // coefficient table slots (prime) and hashing multiplier
-  std::vector<int32_t> bil_ij;
+  std::vector<int32_t> bil_ij, den_ij;
+  std::vector<double> den_v;
   TermTables tt;
   DevBuf site_off, rec, diag, V, R, W, X64, tchi64, rowflag;
   DevBuf in_chi, in_phase, in_amp, in_seed, o_evals, o_status, o_dims, o_delta, o_nmv, o_hops, o_tns, queue;
@@ -2251,6 +2299,31 @@ struct BatchImpl {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   bool fermi = false;
+  // ring mode (sed_batch_ring_*): one persistent launch fed from a request
+  // ring; mapped host memory carries the published tail, the stop flag, the
+  // done flags and every request's outputs, device memory the slots' inputs
+  struct Ring {
+    bool on = false;
+    int cap = 0, n_cta = 0, spin = 0, fp64 = 0;
+    unsigned int next = 0;  // the next request's sequence number
+    int64_t launches = 0;
+    unsigned int* tail = nullptr;  // mapped host allocations (host pointers)
+    int* stop = nullptr;
+    unsigned int* done = nullptr;
+    double* evals = nullptr;
+    int32_t* status = nullptr;
+    int64_t* dims = nullptr;
+    double* delta = nullptr;
+    int32_t* nmv = nullptr;
+    int64_t* hops = nullptr;
+    int64_t* tns = nullptr;
+    DevBuf chi, phase, amp, seed, gw, head;
+    std::vector<char> busy;  // slot holds a request not yet collected
+    cudaStream_t stream = nullptr, copy = nullptr;
+    BatchArgs args{};
+    BatchSmem L{};
+    std::shared_ptr<BatchImpl> redo;  // FP64 batch for requests whose polish missed its target
+  } ring;
   // the captured launch (queue reset + persistent kernel) and the launch
   // configuration it was captured for
   std::vector<unsigned char> graph_key;
@@ -2268,7 +2341,9 @@ struct BatchImpl {
     graph = nullptr;
     graph_key.clear();
   }
+  void ring_free();
   ~BatchImpl() {
+    ring_free();
     drop_graph();
     if (capture_stream) cudaStreamDestroy(capture_stream);
     if (own_stream && stream) cudaStreamDestroy(stream);
@@ -2994,6 +3069,8 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   B->max_req = max_req;
   B->n_bil = n_bil;
   B->n_den = n_den;
+  B->den_ij.assign(den_ij, den_ij + 2 * n_den);
+  B->den_v.assign(den_v, den_v + 2 * n_den);
   B->fermi = G.stats == 1;
   B->bil_ij.assign(bil_ij, bil_ij + 2 * n_bil);
   // hop records: to-site | term index << 8, grouped by from-site
@@ -3282,6 +3359,7 @@ void batch_launch_device(BatchImpl& B, int n_req, const double* chi, const doubl
   SED_REQUIRE(tol > 0.0 && maxiter >= 1, 1, "tol and maxiter must be positive");
   SED_REQUIRE(chi && phase && seeds && evals && status && dims && delta && nmv, 1, "NULL argument");
   SED_REQUIRE(B.n_bil == 0 || amp, 1, "NULL bilinear amplitudes");
+  SED_REQUIRE(!B.ring.on, 1, "the batch's request ring is running: stop it before a batch run");
   B.last_n = n_req;
   B.n_fallback = 0;
   if (n_req == 0) return;
@@ -3407,6 +3485,242 @@ void batch_run(BatchImpl& B, int n_req, const double* chi, const double* phase, 
   if (delta) SED_CUDA(cudaMemcpyAsync(delta, B.o_delta.p, (size_t)n_req * 8, cudaMemcpyDeviceToHost, s));
   if (nmv) SED_CUDA(cudaMemcpyAsync(nmv, B.o_nmv.p, (size_t)n_req * 4, cudaMemcpyDeviceToHost, s));
   SED_CUDA(cudaStreamSynchronize(s));
+}
+
+// ------------------------------------------------------------ ring mode
+// A device-resident request loop: one persistent launch of the batched kernel
+// whose blocks claim requests from a ring as the host publishes them
+// (k_batch's ring_* arguments).  A request starts as soon as a block is free,
+// with no launch per batch; a block that stays idle for idle_ms leaves, and
+// the host relaunches when work arrives while no block is left.  The ring
+// uses the site-gauge hop table, which does not depend on the requests, so
+// every request must have a site gauge.  A request whose mixed-precision
+// polish missed its target is re-solved by an FP64 batch when collected.
+
+template <class T>
+static T* host_mapped(size_t n) {
+  void* p = nullptr;
+  SED_CUDA(cudaHostAlloc(&p, std::max<size_t>(n, 1) * sizeof(T), cudaHostAllocMapped));
+  std::memset(p, 0, std::max<size_t>(n, 1) * sizeof(T));
+  return static_cast<T*>(p);
+}
+template <class T>
+static T* device_view(T* host) {
+  void* d = nullptr;
+  SED_CUDA(cudaHostGetDevicePointer(&d, host, 0));
+  return static_cast<T*>(d);
+}
+
+void BatchImpl::ring_free() {
+  Ring& r = ring;
+  if (r.on && r.stop) {
+    *reinterpret_cast<volatile int*>(r.stop) = 1;
+    if (r.stream) cudaStreamSynchronize(r.stream);  // every block leaves within one idle wait
+  }
+  for (void* p : {(void*)r.tail, (void*)r.stop, (void*)r.done, (void*)r.evals, (void*)r.status, (void*)r.dims,
+                  (void*)r.delta, (void*)r.nmv, (void*)r.hops, (void*)r.tns})
+    if (p) cudaFreeHost(p);
+  if (r.stream) cudaStreamDestroy(r.stream);
+  if (r.copy) cudaStreamDestroy(r.copy);
+  r = Ring{};
+}
+
+static void ring_launch(BatchImpl& B) {
+  BatchImpl::Ring& r = B.ring;
+  BatchSmem L = r.L;
+  dispatch_launch(B, r.args, L, r.n_cta, r.stream, r.fp64 != 0);
+  ++r.launches;
+}
+
+static bool ring_running(BatchImpl& B) {
+  const cudaError_t e = cudaStreamQuery(B.ring.stream);
+  if (e == cudaErrorNotReady) {
+    cudaGetLastError();  // "not ready" is a state, not an error: leave no trace of it
+    return true;
+  }
+  SED_CUDA(e);
+  return false;
+}
+
+void batch_ring_start(BatchImpl& B, int cap, int n_blocks, int idle_ms) {
+  SED_REQUIRE(!B.ring.on, 1, "the ring is already running");
+  SED_REQUIRE(cap >= 1 && cap <= (1 << 20), 1, "ring capacity must be between 1 and 2^20");
+  SED_REQUIRE(n_blocks >= 1, 1, "n_blocks must be positive");
+  SED_REQUIRE(idle_ms >= 1 && idle_ms <= 60000, 1, "idle_ms must be between 1 and 60000");
+  SED_REQUIRE(B.phi_cap > 0 && B.tab_enabled, 5, "ring mode needs the shared-memory hop table of this catalog");
+  const GroupImpl& G = *B.cat->group;
+  cudaStream_t s = B.stream;
+  SED_REQUIRE(prepare_table(B, 0, nullptr, s, true), 5, "ring mode needs the site-gauge hop table");
+  SED_CUDA(cudaStreamSynchronize(s));
+  BatchImpl::Ring& r = B.ring;
+  r = BatchImpl::Ring{};
+  r.cap = cap;
+  r.spin = (int)std::max<int64_t>(1, (int64_t)idle_ms * 1000 / 20);  // 20 us per idle wait
+  r.fp64 = B.precision == 0 ? 1 : 0;
+  r.tail = host_mapped<unsigned int>(1);
+  r.stop = host_mapped<int>(1);
+  r.done = host_mapped<unsigned int>(cap);
+  r.evals = host_mapped<double>((size_t)cap * B.nev);
+  r.status = host_mapped<int32_t>(cap);
+  r.dims = host_mapped<int64_t>(cap);
+  r.delta = host_mapped<double>(cap);
+  r.nmv = host_mapped<int32_t>(cap);
+  r.hops = host_mapped<int64_t>(cap);
+  r.tns = host_mapped<int64_t>((size_t)cap * 2);
+  r.chi.alloc((size_t)cap * G.n_ops * 16);
+  r.phase.alloc((size_t)cap * G.n_ops * G.n_site * 16);
+  r.amp.alloc((size_t)cap * std::max(B.n_bil, 1) * 16);
+  r.seed.alloc((size_t)cap * 8);
+  r.gw.alloc((size_t)cap * G.n_site * 16);
+  r.head.alloc(16);
+  SED_CUDA(cudaMemset(r.head.p, 0, 16));
+  r.busy.assign(cap, 0);
+  SED_CUDA(cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking));
+  SED_CUDA(cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking));
+  BatchArgs a = base_args(B);
+  a.n_req = 0;
+  a.tol = 1e-10;
+  a.maxiter = 300;
+  a.chi = r.chi.as<double2>();
+  a.phase = r.phase.as<double2>();
+  a.amp = r.amp.as<double2>();
+  a.seeds = r.seed.as<uint64_t>();
+  a.V = B.V.as<double2>();
+  a.R = B.R.as<double2>();
+  a.W = B.W.as<double2>();
+  a.X64 = B.X64.as<double2>();
+  a.tchi64 = B.tchi64.as<double2>();
+  a.rowflag = B.rowflag.as<uint8_t>();
+  a.evals = device_view(r.evals);
+  a.status = device_view(r.status);
+  a.dims = device_view(r.dims);
+  a.delta = device_view(r.delta);
+  a.nmv = device_view(r.nmv);
+  a.hops = device_view(r.hops);
+  a.t_ns = device_view(r.tns);
+  a.queue = r.head.as<unsigned int>();
+  a.use_tab = 1;
+  a.gauge = 1;
+  a.gauge_w = r.gw.as<double2>();
+  a.n_phi = B.n_phi;
+  a.hop = B.hop.as<uint64_t>();
+  a.sl_off = B.sl_off.as<uint32_t>();
+  a.sl_w = B.sl_w.as<int32_t>();
+  a.phi_desc = B.phi_desc.as<uint32_t>();
+  a.rep_site = B.rep_site.as<int8_t>();
+  a.pwc64 = B.pwc64.as<double2>();
+  // launch shape: pinned, from the environment, remembered for this catalog
+  // shape, else the batch's default (no timing runs: there are no requests yet)
+  int m = B.m, tpr = 1;
+  if (B.pin_m > 0) {
+    m = B.pin_m;
+    tpr = B.pin_tpr;
+  } else if (!env_batch_shape(&m, &tpr)) {
+    const BatchShapeKey key{B.cat->n_orbits, B.tt.n_terms, G.n_ops, G.n_site, B.fermi ? 1 : 0, B.precision, B.nev,
+                            1, 1, B.m_fixed ? B.m : 0};
+    std::lock_guard<std::mutex> lock(g_bshape_mu);
+    auto it = g_bshapes.find(key);
+    if (it != g_bshapes.end()) {
+      m = it->second.first;
+      tpr = it->second.second;
+    }
+  }
+  a.m = std::min(std::max(m, 2 * (B.nev + 2) + 1), B.m_cap);
+  a.tpr = tpr == 2 ? 2 : 1;
+  a.ring_tail = device_view(r.tail);
+  a.ring_stop = device_view(r.stop);
+  a.ring_done = device_view(r.done);
+  a.ring_cap = cap;
+  a.ring_spin = r.spin;
+  BatchSmem L;
+  int ncta = 1;
+  dispatch_prepare(B, a, L, ncta, r.fp64 != 0);
+  r.n_cta = std::min({ncta, n_blocks, B.n_cta});
+  r.args = a;
+  r.L = L;
+  r.on = true;
+}
+
+int64_t batch_ring_submit(BatchImpl& B, const double* chi, const double* phase, const double* amp, uint64_t seed) {
+  BatchImpl::Ring& r = B.ring;
+  SED_REQUIRE(r.on, 1, "the ring is not running");
+  SED_REQUIRE(chi && phase && (B.n_bil == 0 || amp), 1, "NULL argument");
+  const GroupImpl& G = *B.cat->group;
+  validate_requests(B, 1, phase, amp);
+  std::vector<double> w;
+  SED_REQUIRE(site_gauges(G, 1, phase, w), 1,
+              "ring mode needs a site gauge for every request (flux-twisted translation groups have one)");
+  const unsigned int q = r.next;
+  const int slot = (int)(q % (unsigned int)r.cap);
+  SED_REQUIRE(!r.busy[slot], 5, "the request ring is full: collect finished requests first");
+  const size_t nG = G.n_ops, N = G.n_site;
+  SED_CUDA(cudaMemcpyAsync(r.chi.as<double>() + (size_t)slot * nG * 2, chi, nG * 16, cudaMemcpyHostToDevice, r.copy));
+  SED_CUDA(cudaMemcpyAsync(r.phase.as<double>() + (size_t)slot * nG * N * 2, phase, nG * N * 16,
+                           cudaMemcpyHostToDevice, r.copy));
+  if (B.n_bil)
+    SED_CUDA(cudaMemcpyAsync(r.amp.as<double>() + (size_t)slot * B.n_bil * 2, amp, (size_t)B.n_bil * 16,
+                             cudaMemcpyHostToDevice, r.copy));
+  SED_CUDA(cudaMemcpyAsync(r.seed.as<uint64_t>() + slot, &seed, 8, cudaMemcpyHostToDevice, r.copy));
+  SED_CUDA(cudaMemcpyAsync(r.gw.as<double>() + (size_t)slot * N * 2, w.data(), N * 16, cudaMemcpyHostToDevice,
+                           r.copy));
+  SED_CUDA(cudaStreamSynchronize(r.copy));
+  r.busy[slot] = 1;
+  r.next = q + 1;
+  __atomic_store_n(r.tail, q + 1, __ATOMIC_RELEASE);  // publish: the slot's inputs are in place
+  if (!ring_running(B)) ring_launch(B);
+  return (int64_t)q;
+}
+
+// true when the ticket has finished (outputs filled, ticket released)
+bool batch_ring_wait(BatchImpl& B, int64_t ticket, int timeout_ms, double* evals, int32_t* status, int64_t* dim) {
+  BatchImpl::Ring& r = B.ring;
+  SED_REQUIRE(r.on, 1, "the ring is not running");
+  SED_REQUIRE(ticket >= 0 && (uint64_t)ticket < (uint64_t)r.next && (uint64_t)r.next - (uint64_t)ticket <= (uint64_t)r.cap,
+              1, "unknown ticket");
+  const unsigned int q = (unsigned int)ticket;
+  const int slot = (int)(q % (unsigned int)r.cap);
+  SED_REQUIRE(r.busy[slot], 1, "ticket already collected");
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    if (__atomic_load_n(r.done + slot, __ATOMIC_ACQUIRE) == q + 1) break;
+    // the blocks leave when idle; relaunch if this request is still queued
+    if (!ring_running(B) && __atomic_load_n(r.done + slot, __ATOMIC_ACQUIRE) != q + 1) ring_launch(B);
+    const double el = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (el >= timeout_ms) return false;
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  int32_t st = r.status[slot];
+  for (int i = 0; i < B.nev; ++i) evals[i] = r.evals[(size_t)slot * B.nev + i];
+  int64_t d = r.dims[slot];
+  if (st == kPolishFailed) {
+    // the FP64 batch answers this request (same inputs, same seed)
+    if (!r.redo) {
+      r.redo = make_batch(B.cat, B.n_bil, B.bil_ij.data(), B.n_den, B.den_ij.data(), B.den_v.data(), 0, B.nev, 0, 1);
+    }
+    const GroupImpl& G = *B.cat->group;
+    std::vector<double> chi((size_t)G.n_ops * 2), ph((size_t)G.n_ops * G.n_site * 2), amp((size_t)std::max(B.n_bil, 1) * 2);
+    uint64_t seed = 0;
+    SED_CUDA(cudaMemcpy(chi.data(), r.chi.as<double>() + (size_t)slot * G.n_ops * 2, chi.size() * 8,
+                        cudaMemcpyDeviceToHost));
+    SED_CUDA(cudaMemcpy(ph.data(), r.phase.as<double>() + (size_t)slot * G.n_ops * G.n_site * 2, ph.size() * 8,
+                        cudaMemcpyDeviceToHost));
+    if (B.n_bil)
+      SED_CUDA(cudaMemcpy(amp.data(), r.amp.as<double>() + (size_t)slot * B.n_bil * 2, (size_t)B.n_bil * 16,
+                          cudaMemcpyDeviceToHost));
+    SED_CUDA(cudaMemcpy(&seed, r.seed.as<uint64_t>() + slot, 8, cudaMemcpyDeviceToHost));
+    double delta = 0;
+    int32_t nmv = 0;
+    batch_run(*r.redo, 1, chi.data(), ph.data(), amp.data(), &seed, 1e-10, 300, evals, &st, &d, &delta, &nmv);
+  }
+  if (status) *status = st;
+  if (dim) *dim = d;
+  r.busy[slot] = 0;
+  return true;
+}
+
+void batch_ring_stop(BatchImpl& B) {
+  SED_REQUIRE(B.ring.on, 1, "the ring is not running");
+  B.ring_free();
 }
 
 void batch_last_stats(const BatchImpl& B, int64_t* hops, int64_t* t0, int64_t* t1) {
@@ -3550,6 +3864,43 @@ int sed_batch_run_device(sed_batch* b, int n_req, const double* d_chi, const dou
   });
 }
 
+int sed_batch_ring_start(sed_batch* b, int capacity, int n_blocks, int idle_ms) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    sed::batch_ring_start(*b->p, capacity, n_blocks, idle_ms);
+  });
+}
+int sed_batch_ring_submit(sed_batch* b, const double* chi_reim, const double* group_phase_reim,
+                          const double* bil_t_reim, uint64_t seed, int64_t* ticket) {
+  return bguard([&] {
+    SED_REQUIRE(b && ticket, 1, "NULL argument");
+    *ticket = sed::batch_ring_submit(*b->p, chi_reim, group_phase_reim, bil_t_reim, seed);
+  });
+}
+int sed_batch_ring_wait(sed_batch* b, int64_t ticket, int timeout_ms, double* evals, int32_t* status,
+                        int64_t* dim) {
+  return bguard([&] {
+    SED_REQUIRE(b && evals, 1, "NULL argument");
+    SED_REQUIRE(sed::batch_ring_wait(*b->p, ticket, std::max(timeout_ms, 0), evals, status, dim), SED_ERR_TIMEOUT,
+                "request not finished");
+  });
+}
+int sed_batch_ring_info(const sed_batch* b, int64_t* launches, int32_t* n_blocks, int32_t* running) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    sed::BatchImpl& B = *b->p;
+    if (launches) *launches = B.ring.launches;
+    if (n_blocks) *n_blocks = B.ring.n_cta;
+    if (running) *running = B.ring.on && B.ring.stream && cudaStreamQuery(B.ring.stream) == cudaErrorNotReady;
+    cudaGetLastError();  // the query's not-ready status is not an error
+  });
+}
+int sed_batch_ring_stop(sed_batch* b) {
+  return bguard([&] {
+    SED_REQUIRE(b, 1, "NULL batch");
+    sed::batch_ring_stop(*b->p);
+  });
+}
 int sed_batch_set_stream(sed_batch* b, void* stream) {
   return bguard([&] {
     SED_REQUIRE(b, 1, "NULL batch");

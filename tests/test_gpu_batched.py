@@ -385,3 +385,60 @@ def test_batch_launch_autotuner(oracle):
             ref = np.linalg.eigvalsh(op.dense())
             assert_lanczos_spectrum(out["evals"][b, :min(5, sec.dim)], ref, 1e-9 * max(1.0, abs(ref[0])))
     s2.set_shape(0, 0)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_device_resident_request_loop(oracle, precision):
+    """The device-resident loop (sed_batch_ring_*): requests submitted one at
+    a time to a running persistent launch give the batch run's eigenvalues
+    (same seeds; within the path's tolerance) and the oracle's spectra; a
+    full ring refuses a submit until a ticket is collected; blocks that stay
+    idle leave and the next submit relaunches; a batch run is refused while
+    the ring runs."""
+    import time
+
+    from realspace_exactdiagonalization_gb300 import _lib
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.haldane_honeycomb(2, 4)
+    reqs = flux_scan_requests(spec, TWISTS)
+    ref = _solver(spec, precision).run(reqs)
+    solver = _solver(spec, precision)
+    solver.ring_start(capacity=16, n_blocks=8, idle_ms=50)
+    try:
+        with pytest.raises(_lib.SEDError):
+            solver.run(reqs[:2])
+        got = np.full_like(ref["evals"], np.nan)
+        dims = np.zeros(len(reqs), dtype=np.int64)
+        pending = []
+        for i, r in enumerate(reqs):
+            while True:
+                try:
+                    pending.append((i, solver.ring_submit(r)))
+                    break
+                except _lib.SEDError as e:
+                    assert e.code == _lib.SED_ERR_LIMIT and len(pending) == 16
+                    j, t = pending.pop(0)
+                    ev, st, dims[j] = solver.ring_wait(t)
+                    assert st == 0
+                    got[j] = ev
+        for j, t in pending:
+            ev, st, dims[j] = solver.ring_wait(t)
+            assert st == 0
+            got[j] = ev
+        np.testing.assert_array_equal(dims, ref["dims"])
+        ok = ref["dims"] > 0
+        tol = 1e-9 if precision == "mixed" else 1e-11
+        np.testing.assert_allclose(got[ok, 0], ref["evals"][ok, 0], rtol=tol, atol=1e-12)
+        _assert_oracle_spectra(oracle, "haldane2x4", spec, TWISTS, {"dims": dims, "evals": got})
+        launches = solver.ring_info()["launches"]
+        time.sleep(0.5)  # longer than idle_ms: the blocks leave
+        assert not solver.ring_info()["running"]
+        t = solver.ring_submit(reqs[3])
+        ev, st, _ = solver.ring_wait(t)
+        assert st == 0 and solver.ring_info()["launches"] > launches
+        np.testing.assert_allclose(ev[0], ref["evals"][3, 0], rtol=tol, atol=1e-12)
+    finally:
+        solver.ring_stop()
+    out = solver.run(reqs[:4])  # the object runs batches again after the ring
+    assert (out["status"] == 0).all()
