@@ -406,6 +406,12 @@ def run_ours(args, rank, world):
                      "peak_kind": peak_kind, "kernel": "k_batch (persistent batched Lanczos)",
                      "bytes_per_launch": bytes_launch, "matvec_bytes_per_launch": bytes_mv,
                      "lanczos_bytes_per_launch": bytes_lz, "frac_matvec_bytes_only": bytes_mv / t_launch / 1e9 / peak,
+                     # the DRAM side: the profiled traffic over this run's launch time.  The
+                     # algorithmic bytes above include the gathers that shared memory and L2
+                     # serve, so `frac` can pass 1 while DRAM stays far below its peak
+                     "traffic_gbs": (lambda t: t * n / t_launch / 1e9 if t else None)(profiled_traffic_per_sector()),
+                     "traffic_frac": (lambda t: t * n / t_launch / 1e9 / peak if t else None)(
+                         profiled_traffic_per_sector()),
                      "note": "algorithmic bytes of one launch: every matvec D*(8+4+2s)+hops*(4+1+4+s) (s=8), plus "
                              "every Lanczos iteration's (3+k)*D*8 (three complex64 vector streams and the "
                              "reorthogonalisation's read of the k basis vectors) and every restart's "
@@ -680,6 +686,8 @@ def run_served(args):
         part["medium_max_batch"] = args.served_medium_batch
     if args.served_large_sms:
         part["large_sm_limit"] = args.served_large_sms
+    if args.served_ring_blocks:
+        part["ring_blocks"] = args.served_ring_blocks
     line = served_report(args.served_n, args.served_rate, args.large_workers, plain_all=not args.plain_sampled,
                          plain_per_family=args.plain_per_family, partition=part, native=args.served_native)
     line["partition"] = part
@@ -713,6 +721,8 @@ def main():
                     help="served: catalogs up to this many orbits take the mid-size batch lane")
     ap.add_argument("--served-medium-batch", type=int, default=None,
                     help="served: requests (so SMs) of one mid-size batch launch")
+    ap.add_argument("--served-ring-blocks", type=int, default=0,
+                    help="served: batched families run a device-resident request loop on up to this many SMs")
     ap.add_argument("--served-native", action="store_true",
                     help="served: use the library's native server (sed_server_*) instead of the Python scheduler")
     ap.add_argument("--served-large-sms", type=int, default=0,

@@ -2323,6 +2323,9 @@ struct BatchImpl {
     BatchArgs args{};
     BatchSmem L{};
     std::shared_ptr<BatchImpl> redo;  // FP64 batch for requests whose polish missed its target
+    // submit and wait may be called from different host threads (one
+    // submitting, one collecting): the host-side ring state is guarded
+    std::shared_ptr<std::mutex> mu = std::make_shared<std::mutex>();
   } ring;
   // the captured launch (queue reset + persistent kernel) and the launch
   // configuration it was captured for
@@ -3643,6 +3646,7 @@ void batch_ring_start(BatchImpl& B, int cap, int n_blocks, int idle_ms) {
 
 int64_t batch_ring_submit(BatchImpl& B, const double* chi, const double* phase, const double* amp, uint64_t seed) {
   BatchImpl::Ring& r = B.ring;
+  std::lock_guard<std::mutex> lock(*r.mu);
   SED_REQUIRE(r.on, 1, "the ring is not running");
   SED_REQUIRE(chi && phase && (B.n_bil == 0 || amp), 1, "NULL argument");
   const GroupImpl& G = *B.cat->group;
@@ -3674,21 +3678,30 @@ int64_t batch_ring_submit(BatchImpl& B, const double* chi, const double* phase, 
 // true when the ticket has finished (outputs filled, ticket released)
 bool batch_ring_wait(BatchImpl& B, int64_t ticket, int timeout_ms, double* evals, int32_t* status, int64_t* dim) {
   BatchImpl::Ring& r = B.ring;
-  SED_REQUIRE(r.on, 1, "the ring is not running");
-  SED_REQUIRE(ticket >= 0 && (uint64_t)ticket < (uint64_t)r.next && (uint64_t)r.next - (uint64_t)ticket <= (uint64_t)r.cap,
-              1, "unknown ticket");
   const unsigned int q = (unsigned int)ticket;
-  const int slot = (int)(q % (unsigned int)r.cap);
-  SED_REQUIRE(r.busy[slot], 1, "ticket already collected");
+  int slot = 0;
+  {
+    std::lock_guard<std::mutex> lock(*r.mu);
+    SED_REQUIRE(r.on, 1, "the ring is not running");
+    SED_REQUIRE(ticket >= 0 && (uint64_t)ticket < (uint64_t)r.next &&
+                    (uint64_t)r.next - (uint64_t)ticket <= (uint64_t)r.cap,
+                1, "unknown ticket");
+    slot = (int)(q % (unsigned int)r.cap);
+    SED_REQUIRE(r.busy[slot], 1, "ticket already collected");
+  }
   const auto t0 = std::chrono::steady_clock::now();
   for (;;) {
     if (__atomic_load_n(r.done + slot, __ATOMIC_ACQUIRE) == q + 1) break;
-    // the blocks leave when idle; relaunch if this request is still queued
-    if (!ring_running(B) && __atomic_load_n(r.done + slot, __ATOMIC_ACQUIRE) != q + 1) ring_launch(B);
+    {
+      // the blocks leave when idle; relaunch if this request is still queued
+      std::lock_guard<std::mutex> lock(*r.mu);
+      if (!ring_running(B) && __atomic_load_n(r.done + slot, __ATOMIC_ACQUIRE) != q + 1) ring_launch(B);
+    }
     const double el = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (el >= timeout_ms) return false;
     std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
+  std::lock_guard<std::mutex> lock(*r.mu);
   int32_t st = r.status[slot];
   for (int i = 0; i < B.nev; ++i) evals[i] = r.evals[(size_t)slot * B.nev + i];
   int64_t d = r.dims[slot];

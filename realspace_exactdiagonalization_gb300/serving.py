@@ -148,12 +148,18 @@ class SectorServer:
                  precision: str = "mixed", tol: float = 1e-10, nev: int = 1,
                  medium_max_orbits: int = MEDIUM_MAX_ORBITS, medium_lanes: int = 1,
                  priority_max_orbits: int = PRIORITY_MAX_ORBITS, warm_up: bool = True,
-                 medium_max_batch: int = MEDIUM_MAX_BATCH, large_sm_limit: int = 0):
+                 medium_max_batch: int = MEDIUM_MAX_BATCH, large_sm_limit: int = 0, ring_blocks: int = 0,
+                 ring_idle_ms: int = 100):
         self.budget = float(budget_bytes)
         # device-wide solves size their grids for this many SMs (0: all); the
         # mid-size lane's persistent blocks (at most medium_max_batch of them,
         # one SM each) keep the rest
         self.large_sm_limit = int(large_sm_limit)
+        # ring_blocks > 0: each batched family runs a device-resident request
+        # loop (sed_batch_ring_*) on up to that many SMs instead of batch
+        # lanes; requests go straight into its ring
+        self.ring_blocks = int(ring_blocks)
+        self.ring_idle_ms = int(ring_idle_ms)
         self.priority_max_orbits = priority_max_orbits
         self.precision = precision
         self.tol = tol
@@ -175,7 +181,10 @@ class SectorServer:
             self.resident += cat.n_states * 8 + cat.n_orbits * 9
             if route != "large":
                 cap = max_batch if route == "batch" else min(max_batch, medium_max_batch)
-                for _ in range(batch_lanes if route == "batch" else medium_lanes):
+                n_solvers = batch_lanes if route == "batch" else medium_lanes
+                if route == "batch" and self.ring_blocks > 0:
+                    n_solvers = 1
+                for _ in range(n_solvers):
                     s = BatchedSectorSolver(cat, pairs, spec.density_terms, precision=precision, nev=nev,
                                             max_requests=cap)
                     fam.solvers.append(s)
@@ -196,6 +205,12 @@ class SectorServer:
         self.peak_reserved = 0.0
         if warm_up:
             self.warm_up()
+        self._ring_q: Dict[str, "queue.Queue"] = {}
+        if self.ring_blocks > 0:
+            for fam in self.families.values():
+                if fam.route == "batch":
+                    fam.solvers[0].ring_start(capacity=1024, n_blocks=self.ring_blocks, idle_ms=self.ring_idle_ms)
+                    self._ring_q[fam.name] = queue.Queue()
 
     def warm_up(self, max_wave: int = 152) -> None:
         """Before any request arrives, run one wave of every batched family's
@@ -261,6 +276,26 @@ class SectorServer:
                     self._done.append(r)
                 self._lock.notify_all()
 
+    def _ring_collector(self, fam_name: str):
+        """Collect a family's ring tickets in submission order."""
+        fam = self.families[fam_name]
+        q = self._ring_q[fam_name]
+        while True:
+            item = q.get()
+            if item is None:
+                return
+            ticket, r = item
+            try:
+                ev, st, dim = fam.solvers[0].ring_wait(ticket)
+                r.evals, r.status, r.dim = ev[: r.nev].copy(), st, dim
+            except A._lib.SEDError as e:
+                r.status, r.evals, r.error = e.code, np.full(r.nev, np.nan), str(e)
+            t_end = self._now()
+            with self._lock:
+                r.t_start, r.t_end, r.route = r.arrival, t_end, "ring"
+                self._done.append(r)
+                self._lock.notify_all()
+
     def _large_worker(self):
         pending = self._pending["large"]
         while True:
@@ -313,11 +348,18 @@ class SectorServer:
         self._threads += [threading.Thread(target=self._batch_lane, args=("medium", i), daemon=True)
                           for i in range(self.n_medium)]
         self._threads += [threading.Thread(target=self._large_worker, daemon=True) for _ in range(self.n_large)]
-        for t in self._threads:
+        self._ring_threads = [threading.Thread(target=self._ring_collector, args=(name,), daemon=True)
+                              for name in self._ring_q]
+        for t in self._threads + self._ring_threads:
             t.start()
 
     def submit(self, r: Request) -> None:
         fam = self.families[r.family]
+        if fam.name in self._ring_q:  # straight into the family's device-resident loop
+            r.arrival = self._now()
+            ticket = fam.solvers[0].ring_submit(self._request_arrays(fam, [r])[0])
+            self._ring_q[fam.name].put((ticket, r))
+            return
         with self._lock:
             r.arrival = self._now()
             self._pending[fam.route].append(r)
@@ -327,8 +369,13 @@ class SectorServer:
         with self._lock:
             self._closed = True
             self._lock.notify_all()
-        for t in self._threads:
+        for q in self._ring_q.values():
+            q.put(None)
+        for t in self._threads + getattr(self, "_ring_threads", []):
             t.join()
+        for name in self._ring_q:
+            self.families[name].solvers[0].ring_stop()
+        self._ring_q = {}
         return list(self._done)
 
     def serve(self, requests: Sequence[Request], time_scale: float = 1.0) -> List[Request]:

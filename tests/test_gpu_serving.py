@@ -192,3 +192,24 @@ def test_native_server_matches_oracle(oracle):
         assert e.value.code == _lib.SED_ERR_ARG
     finally:
         srv.close()
+
+
+def test_served_mix_through_device_resident_loops(oracle):
+    """ring_blocks > 0: the batched families are answered by device-resident
+    request loops (sed_batch_ring_*), each request submitted straight into its
+    family's ring; the answers are the oracle's ground energies (1e-9)."""
+    from realspace_exactdiagonalization_gb300.serving import SectorServer, random_requests
+
+    fams = _families()
+    reqs = random_requests(fams, 36, rate=0.0, seed=9, nev=1)
+    srv = SectorServer(fams, budget_bytes=8e9, batch_lanes=2, large_workers=2, small_max_orbits=300,
+                       ring_blocks=8, ring_idle_ms=50)
+    done = sorted(srv.serve(reqs), key=lambda r: r.rid)
+    assert len(done) == len(reqs) and all(r.status == 0 for r in done), [r.error for r in done if r.status]
+    assert {r.route for r in done if srv.families[r.family].route == "batch"} == {"ring"}
+    for r in done:
+        _, sec, op = oracle_objects(oracle, Case(r.family, fams[r.family], theta=r.twist), r.k_index)
+        assert r.dim == sec.dim
+        if sec.dim:
+            e0 = np.linalg.eigvalsh(op.dense())[0]
+            assert abs(r.evals[0] - e0) <= 1e-9 * max(1.0, abs(e0)), (r.rid, r.family, r.route)
