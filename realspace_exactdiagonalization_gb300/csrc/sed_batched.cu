@@ -2509,6 +2509,7 @@ static void graph_launch(BatchImpl& B, const BatchArgs& a, const BatchSmem& L, i
 // tables; this is the batched counterpart of the reference's projection table
 // (build_projection_table / _apply_table!, SRE:680-765), kept per hop.
 static constexpr int kPhiCap = 2048;  // phase-id entries, the zero entry included
+static constexpr int kGaugePhi = 3;   // gauge mode's phase ids: +1, -1, the padding zero
 
 __global__ void k_hop_count(int64_t n_orb, const uint64_t* __restrict__ reps, const uint16_t* off,
                             const uint32_t* rec, int32_t* __restrict__ cnt) {
@@ -3140,25 +3141,26 @@ std::shared_ptr<BatchImpl> make_batch(std::shared_ptr<CatalogImpl> cp, int n_bil
   // fit too; a sector whose x cannot fit keeps x in global memory (L2) and
   // the hop table.
   constexpr size_t kSmemBudget = 220 * 1024;
-  if (precision == 1) {
-    if (batch_layout<float2>(a, true).total > kSmemBudget) {
-      BatchArgs a0 = a;
-      a0.phi_cap = 0;
-      if (batch_layout<float2>(a0, true).total <= kSmemBudget) {
-        B->phi_cap = 0;
-        a.phi_cap = 0;
-      } else {
-        B->x_smem = false;
-        if (batch_layout<float2>(a, false).total > kSmemBudget) {
-          B->phi_cap = 0;
-          a.phi_cap = 0;
-        }
-      }
+  // phase-id capacity: the full table, else the three entries of gauge mode
+  // (+1, -1 and the padding zero: runs whose requests have site gauges keep
+  // the hop table), else none
+  auto fit_phi = [&](bool xs, auto vt) {
+    using VT = decltype(vt);
+    for (int cap : {kPhiCap, kGaugePhi, 0}) {
+      a.phi_cap = cap;
+      if (batch_layout<VT>(a, xs).total <= kSmemBudget) return true;
     }
-  } else if (batch_layout<double2>(a, false).total > kSmemBudget) {
-    B->phi_cap = 0;
-    a.phi_cap = 0;
+    return false;
+  };
+  if (precision == 1) {
+    if (!fit_phi(true, float2{})) {  // x in global memory only when it fits beside no table at all
+      B->x_smem = false;
+      fit_phi(false, float2{});
+    }
+  } else {
+    fit_phi(false, double2{});
   }
+  B->phi_cap = a.phi_cap;
   BatchSmem L;
   int ncta = 1;
   dispatch_prepare(*B, a, L, ncta, precision == 0);

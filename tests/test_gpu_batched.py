@@ -442,3 +442,27 @@ def test_device_resident_request_loop(oracle, precision):
         solver.ring_stop()
     out = solver.run(reqs[:4])  # the object runs batches again after the ring
     assert (out["status"] == 0).all()
+
+
+def test_gauge_only_phase_table_when_shared_memory_is_tight():
+    """Checkerboard 4x4 with Np = 5 (12,586 orbits): its complex64 x fills so
+    much shared memory that the full phase-id table (2048 entries) does not
+    fit beside it.  The batch then keeps gauge mode's three entries (+1, -1,
+    zero), so flux-scan runs still take the site-gauge hop table, and give the
+    on-the-fly matvec's lowest levels (1e-9)."""
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.checkerboard(4, 4, n_filled=5)
+    reqs = flux_scan_requests(spec, [(0.0, 0.0), (0.3, 0.7)])
+    tab = _solver(spec, "mixed", max_requests=64)
+    out = tab.run(reqs)
+    st = tab.last_stats()
+    assert st["hop_table"] and st["site_gauge"]
+    fly = _solver(spec, "mixed", max_requests=64)
+    fly.set_hop_table(False)
+    ref = fly.run(reqs)
+    assert not fly.last_stats()["hop_table"]
+    assert (out["status"] == 0).all() and (ref["status"] == 0).all()
+    np.testing.assert_array_equal(out["dims"], ref["dims"])
+    ok = ref["dims"] > 0
+    np.testing.assert_allclose(out["evals"][ok, 0], ref["evals"][ok, 0], rtol=1e-9, atol=1e-12)
