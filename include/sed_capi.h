@@ -465,6 +465,11 @@ int sed_server_submit(sed_server* s, int32_t family, const double* chi_reim, con
  * then returns) and its sector dimension, and the ticket is released.
  * SED_ERR_TIMEOUT when it has not finished yet. */
 int sed_server_wait(sed_server* s, int64_t ticket, int timeout_ms, double* evals, int32_t* status, int64_t* dim);
+/* The next request to finish, in completion order (any ticket not yet
+ * collected): its ticket and outputs as sed_server_wait, which releases it.
+ * evals must hold the largest nev submitted.  SED_ERR_TIMEOUT when none
+ * finishes within timeout_ms. */
+int sed_server_next(sed_server* s, int timeout_ms, int64_t* ticket, double* evals, int32_t* status, int64_t* dim);
 /* Requests finished and waiting, the peak device memory reserved by the
  * device-wide solves, and the resident catalogs and batch workspaces. */
 int sed_server_stats(const sed_server* s, int64_t* n_done, int64_t* n_pending, double* peak_reserved_bytes,

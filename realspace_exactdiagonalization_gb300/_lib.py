@@ -108,6 +108,7 @@ SIGNATURES = [
     ("sed_server_add_family", _i32, [_p, _p, _i32, _p, _p, _i32, _p, _p, _i32, _p]),
     ("sed_server_submit", _i32, [_p, _i32, _p, _p, _p, _u64, _i32, _p]),
     ("sed_server_wait", _i32, [_p, _i64, _i32, _p, _p, _p]),
+    ("sed_server_next", _i32, [_p, _i32, _p, _p, _p, _p]),
     ("sed_server_stats", _i32, [_p, _p, _p, _p, _p]),
     ("sed_server_destroy", None, [_p]),
 ]

@@ -85,6 +85,7 @@ struct sed_server {
   std::condition_variable cv;       // work arrived / closing / memory released
   std::condition_variable done_cv;  // a request finished
   std::deque<Request*> pending_batch, pending_large;
+  std::deque<int64_t> finished;  // tickets in completion order, for sed_server_next
   std::map<int64_t, std::unique_ptr<Request>> requests;
   int64_t next_ticket = 1, n_done = 0;
   bool started = false, closed = false;
@@ -97,7 +98,18 @@ struct sed_server {
     std::lock_guard<std::mutex> lock(mu);
     r->done = true;
     ++n_done;
+    finished.push_back(r->ticket);
     done_cv.notify_all();
+  }
+  // copy a finished request's outputs and release its ticket (mu held)
+  void collect(std::map<int64_t, std::unique_ptr<Request>>::iterator it, double* evals, int32_t* status,
+               int64_t* dim) {
+    Request* r = it->second.get();
+    for (int i = 0; i < r->nev; ++i) evals[i] = i < (int)r->evals.size() ? r->evals[i] : std::nan("");
+    if (status) *status = r->status;
+    if (dim) *dim = r->dim;
+    if (r->status != SED_OK) sed::set_error(r->error);
+    requests.erase(it);
   }
 };
 
@@ -388,11 +400,28 @@ int sed_server_wait(sed_server* s, int64_t ticket, int timeout_ms, double* evals
     const bool ready = s->done_cv.wait_for(lock, std::chrono::milliseconds(std::max(timeout_ms, 0)),
                                            [&] { return r->done; });
     SED_REQUIRE(ready, SED_ERR_TIMEOUT, "request not finished");
-    for (int i = 0; i < r->nev; ++i) evals[i] = i < (int)r->evals.size() ? r->evals[i] : std::nan("");
-    if (status) *status = r->status;
-    if (dim) *dim = r->dim;
-    if (r->status != SED_OK) sed::set_error(r->error);
-    s->requests.erase(it);
+    s->collect(it, evals, status, dim);
+  });
+}
+
+int sed_server_next(sed_server* s, int timeout_ms, int64_t* ticket, double* evals, int32_t* status, int64_t* dim) {
+  return sguard([&] {
+    SREQ(s && ticket && evals, "NULL argument");
+    std::unique_lock<std::mutex> lock(s->mu);
+    for (;;) {
+      // skip tickets already collected by sed_server_wait
+      while (!s->finished.empty() && !s->requests.count(s->finished.front())) s->finished.pop_front();
+      if (!s->finished.empty()) break;
+      const bool woke = s->done_cv.wait_for(lock, std::chrono::milliseconds(std::max(timeout_ms, 0)), [&] {
+        while (!s->finished.empty() && !s->requests.count(s->finished.front())) s->finished.pop_front();
+        return !s->finished.empty();
+      });
+      SED_REQUIRE(woke, SED_ERR_TIMEOUT, "no request finished");
+    }
+    const int64_t t = s->finished.front();
+    s->finished.pop_front();
+    *ticket = t;
+    s->collect(s->requests.find(t), evals, status, dim);
   });
 }
 

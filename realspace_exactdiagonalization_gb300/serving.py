@@ -468,20 +468,32 @@ class NativeSectorServer:
 
     def serve(self, requests: Sequence[Request], time_scale: float = 1.0) -> List[Request]:
         """Replay a stream: each request submitted at its arrival time (scaled);
-        a collector thread waits for the tickets in submission order and stamps
-        each request when its wait returns, so a request answered ahead of an
-        earlier one is stamped no later than that one's answer."""
+        a collector thread takes the requests as they finish (sed_server_next,
+        completion order) and stamps each when it is handed over."""
         self._t0 = time.perf_counter()
-        q: "queue.Queue" = queue.Queue()
+        by_ticket: Dict[int, Request] = {}
         done: List[Request] = []
+        lock = threading.Lock()
+        total = len(requests)
+        nev_max = max((r.nev for r in requests), default=1)
 
         def collect():
-            while True:
-                item = q.get()
-                if item is None:
-                    return
-                tk, r = item
-                done.append(self.wait(tk, r))
+            C = self._C
+            ev = np.zeros(nev_max, dtype=np.float64)
+            t, st, dim = C.c_int64(0), C.c_int32(0), C.c_int64(0)
+            lib = A._lib.load()
+            while len(done) < total:
+                rc = lib.sed_server_next(self._h, 200, C.byref(t), ev.ctypes.data, C.byref(st), C.byref(dim))
+                if rc == A._lib.SED_ERR_TIMEOUT:
+                    continue
+                A._lib.check(rc)
+                with lock:
+                    r = by_ticket.pop(t.value)
+                r.evals, r.status, r.dim, r.t_end = ev[: r.nev].copy(), st.value, dim.value, self._now()
+                if st.value != 0:
+                    r.error = lib.sed_last_error().decode()
+                r.route = "native"
+                done.append(r)
 
         th = threading.Thread(target=collect, daemon=True)
         th.start()
@@ -490,10 +502,9 @@ class NativeSectorServer:
             delay = arr - self._now()
             if delay > 0:
                 time.sleep(delay)
-            tk = self.submit(r)
-            r.arrival = arr
-            q.put((tk, r))
-        q.put(None)
+            with lock:
+                tk = self.submit(r)  # stamps the arrival
+                by_ticket[tk] = r
         th.join()
         return done
 
