@@ -688,6 +688,8 @@ def run_served(args):
         part["large_sm_limit"] = args.served_large_sms
     if args.served_ring_blocks:
         part["ring_blocks"] = args.served_ring_blocks
+    if args.served_large_krylovdim:
+        part["large_krylovdim"] = args.served_large_krylovdim
     line = served_report(args.served_n, args.served_rate, args.large_workers, plain_all=not args.plain_sampled,
                          plain_per_family=args.plain_per_family, partition=part, native=args.served_native)
     line["partition"] = part
@@ -721,6 +723,8 @@ def main():
                     help="served: catalogs up to this many orbits take the mid-size batch lane")
     ap.add_argument("--served-medium-batch", type=int, default=None,
                     help="served: requests (so SMs) of one mid-size batch launch")
+    ap.add_argument("--served-large-krylovdim", type=int, default=0,
+                    help="served: Krylov dimension of the device-wide solves (0: the server's default)")
     ap.add_argument("--served-ring-blocks", type=int, default=0,
                     help="served: batched families run a device-resident request loop on up to this many SMs")
     ap.add_argument("--served-native", action="store_true",

@@ -212,7 +212,9 @@ void sed_server::large_worker() {
       if (st == SED_OK) {
         sed_solve_info info{};
         std::vector<double> ev(r->nev);
-        st = sed_solve(op, r->nev, tol, 300, 0, r->seed, ev.data(), nullptr, &info);
+        // Krylov dimension 24: on the served mix's one-eigenvalue requests it
+        // took 3.5 % less device time than 30, and 40 took 10 % more
+        st = sed_solve(op, r->nev, tol, 300, 24, r->seed, ev.data(), nullptr, &info);
         if (st == SED_OK) {
           const int k = (int)std::min<int64_t>(r->nev, dim);
           for (int i = 0; i < k; ++i) r->evals[i] = ev[i];

@@ -149,7 +149,7 @@ class SectorServer:
                  medium_max_orbits: int = MEDIUM_MAX_ORBITS, medium_lanes: int = 1,
                  priority_max_orbits: int = PRIORITY_MAX_ORBITS, warm_up: bool = True,
                  medium_max_batch: int = MEDIUM_MAX_BATCH, large_sm_limit: int = 0, ring_blocks: int = 0,
-                 ring_idle_ms: int = 100):
+                 ring_idle_ms: int = 100, large_krylovdim: int = 24):
         self.budget = float(budget_bytes)
         # device-wide solves size their grids for this many SMs (0: all); the
         # mid-size lane's persistent blocks (at most medium_max_batch of them,
@@ -159,6 +159,9 @@ class SectorServer:
         # loop (sed_batch_ring_*) on up to that many SMs instead of batch
         # lanes; requests go straight into its ring
         self.ring_blocks = int(ring_blocks)
+        # Krylov dimension of the device-wide solves: 24 answered the served
+        # mix's one-eigenvalue requests 3.5 % faster than the library's 30
+        self.large_krylovdim = int(large_krylovdim)
         self.ring_idle_ms = int(ring_idle_ms)
         self.priority_max_orbits = priority_max_orbits
         self.precision = precision
@@ -327,7 +330,8 @@ class SectorServer:
                         H.set_priority(True)
                     if self.large_sm_limit > 0:
                         H.set_sm_limit(self.large_sm_limit)
-                    vals, _, info = H.solve(r.nev, tol=self.tol, seed=r.seed, want_vectors=False)
+                    vals, _, info = H.solve(r.nev, tol=self.tol, seed=r.seed, krylovdim=self.large_krylovdim,
+                                            want_vectors=False)
                     status, delta = 0, info.max_delta_polish
                     del H
                 r.evals, r.status, r.dim, r.delta_polish = np.asarray(vals), status, basis.dim, delta
