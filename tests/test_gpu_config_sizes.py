@@ -133,3 +133,33 @@ def test_configured_size_tables_rows_and_spectrum(oracle, name):
     Hm = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms(), spec.density_terms, precision="mixed")
     valsm, _, info = Hm.solve(nev, tol=1e-10, want_vectors=False)
     np.testing.assert_allclose(valsm, vals64, rtol=1e-9, atol=0, err_msg=name)
+
+
+def test_flux_scan_768_mixed_against_fp64():
+    """Config 4 at its stated size: the 768 sectors of the Haldane 3x4 flux
+    scan (12 momenta x 8 x 8 twists, about 11,200 rows each) in one mixed
+    launch and one FP64 launch.  Every sector's ground energy agrees within
+    the mixed path's 1e-9 relative, every request converges, and the zero-twist
+    k = (0, 0) sector gives the reference's stored E0 = -14.301456146831118
+    (benchmark_raw.csv:20-21) within 1e-11 in FP64."""
+    import realspace_exactdiagonalization_gb300.api as A
+    from realspace_exactdiagonalization_gb300 import lattice as L
+    from realspace_exactdiagonalization_gb300.batched import BatchedSectorSolver, flux_scan_requests
+
+    spec = L.haldane_honeycomb(3, 4)
+    twists = [(a / 8, b / 8) for a in range(8) for b in range(8)]
+    reqs = flux_scan_requests(spec, twists)
+    assert len(reqs) == 768
+    G = L.build_translation_group(spec.lattice)
+    cat = A.build_symmetry_orbit_catalog(n_filled=spec.n_filled, symmetry_group=G, particle_statistics=A.Bosonic())
+    pairs = [(i, j) for (i, j, _) in spec.bilinear_terms()]
+    out = {}
+    for prec in ("mixed", "fp64"):
+        s = BatchedSectorSolver(cat, pairs, spec.density_terms, precision=prec, nev=4, max_requests=768)
+        out[prec] = s.run(reqs)
+        assert (out[prec]["status"] == 0).all()
+    np.testing.assert_array_equal(out["mixed"]["dims"], out["fp64"]["dims"])
+    assert out["fp64"]["dims"].min() > 11000
+    e_mixed, e_fp64 = out["mixed"]["evals"][:, 0], out["fp64"]["evals"][:, 0]
+    np.testing.assert_allclose(e_mixed, e_fp64, rtol=1e-9, atol=0)
+    assert abs(e_fp64[0] - (-14.301456146831118)) <= 1e-11 * 14.3
