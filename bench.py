@@ -688,6 +688,7 @@ def run_served(args):
         part["large_sm_limit"] = args.served_large_sms
     if args.served_ring_blocks:
         part["ring_blocks"] = args.served_ring_blocks
+        part["ring_idle_ms"] = args.served_ring_idle_ms
     if args.served_large_krylovdim:
         part["large_krylovdim"] = args.served_large_krylovdim
     line = served_report(args.served_n, args.served_rate, args.large_workers, plain_all=not args.plain_sampled,
@@ -727,6 +728,8 @@ def main():
                     help="served: Krylov dimension of the device-wide solves (0: the server's default)")
     ap.add_argument("--served-ring-blocks", type=int, default=0,
                     help="served: batched families run a device-resident request loop on up to this many SMs")
+    ap.add_argument("--served-ring-idle-ms", type=int, default=2,
+                    help="served: idle time after which a device-resident loop's blocks leave")
     ap.add_argument("--served-native", action="store_true",
                     help="served: use the library's native server (sed_server_*) instead of the Python scheduler")
     ap.add_argument("--served-large-sms", type=int, default=0,

@@ -149,7 +149,7 @@ class SectorServer:
                  medium_max_orbits: int = MEDIUM_MAX_ORBITS, medium_lanes: int = 1,
                  priority_max_orbits: int = PRIORITY_MAX_ORBITS, warm_up: bool = True,
                  medium_max_batch: int = MEDIUM_MAX_BATCH, large_sm_limit: int = 0, ring_blocks: int = 0,
-                 ring_idle_ms: int = 100, large_krylovdim: int = 24):
+                 ring_idle_ms: int = 2, large_krylovdim: int = 24):
         self.budget = float(budget_bytes)
         # device-wide solves size their grids for this many SMs (0: all); the
         # mid-size lane's persistent blocks (at most medium_max_batch of them,
