@@ -360,16 +360,21 @@ int sed_batch_set_x_in_shared_memory(sed_batch* b, int enable);
  * popcounts).  Costs 8 bytes per hop of device memory; rebuilt when a run's
  * twist-phase classes differ from the last run's.  Runs whose group phases take
  * more than four distinct values per group element, or whose sectors leave no
- * shared memory for its coefficient tables, use the on-the-fly matvec. */
+ * shared memory for its coefficient tables, use the on-the-fly matvec.  The
+ * records of each row are reordered so that a warp's shared-memory gathers
+ * fall into different bank groups; SED_BATCH_BANK_ORDER=0 in the environment
+ * keeps them in enumeration order (only the rounding of each row's sum
+ * differs). */
 int sed_batch_set_hop_table(sed_batch* b, int enable);
 /* Launch shape of the batched solve (no counterpart in the reference): the
  * threads per row of the hop-table matvec (1, or 2 lanes splitting a row's
  * records) and the Krylov dimension of the thick-restart Lanczos.  By default
  * an autotuner times the candidates -- threads per row 1 and 2, and Krylov
  * dimensions 24, 20 and 28 when sed_batch_create got krylovdim 0 (else that
- * one) -- on one wave of the first run's requests per catalog shape, with
- * CUDA events on the batch stream (so that run waits on the host), and keeps
- * the fastest for the process.  SED_BATCH_SHAPE="krylovdim,threads_per_row"
+ * one) -- on one wave of the first run's requests per catalog shape, scoring
+ * each by its mean request time from the kernel's per-request device clocks
+ * (best of two trials; that run waits on the host), and keeps the fastest for
+ * the process.  SED_BATCH_SHAPE="krylovdim,threads_per_row"
  * in the environment or sed_batch_set_shape pins a shape ((0, 0) returns to
  * the autotuner; krylovdim at most 28 or the one given at creation).
  * sed_batch_shape reports the shape of the last run and how many autotuner
