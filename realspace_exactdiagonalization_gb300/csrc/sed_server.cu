@@ -357,8 +357,18 @@ int sed_server_add_family(sed_server* s, const sed_catalog* c, int n_bil, const 
         }
       }
     }
-    SED_REQUIRE(s->resident + resident <= s->budget, SED_ERR_NOMEM,
-                "resident catalogs and batch workspaces exceed the server's budget");
+    // the families vector may only change while no worker thread reads it:
+    // check and append under the lock that starts the workers
+    std::lock_guard<std::mutex> lock(s->mu);
+    const char* refuse = s->started ? "families must be added before the first request"
+                         : s->resident + resident > s->budget
+                             ? "resident catalogs and batch workspaces exceed the server's budget"
+                             : nullptr;
+    if (refuse) {
+      for (sed_batch* x : f.lanes) sed_batch_destroy(x);
+      delete f.cat;
+      SED_REQUIRE(false, s->started ? SED_ERR_ARG : SED_ERR_NOMEM, refuse);
+    }
     s->resident += resident;
     *family = (int32_t)s->families.size();
     s->families.push_back(std::move(f));
