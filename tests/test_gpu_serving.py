@@ -213,3 +213,38 @@ def test_served_mix_through_device_resident_loops(oracle):
         if sec.dim:
             e0 = np.linalg.eigvalsh(op.dense())[0]
             assert abs(r.evals[0] - e0) <= 1e-9 * max(1.0, abs(e0)), (r.rid, r.family, r.route)
+
+
+def test_native_server_refusals():
+    """The native server's refusals: an unknown ticket, sed_server_next on an
+    idle server (SED_ERR_TIMEOUT), a family registered after the first
+    request (SED_ERR_ARG), and an unknown family."""
+    import ctypes as C
+
+    from realspace_exactdiagonalization_gb300 import _lib
+    from realspace_exactdiagonalization_gb300.serving import NativeSectorServer, random_requests
+
+    fams = {"haldane2x4": L.haldane_honeycomb(2, 4)}
+    srv = NativeSectorServer(fams, budget_bytes=4e9, batch_lanes=1, large_workers=1, small_max_orbits=300)
+    lib = _lib.load()
+    try:
+        ev = np.zeros(1)
+        st, dim, t = C.c_int32(0), C.c_int64(0), C.c_int64(0)
+        assert lib.sed_server_wait(srv._h, 12345, 0, ev.ctypes.data, C.byref(st), C.byref(dim)) == _lib.SED_ERR_ARG
+        assert lib.sed_server_next(srv._h, 0, C.byref(t), ev.ctypes.data, C.byref(st), C.byref(dim)) == \
+            _lib.SED_ERR_TIMEOUT
+        r = random_requests(fams, 1, rate=0.0, seed=3, nev=1)[0]
+        ticket = srv.submit(r)
+        srv.wait(ticket, r)
+        assert r.status == 0 and r.dim > 0
+        cat = srv.catalogs["haldane2x4"]
+        bij = np.zeros(2, dtype=np.int32)
+        bt = np.zeros(1, dtype=np.complex128)
+        fid = C.c_int32(-1)
+        assert lib.sed_server_add_family(srv._h, cat.handle, 0, bij.ctypes.data, bt.ctypes.data, 0, None, None, 1,
+                                         C.byref(fid)) == _lib.SED_ERR_ARG
+        chi = np.ones(16, dtype=np.complex128)
+        assert lib.sed_server_submit(srv._h, 7, chi.ctypes.data, chi.ctypes.data, chi.ctypes.data, 1, 1,
+                                     C.byref(t)) == _lib.SED_ERR_ARG
+    finally:
+        srv.close()
