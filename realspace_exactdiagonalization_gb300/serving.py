@@ -22,6 +22,12 @@ Here a scheduler keeps the GPU busy with many requests at once:
   the GPU concurrently from one process.
 A request's result depends only on its own inputs and seed: the same request
 gives the same eigenvalues alone and in any mix.
+
+:class:`NativeSectorServer` runs the same scheduling in the library itself
+(``sed_server_*``: C++ threads behind the C ABI, the entry points a Julia
+service would call).  With ``ring_blocks > 0`` the batched families are
+answered by device-resident request loops (``sed_batch_ring_*``) instead of
+batch lanes.
 """
 from __future__ import annotations
 
