@@ -28,7 +28,6 @@ raises ``ValueError``.
 from __future__ import annotations
 
 import ctypes as C
-import itertools
 import math
 from typing import Dict, List, Optional, Sequence, Tuple
 

@@ -31,7 +31,6 @@ batch lanes.
 """
 from __future__ import annotations
 
-import math
 import queue
 import threading
 import time

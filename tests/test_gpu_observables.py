@@ -2,7 +2,6 @@
 answers: the projected position operator and the Fock-space overlaps, then
 the full Chern number and charge pump of the bosonic Haldane 2x3 model
 (doc/charge_pump.ipynb cells 5 and 7)."""
-import math
 
 import numpy as np
 import pytest

@@ -8,7 +8,6 @@ the twisted spectra and the Fock-space overlaps themselves."""
 import math
 
 import numpy as np
-import pytest
 
 from realspace_exactdiagonalization_gb300 import lattice as L
 
