@@ -17,7 +17,7 @@ import os
 import numpy as np
 import pytest
 
-from cases import Case, x_random
+from cases import Case, assert_lanczos_spectrum, x_random
 
 pytestmark = pytest.mark.gpu
 
@@ -184,3 +184,37 @@ def test_species_rejections():
                                                                        for i in range(n // 2)]
     with pytest.raises(_lib.SEDError, match="species"):
         A.MatrixFreeHamiltonian(basis, cross, [])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("name", ["hubbard2x4_4u4d_flux", "hubbard3x2_3u3d_flux"])
+def test_species_blocks_through_the_batch(oracle, name, precision):
+    """A two-species catalog through the batched solver (its site-gauge hop
+    table, bank-ordered records): every (momentum, twist) request gives the
+    block's sector dimension and the spectrum of the oracle's sector matrix
+    restricted to the block (Lanczos semantics, 1e-9)."""
+    from realspace_exactdiagonalization_gb300.batched import BatchedSectorSolver, flux_scan_requests
+
+    case = CASES[name]
+    twists = [(0.0, 0.0), (0.3, 0.1), (0.5, 0.75)]
+    reqs = flux_scan_requests(case.spec, twists)
+    pairs = [(i, j) for (i, j, _) in case.spec.bilinear_terms()]
+    solver = BatchedSectorSolver(_device_catalog(case), pairs, case.spec.density_terms, precision=precision, nev=3,
+                                 max_requests=64)
+    out = solver.run(reqs)
+    assert (out["status"] == 0).all()
+    assert solver.last_stats()["hop_table"]
+    nk = len(reqs) // len(twists)
+    for b in range(len(reqs)):
+        tcase = Case(name, case.spec, theta=twists[b // nk])
+        oc, keep = _restriction(oracle, tcase)
+        osec = oracle.Sector(oc, tcase.irreps()[b % nk].array())
+        _, _, oorb = osec.arrays()
+        rows = keep[oorb]
+        assert out["dims"][b] == int(rows.sum()), (name, b)
+        if not rows.any():
+            continue
+        Hb = oracle.Op(osec, tcase.bilinear0(), tcase.density0()).dense()[np.ix_(rows, rows)]
+        ref = np.linalg.eigvalsh(Hb)
+        k = min(3, int(rows.sum()))
+        assert_lanczos_spectrum(out["evals"][b, :k], ref, 1e-9 * max(1.0, abs(ref[0])), msg=f"{name} {b}")
