@@ -419,7 +419,11 @@ void sed_batch_destroy(sed_batch* b);
  * the site-gauge hop table, so every request's group must have a site gauge
  * (flux-twisted translation groups do; SED_ERR_ARG otherwise); a request
  * whose mixed-precision check failed is re-solved in FP64 when collected.
- * While the ring runs, sed_batch_run on the same object is refused. */
+ * While the ring runs, sed_batch_run on the same object is refused.  Unlike
+ * the other calls on one object, the ring calls are thread-safe among
+ * themselves: one thread may submit while others wait and another stops the
+ * ring (a wait then fails with "the ring was stopped"); a ticket is collected
+ * once, by whichever wait gets it first. */
 int sed_batch_ring_start(sed_batch* b, int capacity, int n_blocks, int idle_ms);
 /* SED_ERR_LIMIT when every slot holds a request not yet collected. */
 int sed_batch_ring_submit(sed_batch* b, const double* chi_reim, const double* group_phase_reim,

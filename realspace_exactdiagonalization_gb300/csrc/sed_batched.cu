@@ -2323,10 +2323,14 @@ struct BatchImpl {
     BatchArgs args{};
     BatchSmem L{};
     std::shared_ptr<BatchImpl> redo;  // FP64 batch for requests whose polish missed its target
-    // submit and wait may be called from different host threads (one
-    // submitting, one collecting): the host-side ring state is guarded
-    std::shared_ptr<std::mutex> mu = std::make_shared<std::mutex>();
   } ring;
+  // start, submit, wait, info and stop may be called from different host
+  // threads (one submitting, one collecting, one stopping): the host-side ring
+  // state is guarded by ring_mu, which outlives every ring, and ring_gen counts
+  // the rings started, so a waiter notices a stop (and a restart) between two
+  // of its polls
+  std::mutex ring_mu;
+  uint64_t ring_gen = 0;
   // the captured launch (queue reset + persistent kernel) and the launch
   // configuration it was captured for
   std::vector<unsigned char> graph_key;
@@ -3548,6 +3552,7 @@ static bool ring_running(BatchImpl& B) {
 }
 
 void batch_ring_start(BatchImpl& B, int cap, int n_blocks, int idle_ms) {
+  std::lock_guard<std::mutex> lock(B.ring_mu);
   SED_REQUIRE(!B.ring.on, 1, "the ring is already running");
   SED_REQUIRE(cap >= 1 && cap <= (1 << 20), 1, "ring capacity must be between 1 and 2^20");
   SED_REQUIRE(n_blocks >= 1, 1, "n_blocks must be positive");
@@ -3559,6 +3564,14 @@ void batch_ring_start(BatchImpl& B, int cap, int n_blocks, int idle_ms) {
   SED_CUDA(cudaStreamSynchronize(s));
   BatchImpl::Ring& r = B.ring;
   r = BatchImpl::Ring{};
+  // a failure below releases what was already allocated
+  struct Undo {
+    BatchImpl& B;
+    bool armed = true;
+    ~Undo() {
+      if (armed) B.ring_free();
+    }
+  } undo{B};
   r.cap = cap;
   r.spin = (int)std::max<int64_t>(1, (int64_t)idle_ms * 1000 / 20);  // 20 us per idle wait
   r.fp64 = B.precision == 0 ? 1 : 0;
@@ -3644,11 +3657,13 @@ void batch_ring_start(BatchImpl& B, int cap, int n_blocks, int idle_ms) {
   r.args = a;
   r.L = L;
   r.on = true;
+  ++B.ring_gen;
+  undo.armed = false;
 }
 
 int64_t batch_ring_submit(BatchImpl& B, const double* chi, const double* phase, const double* amp, uint64_t seed) {
   BatchImpl::Ring& r = B.ring;
-  std::lock_guard<std::mutex> lock(*r.mu);
+  std::lock_guard<std::mutex> lock(B.ring_mu);
   SED_REQUIRE(r.on, 1, "the ring is not running");
   SED_REQUIRE(chi && phase && (B.n_bil == 0 || amp), 1, "NULL argument");
   const GroupImpl& G = *B.cat->group;
@@ -3682,28 +3697,36 @@ bool batch_ring_wait(BatchImpl& B, int64_t ticket, int timeout_ms, double* evals
   BatchImpl::Ring& r = B.ring;
   const unsigned int q = (unsigned int)ticket;
   int slot = 0;
-  {
-    std::lock_guard<std::mutex> lock(*r.mu);
-    SED_REQUIRE(r.on, 1, "the ring is not running");
+  uint64_t gen = 0;
+  // the ticket is still this caller's to collect: same ring, issued, its slot
+  // not yet reused by a later ticket and not yet collected (mutex held)
+  auto check_ticket = [&] {
+    SED_REQUIRE(r.on && B.ring_gen == gen, 1, "the ring was stopped");
     SED_REQUIRE(ticket >= 0 && (uint64_t)ticket < (uint64_t)r.next &&
                     (uint64_t)r.next - (uint64_t)ticket <= (uint64_t)r.cap,
                 1, "unknown ticket");
     slot = (int)(q % (unsigned int)r.cap);
     SED_REQUIRE(r.busy[slot], 1, "ticket already collected");
+  };
+  {
+    std::lock_guard<std::mutex> lock(B.ring_mu);
+    SED_REQUIRE(r.on, 1, "the ring is not running");
+    gen = B.ring_gen;
+    check_ticket();
   }
   const auto t0 = std::chrono::steady_clock::now();
+  std::unique_lock<std::mutex> lock(B.ring_mu, std::defer_lock);
   for (;;) {
-    if (__atomic_load_n(r.done + slot, __ATOMIC_ACQUIRE) == q + 1) break;
-    {
-      // the blocks leave when idle; relaunch if this request is still queued
-      std::lock_guard<std::mutex> lock(*r.mu);
-      if (!ring_running(B) && __atomic_load_n(r.done + slot, __ATOMIC_ACQUIRE) != q + 1) ring_launch(B);
-    }
+    lock.lock();
+    check_ticket();
+    if (__atomic_load_n(r.done + slot, __ATOMIC_ACQUIRE) == q + 1) break;  // collected below, lock held
+    // the blocks leave when idle; relaunch if this request is still queued
+    if (!ring_running(B)) ring_launch(B);
+    lock.unlock();
     const double el = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (el >= timeout_ms) return false;
     std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
-  std::lock_guard<std::mutex> lock(*r.mu);
   int32_t st = r.status[slot];
   for (int i = 0; i < B.nev; ++i) evals[i] = r.evals[(size_t)slot * B.nev + i];
   int64_t d = r.dims[slot];
@@ -3734,6 +3757,7 @@ bool batch_ring_wait(BatchImpl& B, int64_t ticket, int timeout_ms, double* evals
 }
 
 void batch_ring_stop(BatchImpl& B) {
+  std::lock_guard<std::mutex> lock(B.ring_mu);
   SED_REQUIRE(B.ring.on, 1, "the ring is not running");
   B.ring_free();
 }
@@ -3904,6 +3928,7 @@ int sed_batch_ring_info(const sed_batch* b, int64_t* launches, int32_t* n_blocks
   return bguard([&] {
     SED_REQUIRE(b, 1, "NULL batch");
     sed::BatchImpl& B = *b->p;
+    std::lock_guard<std::mutex> lock(B.ring_mu);
     if (launches) *launches = B.ring.launches;
     if (n_blocks) *n_blocks = B.ring.n_cta;
     if (running) *running = B.ring.on && B.ring.stream && cudaStreamQuery(B.ring.stream) == cudaErrorNotReady;

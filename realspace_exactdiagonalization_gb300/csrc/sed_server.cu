@@ -379,6 +379,11 @@ int sed_server_submit(sed_server* s, int32_t family, const double* chi_reim, con
                       const double* bil_t_reim, uint64_t seed, int nev, int64_t* ticket) {
   return sguard([&] {
     SREQ(s && chi_reim && group_phase_reim && ticket, "NULL argument");
+    // the family table is read under the lock: sed_server_add_family may be
+    // appending to it from another thread until the first request starts the
+    // workers
+    std::lock_guard<std::mutex> lock(s->mu);
+    SREQ(!s->closed, "the server is closed");
     SREQ(family >= 0 && family < (int32_t)s->families.size(), "unknown family");
     const Family& f = s->families[family];
     SREQ(f.n_bil == 0 || bil_t_reim, "NULL bilinear amplitudes");
@@ -390,8 +395,6 @@ int sed_server_submit(sed_server* s, int32_t family, const double* chi_reim, con
     r->chi.assign(chi_reim, chi_reim + 2 * f.n_ops);
     r->phase.assign(group_phase_reim, group_phase_reim + 2 * (size_t)f.n_ops * f.n_site);
     if (f.n_bil) r->amp.assign(bil_t_reim, bil_t_reim + 2 * f.n_bil);
-    std::lock_guard<std::mutex> lock(s->mu);
-    SREQ(!s->closed, "the server is closed");
     r->ticket = s->next_ticket++;
     *ticket = r->ticket;
     Request* p = r.get();
@@ -406,11 +409,15 @@ int sed_server_wait(sed_server* s, int64_t ticket, int timeout_ms, double* evals
   return sguard([&] {
     SREQ(s && evals, "NULL argument");
     std::unique_lock<std::mutex> lock(s->mu);
-    auto it = s->requests.find(ticket);
-    SREQ(it != s->requests.end(), "unknown ticket (or already collected)");
-    Request* r = it->second.get();
-    const bool ready = s->done_cv.wait_for(lock, std::chrono::milliseconds(std::max(timeout_ms, 0)),
-                                           [&] { return r->done; });
+    SREQ(s->requests.count(ticket), "unknown ticket (or already collected)");
+    // the ticket is looked up again after every wake-up: another thread's
+    // sed_server_wait or sed_server_next may have collected it meanwhile
+    auto it = s->requests.end();
+    const bool ready = s->done_cv.wait_for(lock, std::chrono::milliseconds(std::max(timeout_ms, 0)), [&] {
+      it = s->requests.find(ticket);
+      return it == s->requests.end() || it->second->done;
+    });
+    SREQ(it != s->requests.end(), "ticket collected by another caller");
     SED_REQUIRE(ready, SED_ERR_TIMEOUT, "request not finished");
     s->collect(it, evals, status, dim);
   });

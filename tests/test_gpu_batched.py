@@ -444,6 +444,72 @@ def test_device_resident_request_loop(oracle, precision):
     assert (out["status"] == 0).all()
 
 
+def test_ring_calls_from_several_threads():
+    """The ring calls are thread-safe among themselves: two threads waiting on
+    one ticket get the answer once (the other: "already collected"); a stop
+    while another thread waits ends that wait with an error, or with the
+    answer if it came first; a ticket of a stopped ring is refused after a
+    restart; the restarted ring answers as before."""
+    import threading
+
+    from realspace_exactdiagonalization_gb300 import _lib
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.haldane_honeycomb(2, 4)
+    reqs = flux_scan_requests(spec, TWISTS)
+    ref = _solver(spec, "mixed").run(reqs[:8])
+    solver = _solver(spec, "mixed")
+    solver.ring_start(capacity=16, n_blocks=8, idle_ms=50)
+    try:
+        for i in range(3):
+            t = solver.ring_submit(reqs[i])
+            got, errs = [], []
+
+            def waiter():
+                try:
+                    got.append(solver.ring_wait(t, timeout_ms=60_000))
+                except _lib.SEDError as e:
+                    errs.append(str(e))
+
+            th = [threading.Thread(target=waiter) for _ in range(2)]
+            for x in th:
+                x.start()
+            for x in th:
+                x.join()
+            assert len(got) == 1 and len(errs) == 1 and "collected" in errs[0], (got, errs)
+            ev, st, dim = got[0]
+            assert st == 0 and dim == ref["dims"][i]
+            if dim:
+                np.testing.assert_allclose(ev[0], ref["evals"][i, 0], rtol=1e-9, atol=1e-12)
+        t = solver.ring_submit(reqs[3])
+        got, errs = [], []
+
+        def waiter2():
+            try:
+                got.append(solver.ring_wait(t, timeout_ms=60_000))
+            except _lib.SEDError as e:
+                errs.append(str(e))
+
+        w = threading.Thread(target=waiter2)
+        w.start()
+        solver.ring_stop()
+        w.join()
+        assert len(got) + len(errs) == 1
+        if errs:
+            assert "stopped" in errs[0] or "not running" in errs[0], errs
+        else:
+            assert got[0][1] == 0
+        solver.ring_start(capacity=16, n_blocks=8, idle_ms=50)
+        with pytest.raises(_lib.SEDError):
+            solver.ring_wait(t + 5, timeout_ms=0)
+        ev, st, dim = solver.ring_wait(solver.ring_submit(reqs[4]))
+        assert st == 0 and dim == ref["dims"][4]
+        if dim:
+            np.testing.assert_allclose(ev[0], ref["evals"][4, 0], rtol=1e-9, atol=1e-12)
+    finally:
+        solver.ring_stop()
+
+
 def test_gauge_only_phase_table_when_shared_memory_is_tight():
     """Checkerboard 4x4 with Np = 5 (12,586 orbits): its complex64 x fills so
     much shared memory that the full phase-id table (2048 entries) does not

@@ -248,3 +248,40 @@ def test_native_server_refusals():
                                      C.byref(t)) == _lib.SED_ERR_ARG
     finally:
         srv.close()
+
+
+def test_native_server_one_collector_per_ticket():
+    """Two threads waiting on one ticket at once (sed_server_wait from both):
+    exactly one receives the answer, the other SED_ERR_ARG; the server stays
+    usable."""
+    import ctypes as C
+    import threading
+
+    from realspace_exactdiagonalization_gb300 import _lib
+    from realspace_exactdiagonalization_gb300.serving import NativeSectorServer, random_requests
+
+    fams = {"haldane2x4": L.haldane_honeycomb(2, 4)}
+    srv = NativeSectorServer(fams, budget_bytes=4e9, batch_lanes=1, large_workers=1, small_max_orbits=300)
+    lib = _lib.load()
+    try:
+        for seed in range(3):
+            r = random_requests(fams, 1, rate=0.0, seed=20 + seed, nev=1)[0]
+            ticket = srv.submit(r)
+            rcs, evs = [None, None], [np.zeros(1), np.zeros(1)]
+
+            def waiter(i):
+                st, dim = C.c_int32(0), C.c_int64(0)
+                rcs[i] = lib.sed_server_wait(srv._h, ticket, 60_000, evs[i].ctypes.data, C.byref(st), C.byref(dim))
+
+            th = [threading.Thread(target=waiter, args=(i,)) for i in range(2)]
+            for t in th:
+                t.start()
+            for t in th:
+                t.join()
+            assert sorted(rcs) == [0, _lib.SED_ERR_ARG], rcs
+            assert np.isfinite(evs[rcs.index(0)][0])
+        r = random_requests(fams, 1, rate=0.0, seed=30, nev=1)[0]
+        srv.wait(srv.submit(r), r)
+        assert r.status == 0
+    finally:
+        srv.close()
