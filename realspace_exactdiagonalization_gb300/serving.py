@@ -366,7 +366,23 @@ class SectorServer:
         fam = self.families[r.family]
         if fam.name in self._ring_q:  # straight into the family's device-resident loop
             r.arrival = self._now()
-            ticket = fam.solvers[0].ring_submit(self._request_arrays(fam, [r])[0])
+            req = self._request_arrays(fam, [r])[0]
+            while True:
+                try:
+                    ticket = fam.solvers[0].ring_submit(req)
+                    break
+                except A._lib.SEDError as e:
+                    if e.code == A._lib.SED_ERR_LIMIT:
+                        # every slot awaits collection: the collector, which
+                        # takes the tickets in order, frees the oldest soon
+                        time.sleep(1e-4)
+                        continue
+                    with self._lock:  # refused: reported on the request, like the other routes
+                        r.status, r.evals, r.error = e.code, np.full(r.nev, np.nan), str(e)
+                        r.t_start, r.t_end, r.route = r.arrival, self._now(), "ring"
+                        self._done.append(r)
+                        self._lock.notify_all()
+                    return
             self._ring_q[fam.name].put((ticket, r))
             return
         with self._lock:
