@@ -331,3 +331,70 @@ def test_gather_launch_shapes_match_oracle(oracle, name, precision):
             assert H.apply_shape(precision == "mixed") == (tpr, block)
             assert np.abs(y - ref).max() <= tol * scale, (name, k, precision, tpr, block)
         H.set_apply_shape(0, 0)
+
+
+@pytest.mark.parametrize("spec_name,n_filled", [("ring16", 0), ("ring16", 16), ("checkerboard3x2_f_flux", 0),
+                                                ("checkerboard3x2_f_flux", 12), ("checkerboard3x2_b_flux", 12)])
+def test_empty_and_full_fillings(oracle, spec_name, n_filled):
+    """n_filled = 0 or n_site, the reference's special case (SRE:410-431: one
+    orbit whose stabilizer is the whole group): the catalog tables bit for bit,
+    every momentum sector's basis (the one orbit belongs to the sectors whose
+    characters match its stabilizer phases -- at flux, the product of the
+    twist phases over all sites), and in each non-empty sector the matvec and
+    the single eigenvalue against the oracle."""
+    import dataclasses
+
+    import realspace_exactdiagonalization_gb300.api as A
+
+    base = case_by_name(spec_name)
+    case = dataclasses.replace(base, name=f"{spec_name}_n{n_filled}",
+                               spec=dataclasses.replace(base.spec, n_filled=n_filled))
+    G = case.group()
+    oc = oracle.Catalog(G.perm0(), G.phases(), G.identity_idx - 1, case.stats_code, n_filled)
+    dc = _device(case)
+    assert dc.n_states == oc.n_states == 1 and dc.n_orbits == oc.n_orbits == 1
+    np.testing.assert_array_equal(dc.representative_mask_list, oc.get(oracle.FIELD_REPS))
+    np.testing.assert_array_equal(dc.stabilizer_order_list, oc.get(oracle.FIELD_STAB_ORDER))
+    np.testing.assert_array_equal(dc._get(3), oc.get(oracle.FIELD_STAB_G))
+    np.testing.assert_array_equal(bits(dc._get(4)), bits(oc.get(oracle.FIELD_STAB_PHASE)))
+    np.testing.assert_array_equal(dc.rep_rank_table, oc.get(oracle.FIELD_REP_RANK))
+    np.testing.assert_array_equal(dc.rep_sym_table, oc.get(oracle.FIELD_REP_SYM))
+    np.testing.assert_array_equal(bits(dc.rep_amp_table), bits(oc.get(oracle.FIELD_REP_AMP)))
+    nonempty = 0
+    for k, irr in enumerate(case.irreps()):
+        osec = oracle.Sector(oc, irr.array())
+        dsec = A.build_symmetry_sector_basis(dc, irr)
+        assert dsec.dim == osec.dim, (case.name, k)
+        if osec.dim == 0:
+            continue
+        nonempty += 1
+        np.testing.assert_array_equal(dsec.representative_mask_list, osec.arrays()[0])
+        op = oracle.Op(osec, case.bilinear0(), case.density0())
+        H = A.MatrixFreeHamiltonian(dsec, case.bilinear1(), case.density1(), None, precision="fp64")
+        x = np.array([0.6 - 0.8j])
+        y_ref = op.apply(x, mode=0)
+        assert abs(H(x)[0] - y_ref[0]) <= 1e-12 * max(1.0, abs(y_ref[0])), (case.name, k)
+        vals, _, _ = H.solve(1, tol=1e-10, seed=1, want_vectors=False)
+        e = np.linalg.eigvalsh(op.dense())[0]
+        assert abs(vals[0] - e) <= 1e-12 * max(1.0, abs(e)), (case.name, k)
+    assert nonempty >= 1
+    # the same one-orbit catalog through the batched solver (a hop table
+    # without records), mixed precision, every momentum at two twists
+    from realspace_exactdiagonalization_gb300.batched import BatchedSectorSolver, flux_scan_requests
+
+    twists = [(0.0, 0.0), (0.3, 0.1)]
+    reqs = flux_scan_requests(case.spec, twists)
+    pairs = [(i, j) for (i, j, _) in case.spec.bilinear_terms()]
+    solver = BatchedSectorSolver(dc, pairs, case.spec.density_terms, precision="mixed", nev=1, max_requests=64)
+    out = solver.run(reqs)
+    assert (out["status"] == 0).all()
+    nk = len(reqs) // len(twists)
+    for b in range(len(reqs)):
+        tcase = dataclasses.replace(case, theta=twists[b // nk])
+        _, osec, op = oracle_objects(oracle, tcase, b % nk)
+        assert out["dims"][b] == osec.dim, (case.name, b)
+        if osec.dim:
+            e = np.linalg.eigvalsh(op.dense())[0]
+            assert abs(out["evals"][b, 0] - e) <= 1e-10 * max(1.0, abs(e)), (case.name, b)
+        else:
+            assert np.isnan(out["evals"][b, 0])
