@@ -510,6 +510,29 @@ def test_ring_calls_from_several_threads():
         solver.ring_stop()
 
 
+@pytest.mark.parametrize("statistics", ["fermionic", "bosonic"])
+def test_flux_period_one(oracle, statistics):
+    """A whole flux quantum changes nothing but the momentum labels
+    (flux_regression.jl:53-60, global energies at twist 0 and 1 equal): the
+    batch at twists (0, 0) and (1, 0) gives the same multiset of sector
+    dimensions and of sector ground energies (1e-10), and every request at
+    twist (0.23, 0) in between the oracle's spectrum."""
+    from realspace_exactdiagonalization_gb300.batched import flux_scan_requests
+
+    spec = L.checkerboard(3, 2, n_filled=4, statistics=statistics)
+    twists = [(0.0, 0.0), (0.23, 0.0), (1.0, 0.0)]
+    out = _solver(spec, "mixed").run(flux_scan_requests(spec, twists))
+    assert (out["status"] == 0).all()
+    _assert_oracle_spectra(oracle, f"checkerboard3x2_{statistics}", spec, twists, out)
+    nk = len(out["dims"]) // len(twists)
+    d0, d1 = out["dims"][:nk], out["dims"][2 * nk:]
+    np.testing.assert_array_equal(np.sort(d0), np.sort(d1))
+    e0 = np.sort(out["evals"][:nk, 0][d0 > 0])
+    e1 = np.sort(out["evals"][2 * nk:, 0][d1 > 0])
+    np.testing.assert_allclose(e1, e0, rtol=0, atol=1e-10 * max(1.0, np.abs(e0).max()))
+    assert np.abs(out["evals"][nk:2 * nk, 0][out["dims"][nk:2 * nk] > 0].min() - e0.min()) > 1e-6  # the twist matters
+
+
 def test_gauge_only_phase_table_when_shared_memory_is_tight():
     """Checkerboard 4x4 with Np = 5 (12,586 orbits): its complex64 x fills so
     much shared memory that the full phase-id table (2048 entries) does not
