@@ -22,7 +22,9 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <mutex>
 
+#include "../../include/sed_capi.h"
 #include "sed_dfloat.cuh"
 #include "sed_internal.cuh"
 
@@ -391,10 +393,11 @@ __global__ void __launch_bounds__(kBS) k_cf_norm2_part(int64_t n, const float2* 
 // part[l*nblk + b] = block b's share of conj(V_l) w for the kDotCh vectors of
 // chunk blockIdx.y: w is read once per kDotCh basis vectors.  Each thread
 // takes two consecutive elements per step (16-byte loads; vectors start on
-// 512-byte boundaries), the last one of an odd n by thread 0 of block 0.  The
-// sweep relies on the threads' own loads: a bulk L2 prefetch ahead of them
-// measured slower here (3.6 against 5.9 TB/s for 24 vectors of 14.1M
-// elements).
+// 512-byte boundaries), the last one of an odd n by thread 0 of block 0.  A
+// bulk L2 prefetch ahead of the threads' loads measured slower here (3.6
+// against 5.9 TB/s for 24 vectors of 14.1M elements); vectors of 2^18
+// elements and more are staged through shared memory instead
+// (k_cf_multidot_tma below), and this kernel serves the shorter ones.
 static constexpr int kDotCh = 16;
 __device__ __forceinline__ void cf_dot_acc(float& re, float& im, float2 v, float2 x) {
   re = __fmaf_rn(v.x, x.x, __fmaf_rn(v.y, x.y, re));
@@ -432,6 +435,137 @@ __global__ void __launch_bounds__(kBS) k_cf_multidot(int64_t n, const float2* __
     }
 }
 
+
+// The same dot products with the vectors staged through shared memory by the
+// bulk-copy (TMA) engine.  Each block takes tiles of `tile` elements (a grid
+// stride over the tiles); for every tile, lanes 0..cn of warp 0 copy w and the
+// chunk's cn vectors into one of two shared-memory stages with
+// cp.async.bulk, completing on the stage's mbarrier, while the block reads
+// the other stage.  The copy engine keeps a whole stage in flight per SM, which
+// the register-held loads of k_cf_multidot cannot: on 4.0M-element vectors a
+// 14-vector pass took 111 against 138 us, the two-vector local pass 32 against
+// 43 us.  Requirements (checked by the caller): ld a multiple of 64 elements
+// and V, w 16-byte aligned, so every copy starts on a 512-byte boundary and
+// moves a multiple of 512 bytes; the elements in [n, ld) are read but not used.
+// Every wait is bounded: a stage that does not complete within kTmaSpin polls
+// sets *err, the block waits (bounded) for its copies still in flight and
+// leaves without writing its partials.
+static constexpr int kTmaStages = 2;
+static constexpr size_t kTmaSmemBudget = 208000;  // bytes of staging per block (one block per SM)
+static constexpr int kTmaMinN = 1 << 18;           // below this, too few tiles per block to pipeline
+static constexpr uint32_t kTmaSpin = 1u << 26;
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// true when the phase of the given parity completed within kTmaSpin polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+  for (uint32_t it = 0; it < kTmaSpin; ++it)
+    if (mbar_try_wait(b, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(b))
+               : "memory");
+}
+// tile (elements, a multiple of 256) for a chunk of cn vectors plus w
+static inline int tma_tile(int cn) {
+  const int t = (int)(kTmaSmemBudget / ((size_t)kTmaStages * (cn + 1) * 8)) / 256 * 256;
+  return std::max(256, std::min(t, 8192));
+}
+static inline size_t tma_smem(int cn, int tile) { return 128 + (size_t)kTmaStages * (cn + 1) * tile * 8; }
+
+__global__ void __launch_bounds__(kBS, 1) k_cf_multidot_tma(int64_t n, const float2* __restrict__ V, int64_t ld,
+                                                            int nv, const float2* __restrict__ w,
+                                                            double2* __restrict__ part, int tile,
+                                                            const int* __restrict__ skip, int* __restrict__ err) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);    // kTmaStages barriers
+  float2* stage = reinterpret_cast<float2*>(smem + 128);  // [kTmaStages][cn + 1][tile]
+  __shared__ int s_fail;
+  const int l0 = blockIdx.y * kDotCh;
+  const int cn = min(kDotCh, nv - l0);
+  const int64_t n_tiles = (ld + tile - 1) / tile;
+  const int64_t my_tiles = blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const size_t stage_el = (size_t)(cn + 1) * tile;
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    for (int s = 0; s < kTmaStages; ++s) mbar_init(&bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  // warp 0: lane 0 arms the stage's barrier with the tile's bytes, then lane
+  // c copies slot c (0: w, c > 0: vector l0 + c - 1)
+  auto issue = [&](int64_t i) {
+    const int s = (int)(i % kTmaStages);
+    const int64_t e0 = (blockIdx.x + i * gridDim.x) * (int64_t)tile;
+    const uint32_t bytes = (uint32_t)(min((int64_t)tile, ld - e0) * 8);
+    if (lane == 0) mbar_expect_tx(&bar[s], bytes * (uint32_t)(cn + 1));
+    __syncwarp();
+    if (lane <= cn)
+      bulk_g2s(stage + (size_t)s * stage_el + (size_t)lane * tile,
+               lane == 0 ? w + e0 : V + (size_t)(l0 + lane - 1) * ld + e0, bytes, &bar[s]);
+  };
+  if (threadIdx.x < 32)
+    for (int64_t i = 0; i < kTmaStages && i < my_tiles; ++i) issue(i);
+  float re[kDotCh], im[kDotCh];
+#pragma unroll
+  for (int c = 0; c < kDotCh; ++c) re[c] = im[c] = 0.f;
+  int64_t i = 0;
+  for (; i < my_tiles; ++i) {
+    const int s = (int)(i % kTmaStages);
+    if (!mbar_wait(&bar[s], (uint32_t)((i / kTmaStages) & 1))) atomicExch(&s_fail, 1);
+    __syncthreads();
+    if (s_fail) break;
+    const int64_t e0 = (blockIdx.x + i * gridDim.x) * (int64_t)tile;
+    const float2* st = stage + (size_t)s * stage_el;
+    for (int q = threadIdx.x; q < tile / 2; q += kBS) {  // element pairs
+      const int64_t e = e0 + 2 * q;
+      const float4 x = reinterpret_cast<const float4*>(st)[q];
+      const bool ok0 = e < n, ok1 = e + 1 < n;
+#pragma unroll
+      for (int c = 0; c < kDotCh; ++c)
+        if (c < cn) {
+          const float4 v = reinterpret_cast<const float4*>(st + (size_t)(c + 1) * tile)[q];
+          if (ok0) cf_dot_acc(re[c], im[c], make_float2(v.x, v.y), make_float2(x.x, x.y));
+          if (ok1) cf_dot_acc(re[c], im[c], make_float2(v.z, v.w), make_float2(x.z, x.w));
+        }
+    }
+    __syncthreads();  // the block is done with stage s: refill it
+    if (threadIdx.x < 32 && i + kTmaStages < my_tiles) issue(i + kTmaStages);
+  }
+  if (s_fail) {
+    if (threadIdx.x == 0) {
+      atomicExch(err, 1);
+      for (int64_t j = i; j < my_tiles && j < i + kTmaStages; ++j)
+        mbar_wait(&bar[j % kTmaStages], (uint32_t)((j / kTmaStages) & 1));
+    }
+    __syncthreads();
+    return;
+  }
+#pragma unroll
+  for (int c = 0; c < kDotCh; ++c)
+    if (c < cn) {
+      const double2 r = block_sum2((double)re[c], (double)im[c]);
+      if (threadIdx.x == 0) part[(size_t)(l0 + c) * gridDim.x + blockIdx.x] = r;
+    }
+}
 
 // w -= sum_l c_l V_l, each FP64 coefficient applied as hi + lo floats;
 // optionally the block partial of |w|^2.  skip: the device flag of the
@@ -635,11 +769,11 @@ namespace {
 
 struct VecOps {
   int64_t n;
-  int nblk, nblk_dot;
+  int nblk, nblk_dot, sms;
   cudaStream_t s;
-  DevBuf part, part1, coef, scal, flag;  // partial sums, coefficients, scalars, skip flag
+  DevBuf part, part1, coef, scal, flag, err;  // partial sums, coefficients, scalars, skip flag, wait-timeout flag
   double* host = nullptr;          // pinned scratch
-  VecOps(int64_t n_, cudaStream_t s_, int sms_) : n(n_), s(s_) {
+  VecOps(int64_t n_, cudaStream_t s_, int sms_) : n(n_), sms(sms_), s(s_) {
     const int64_t sms = sms_;
     nblk = (int)std::max<int64_t>(1, std::min<int64_t>((n + kBS * 4 - 1) / (kBS * 4), sms * 4));
     // the complex64 dot kernel's grid is one full wave of its resident blocks
@@ -652,6 +786,8 @@ struct VecOps {
     coef.alloc(256 * 16);
     scal.alloc(64);
     flag.alloc(16);
+    err.alloc(16);
+    SED_CUDA(cudaMemsetAsync(err.p, 0, 16, s));
     SED_CUDA(cudaMallocHost((void**)&host, 4096));
   }
   ~VecOps() {
@@ -672,8 +808,33 @@ struct VecOps {
     k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), nblk, coef.as<double2>() + off, acc ? 1 : 0);
   }
   void multidot(const float2* V, int64_t ld, int nv, const float2* w, int off, bool acc) {
-    k_cf_multidot<<<dim3(nblk_dot, (nv + kDotCh - 1) / kDotCh), kBS, 0, s>>>(n, V, ld, nv, w, part.as<double2>());
+    const dim3 grid_y(1, (nv + kDotCh - 1) / kDotCh);
+    if (n >= kTmaMinN && ld % 64 == 0 && ((uintptr_t)V | (uintptr_t)w) % 16 == 0) {
+      // vectors staged through shared memory by the bulk-copy engine
+      const int tile = tma_tile(std::min(kDotCh, nv));
+      // one block per SM, at most as many as the partial-sum buffer holds
+      const int g = (int)std::min<int64_t>({(ld + tile - 1) / tile, (int64_t)sms, (int64_t)std::max(nblk, nblk_dot)});
+      {
+        // every chunk's footprint is within 128 + kTmaSmemBudget bytes
+        static std::mutex mu;
+        static SmemOptIn optin;
+        std::lock_guard<std::mutex> lock(mu);
+        optin.ensure(k_cf_multidot_tma, 128 + kTmaSmemBudget);
+      }
+      k_cf_multidot_tma<<<dim3(g, grid_y.y), kBS, tma_smem(std::min(kDotCh, nv), tile), s>>>(
+          n, V, ld, nv, w, part.as<double2>(), tile, nullptr, err.as<int>());
+      k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), g, coef.as<double2>() + off, acc ? 1 : 0);
+      return;
+    }
+    k_cf_multidot<<<dim3(nblk_dot, grid_y.y), kBS, 0, s>>>(n, V, ld, nv, w, part.as<double2>());
     k_reduce_part2<<<nv, kBS, 0, s>>>(part.as<double2>(), nblk_dot, coef.as<double2>() + off, acc ? 1 : 0);
+  }
+  // a bounded wait of the staged dot kernel ran out (its partials are not valid)
+  bool timed_out() {
+    int e = 0;
+    SED_CUDA(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, s));
+    SED_CUDA(cudaStreamSynchronize(s));
+    return e != 0;
   }
   // w -= V[0..nv) coef[off..], optionally scal[slot] = |w|^2
   // (skip: device flag of the selective reorthogonalisation, complex64 only)
@@ -999,6 +1160,7 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
         // the complex64 run cannot resolve these levels to the target (e.g.
         // a gap below its noise floor): answer with a full FP64 solve instead
         // of returning an unconverged pair
+        SED_REQUIRE(!ops.timed_out(), SED_ERR_TIMEOUT, "a bounded wait of the staged dot kernel ran out");
         const int mv32 = res.matvecs, mv64 = res.matvecs64, rs = res.restarts;
         op.precision = 0;
         SolveResult r64;
@@ -1027,6 +1189,9 @@ SolveResult solve(OpImpl& op, int nev_out, double tol, int maxiter, int krylovdi
     k = keep;
     ++res.restarts;
   }
+  // a staged dot pass whose bounded wait ran out left partial sums that are
+  // not valid
+  SED_REQUIRE(!ops.timed_out(), SED_ERR_TIMEOUT, "a bounded wait of the staged dot kernel ran out");
 
   for (int i = 0; i < nev_out; ++i) evals_out[i] = evals[i];
   if (evecs) {
