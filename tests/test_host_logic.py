@@ -1,7 +1,8 @@
 """Host-side arithmetic behind reported numbers (no GPU): the roofline's
 Lanczos byte count follows the thick-restart schedule the kernels run, and the
 served scheduler's device-memory estimate covers what a device-wide mixed
-solve allocates."""
+solve allocates, and the served scheduler's ring route handles a full ring and
+a refused request."""
 import os
 import sys
 
@@ -56,3 +57,53 @@ def test_solver_footprint_covers_the_allocations():
             alloc = (2 * max(m + 1, 3 * nw + 1) + 1) * ldc * 8 + (5 * nw) * n * 16 + 2 * ldc * 16
             assert solver_footprint(n, nev) >= alloc, (n, nev)
             assert solver_footprint(n, nev + 1) > solver_footprint(n, nev)
+
+
+def test_ring_route_waits_for_a_slot_and_reports_refusals_per_request():
+    """SectorServer.submit on a family served by a device-resident ring: a full
+    ring (SED_ERR_LIMIT) is a wait for the collector, not a failure; any other
+    refusal is reported on the request itself (status, NaN evals, message), as
+    the other routes report theirs, and the stream goes on.  Host logic only:
+    the ring is a fake."""
+    import queue
+    import threading
+    import time
+    from types import SimpleNamespace
+
+    import numpy as np
+
+    from realspace_exactdiagonalization_gb300 import _lib
+    from realspace_exactdiagonalization_gb300.serving import Request, SectorServer
+
+    class FakeRing:
+        def __init__(self, outcomes):
+            self.outcomes = list(outcomes)  # SED_* codes to raise, then tickets
+            self.calls = 0
+
+        def ring_submit(self, req):
+            self.calls += 1
+            o = self.outcomes.pop(0)
+            if isinstance(o, int) and o < 0:
+                raise _lib.SEDError(-o, f"refused with {-o}")
+            return o
+
+    srv = object.__new__(SectorServer)  # no catalogs or device state: only the submit path
+    srv._t0 = time.perf_counter()
+    srv._lock = threading.Condition()
+    srv._done = []
+    srv._request_arrays = lambda fam, reqs: [None for _ in reqs]
+    ring = FakeRing([-_lib.SED_ERR_LIMIT, -_lib.SED_ERR_LIMIT, 7, -_lib.SED_ERR_ARG, 8])
+    srv.families = {"ring20": SimpleNamespace(name="ring20", solvers=[ring])}
+    srv._ring_q = {"ring20": queue.Queue()}
+
+    r1 = Request(rid=1, family="ring20", k_index=0, twist=(0.0, 0.0))
+    srv.submit(r1)  # two full-ring refusals, then ticket 7
+    assert ring.calls == 3 and srv._ring_q["ring20"].get_nowait() == (7, r1) and not srv._done
+    r2 = Request(rid=2, family="ring20", k_index=0, twist=(0.0, 0.0), nev=2)
+    srv.submit(r2)  # refused outright: reported on the request
+    assert srv._done == [r2] and r2.status == _lib.SED_ERR_ARG and r2.route == "ring"
+    assert np.isnan(r2.evals).all() and len(r2.evals) == 2 and "refused" in r2.error
+    assert srv._ring_q["ring20"].empty()
+    r3 = Request(rid=3, family="ring20", k_index=0, twist=(0.0, 0.0))
+    srv.submit(r3)  # the stream goes on
+    assert srv._ring_q["ring20"].get_nowait() == (8, r3)
