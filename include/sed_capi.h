@@ -282,7 +282,10 @@ void sed_op_destroy(sed_op* op);
  * at most its width); request SED_PREC_FP64 for spectra with such clusters.
  * The first gather matvec of an operator (when it has no hop table) times
  * eight launch shapes and waits on the host for them; later solves of the same
- * catalog shape reuse the choice (see sed_op_set_apply_shape). */
+ * catalog shape reuse the choice (see sed_op_set_apply_shape).  Mixed solves of
+ * sectors with 2^18 orbits or more stage their dot products through shared
+ * memory with bulk copies, under bounded waits: a wait that runs out makes the
+ * call return SED_ERR_TIMEOUT rather than a result. */
 int sed_solve(sed_op* op, int nev, double tol, int maxiter, int krylovdim, uint64_t seed, double* evals,
               double* evecs_reim, sed_solve_info* info);
 
