@@ -398,3 +398,25 @@ def test_empty_and_full_fillings(oracle, spec_name, n_filled):
             assert abs(out["evals"][b, 0] - e) <= 1e-10 * max(1.0, abs(e)), (case.name, b)
         else:
             assert np.isnan(out["evals"][b, 0])
+
+
+def test_mixed_solve_on_an_odd_large_catalog():
+    """A mixed-precision solve whose catalog is large enough for the staged
+    (bulk-copy) dot sweeps and has an odd orbit count, so the last element of
+    every vector sits alone in its pair: ring29 with 13 hard-core bosons
+    (C(29,13)/29 = 2,340,135 orbits), momentum 0.  The lowest eigenvalues agree
+    with the FP64 solve within the mixed path's 1e-9 relative."""
+    import realspace_exactdiagonalization_gb300.api as A
+    import realspace_exactdiagonalization_gb300.lattice as L
+
+    spec = L.ring_xxz(29, 1.0, 2.0, n_filled=13)
+    G = L.build_translation_group(spec.lattice)
+    cat = A.build_symmetry_orbit_catalog(n_filled=13, symmetry_group=G, particle_statistics=A.Bosonic())
+    assert cat.n_orbits == 2340135 and cat.n_orbits % 2 == 1
+    basis = A.build_symmetry_sector_basis(cat, L.build_translation_irrep_list(G, spec.lattice)[0])
+    vals = {}
+    for prec in ("fp64", "mixed"):
+        H = A.MatrixFreeHamiltonian(basis, spec.bilinear_terms(), spec.density_terms, precision=prec)
+        vals[prec], _, info = H.solve(3, tol=1e-10, want_vectors=False)
+        del H
+    np.testing.assert_allclose(vals["mixed"], vals["fp64"], rtol=1e-9, atol=0)
